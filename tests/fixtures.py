@@ -1,0 +1,48 @@
+"""Loading the golden vectors of tests/golden/ and comparing states."""
+import glob
+import os
+
+import numpy as np
+
+from picpp_gb300 import initstate as I
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden_names(prefix=""):
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, prefix + "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    nx, ny, nz = (int(v) for v in z["box"])
+    dx, dy, dz, dt, theta, eta, cfix = (float(v) for v in z["params"])
+    box = I.Box(nx, ny, nz, dx, dy, dz, dt, theta, eta, cfix)
+    species, out = [], []
+    for s in range(int(z["nspecies"])):
+        q, m, w = (float(v) for v in z[f"s{s}_qmw"])
+        sp = dict(q=q, m=m, w=w)
+        for k in ("cell", "ox", "oy", "oz", "px", "py", "pz"):
+            sp[k] = z[f"s{s}_{k}"].copy()
+        species.append(sp)
+        out.append({k: z[f"s{s}_out_{k}"].copy() for k in ("x", "y", "z", "px", "py", "pz")})
+    st = I.State(box, species, z["E0"].copy(), z["B0"].copy())
+    extra = {k[2:]: z[k].copy() for k in z.files if k.startswith("x_")}
+    return dict(state=st, solver=int(z["solver"]), steps=int(z["steps"]), out=out,
+                E=z["E"].copy(), B=z["B"].copy(), extra=extra)
+
+
+def copy_species(species):
+    return [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()} for s in species]
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(a - b))) / scale
+
+
+def periodic_dist(a, b, L):
+    d = np.asarray(a) - np.asarray(b)
+    return np.abs((d + L / 2) % L - L / 2)

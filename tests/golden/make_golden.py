@@ -1,0 +1,74 @@
+"""Generates the golden vectors in this directory from the PIC++ reference.
+
+Each case builds a seeded initial state (picpp_gb300.initstate), runs the
+reference -- compiled from its own sources by oracle/Makefile and driven by
+oracle/ref/harness.cpp -- and stores inputs and outputs in one .npz.  The
+reference tree is needed to run this script; the fixtures it writes are what
+the tests read on machines without it.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import pyoracle as O  # noqa: E402
+from picpp_gb300 import initstate as I  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _noise(st, amp, seed):
+    rng = np.random.default_rng(seed)
+    st.E = st.E + amp * rng.standard_normal(st.E.shape)
+    st.B = st.B + amp * rng.standard_normal(st.B.shape)
+    return st
+
+
+def _save(name, solver, st, steps, out_sp, E, B, extra):
+    d = dict(solver=solver, steps=steps,
+             box=np.array([st.box.nx, st.box.ny, st.box.nz]),
+             params=np.array([st.box.dx, st.box.dy, st.box.dz, st.box.dt, st.box.theta, st.box.eta, st.box.cfix]),
+             E0=st.E, B0=st.B, E=E, B=B, nspecies=len(st.species))
+    for s, (sp, o) in enumerate(zip(st.species, out_sp)):
+        d[f"s{s}_qmw"] = np.array([sp["q"], sp["m"], sp["w"]])
+        for k in ("cell", "ox", "oy", "oz", "px", "py", "pz"):
+            d[f"s{s}_{k}"] = sp[k]
+        for k in ("x", "y", "z", "px", "py", "pz"):
+            d[f"s{s}_out_{k}"] = o[k]
+    for k, v in extra.items():
+        d[f"x_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print("wrote", name)
+
+
+def buneman(name, nx, ny, nz, ppc, steps, seed):
+    st = _noise(I.buneman_plasma(nx, ny, nz, ppc=ppc, seed=seed), 0.05, seed + 100)
+    out_sp, E, B, extra = O.run_reference(0, st.box, st.species, st.E, st.B, steps)
+    _save(name, 0, st, steps, out_sp, E, B, extra)
+
+
+def implicit(name, nx, ny, nz, ppc, steps, seed, beam_gamma=2.0, dt=0.2):
+    st = _noise(I.beams_plasma(nx, ny, nz, ppc=ppc, beam_gamma=beam_gamma, dt=dt, seed=seed), 0.05, seed + 100)
+    out_sp, E, B, extra = O.run_reference(1, st.box, st.species, st.E, st.B, steps, dump=True)
+    _save(name, 1, st, steps, out_sp, E, B, extra)
+
+
+def main():
+    if not O.reference_available():
+        sys.exit("the PIC++ reference tree is not available here")
+    buneman("buneman_8x8x8_3steps", 8, 8, 8, 2, 3, 11)
+    buneman("buneman_12x6x5_2steps", 12, 6, 5, 3, 2, 12)
+    buneman("buneman_2d_16x8x1_3steps", 16, 8, 1, 4, 3, 13)
+    implicit("implicit_6x5x7_1step", 6, 5, 7, 2, 1, 21)
+    implicit("implicit_8x8x8_3steps", 8, 8, 8, 2, 3, 22)
+    implicit("implicit_gamma10_6x6x6_2steps", 6, 6, 6, 2, 2, 23, beam_gamma=10.0, dt=0.5)
+
+
+if __name__ == "__main__":
+    main()

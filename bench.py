@@ -1,0 +1,310 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 PIC hot path (one JSON line on rank 0).
+
+Workload (default): the explicit Buneman/Tristan Yee step on a periodic
+128^3 box, electron-proton plasma (mass ratio 100), 16 particles per cell per
+species (67,108,864 particles), dx = 0.1, Courant 0.45, theta_e = 0.1,
+theta_p = 1e-3, B0 along x with sigma = 0.1; FP32 particles (cell index +
+offset) and Yee fields, FP64 current.  A step is one full explicit step:
+B half step, fused gather/push/zigzag deposit, B half step, current
+assembly, E step, plus the cell sort when it is due.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Multi-GPU runs are independent replicas (one per rank, no collective on the
+data path); the value is the sum over ranks of particle-steps/s computed
+from the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s/GPU; implicit-solve time to 1e-8 residual, learned vs plain"
+UNIT = "particle-steps/s"
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--grid", type=int, nargs=3, default=[128, 128, 128])
+    p.add_argument("--ppc", type=int, default=16)
+    p.add_argument("--sort-every", type=int, default=4)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- CPU side
+def _oracle_worker(args):
+    """One replica of the oracle on a bounded sample box (spawned process)."""
+    nx, ny, nz, ppc, steps, seed = args
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from picpp_gb300 import initstate as I
+    st = I.buneman_plasma(nx, ny, nz, ppc=ppc, seed=seed)
+    g = O.make_grid(st.box)
+    sp = st.species
+    E, B = st.E.copy(), st.B.copy()
+    O.buneman_step(g, sp, E, B)   # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.buneman_step(g, sp, E, B)
+    dt = time.perf_counter() - t0
+    return sum(len(s["cell"]) for s in sp) * steps, dt
+
+
+def cpu_baseline(ppc, procs=1, target_s=10.0):
+    """The oracle (plain-C restatement of the reference) on a 16^3 sample box
+    with the workload's ppc and physics; procs independent replicas."""
+    import multiprocessing as mp
+    sample = (16, 16, 16, ppc)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        n, dt = pool.apply(_oracle_worker, ((*sample, 2, 11),))
+    per_step = dt / 2
+    steps = max(2, int(target_s / max(per_step, 1e-3)))
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_oracle_worker, [(*sample, steps, 100 + r) for r in range(procs)])
+    total = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    desc = f"{procs} replica(s) of a 16x16x16 box, {ppc} ppc x 2 species, {steps} steps each"
+    return total / wall, desc, steps
+
+
+def run_reference(a):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    t0 = time.perf_counter()
+    vals = []
+    for _ in range(a.warmup):
+        cpu_baseline(a.ppc, procs, target_s=2.0)
+    for _ in range(a.steps):
+        v, desc, steps = cpu_baseline(a.ppc, procs, target_s=2.0)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": _config(a),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _config(a):
+    nx, ny, nz = a.grid
+    n = nx * ny * nz * a.ppc * 2
+    return {"workload": f"buneman_yee_{nx}x{ny}x{nz}_{a.ppc}ppc_2species", "grid": [nx, ny, nz],
+            "ppc_per_species": a.ppc, "species": 2, "particles": n, "mass_ratio": 100,
+            "dx": 0.1, "courant": 0.45, "precision": "fp32 particles and Yee fields, fp64 current",
+            "sort_every": a.sort_every, "parallelism": f"replicas x{a.gpus}",
+            "l2_policy": "inputs larger than L2 (particle state 1.9 GB per GPU)"}
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    def __init__(self, index):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in open(self.path):
+            f = [x.strip() for x in row.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1].split()[0]))
+                smax.append(float(f[2].split()[0]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- GPU side
+def run_gb300(a):
+    import numpy as np
+    import torch
+    import picpp_gb300 as P
+    from picpp_gb300 import initstate as I
+
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    P.load_library()
+    nx, ny, nz = a.grid
+    st = I.buneman_plasma(nx, ny, nz, ppc=a.ppc, seed=2 + rank)
+    npart = sum(len(s["cell"]) for s in st.species)
+    sim = P.GpuSimulation(st.box, P.BUNEMAN, particle_real=P.F32, sort_every=a.sort_every)
+    sim.upload_state(st)
+    stream = torch.cuda.ExternalStream(sim.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    sim.buneman_step(a.warmup)
+    barrier()
+    clocks = Clocks(local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.buneman_step(a.steps)
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / a.steps
+    value = npart * world / (ms_step * 1e-3)
+
+    # phase breakdown of the same workload, a separate profiled pass
+    sim.profile(True)
+    sim.buneman_step(a.steps)
+    phases, launches = sim.profile(False)
+    launches_per_step = launches / a.steps
+    push_ms = phases["push_deposit"] / a.steps
+    N = nx * ny * nz
+    alg_bytes = 56 * npart + 24 * N   # particles r+w (28 B each way) + E,B gather (FP32) once per cell
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (push_ms * 1e-3) / 1e9
+    roof = {"kernel": "k_push_deposit_tile<float,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_source": "measured" if peaks else "fallback",
+            "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": push_ms,
+            "phase_ms_per_step": {k: v / a.steps for k, v in phases.items() if v > 0}}
+
+    # end to end through the C ABI with pinned host buffers
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    hsp = []
+    for s in st.species:
+        n = len(s["cell"])
+        d = {k: pinned(n, torch.float64) for k in ("ox", "oy", "oz", "px", "py", "pz")}
+        d["cell"] = pinned(n, torch.int32)
+        for k in d:
+            d[k][:] = s[k]
+        hsp.append(d)
+    hE = pinned(st.E.shape, torch.float64); hE[:] = st.E
+    hB = pinned(st.B.shape, torch.float64); hB[:] = st.B
+    hJ = pinned(st.E.shape, torch.float64)
+    h2d = sum(len(d["cell"]) * (4 + 6 * 8) for d in hsp) + 2 * hE.nbytes
+    d2h = sum(len(d["cell"]) * (4 + 6 * 8) for d in hsp) + 3 * hE.nbytes
+    L = sim.L
+    ptr = lambda x: x.ctypes.data_as(P._dp)  # noqa: E731
+    iptr = lambda x: x.ctypes.data_as(P._ip)  # noqa: E731
+
+    def e2e_step():
+        for sid, d in enumerate(hsp):
+            sim._ck(L.pic_upload_particles(sim.ctx, sid, len(d["cell"]), iptr(d["cell"]), ptr(d["ox"]), ptr(d["oy"]),
+                                           ptr(d["oz"]), ptr(d["px"]), ptr(d["py"]), ptr(d["pz"]), None))
+        sim._ck(L.pic_upload_fields(sim.ctx, ptr(hE), ptr(hB)))
+        sim._ck(L.pic_buneman_step(sim.ctx, 1))
+        for sid, d in enumerate(hsp):
+            sim._ck(L.pic_download_particles(sim.ctx, sid, None, iptr(d["cell"]), ptr(d["ox"]), ptr(d["oy"]),
+                                             ptr(d["oz"]), ptr(d["px"]), ptr(d["py"]), ptr(d["pz"]), None))
+        sim._ck(L.pic_download_fields(sim.ctx, ptr(hE), ptr(hB), ptr(hJ)))
+
+    e2e_step()
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(a.e2e_steps):
+        e2e_step()
+    f1.record(stream)
+    f1.synchronize()
+    barrier()
+    e2e_ms = f0.elapsed_time(f1) / a.e2e_steps
+    e2e_val = npart * world / (e2e_ms * 1e-3)
+
+    if rank == 0:
+        cpu = None
+        if not a.no_cpu_baseline:
+            v, desc, _ = cpu_baseline(a.ppc, 1, target_s=10.0)
+            cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Maxwell-Juttner plasma)",
+            "config": _config(a), "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms},
+            "gpu_launches": int(round(launches_per_step * a.steps)), "clocks": ck,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

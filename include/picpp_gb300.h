@@ -1,0 +1,197 @@
+/*
+ * picpp_gb300.h -- C ABI of the GB300 (sm_103a) implementation of PIC++'s
+ * per-timestep hot path.
+ *
+ * The reference has no plugin or FFI layer: the hot path sits behind the
+ * member functions of class Simulation that the step loop of
+ * Simulation::simulate calls (PIC++/simulation.cpp:164-259, 296-309, 360).
+ * Each phase entry point below names the member function it replaces.  All
+ * of them act on one context that owns every device buffer; host buffers
+ * stay owned by the caller.  Every call is synchronous on the context's
+ * CUDA stream (it returns after the GPU work finished) and returns a status
+ * code; the reference instead prints, writes errorLog.dat and exits
+ * (PIC++/util.cpp:119-129).
+ *
+ * Layout shared by every grid argument: a periodic box of nx*ny*nz cells,
+ * component-major then k, j, i with i fastest (a[c][k][j][i]).  Explicit
+ * (Yee) runs keep Ex at (i+1/2, j, k), Ey at (i, j+1/2, k), Ez at
+ * (i, j, k+1/2), Bx at (i, j+1/2, k+1/2), By at (i+1/2, j, k+1/2),
+ * Bz at (i+1/2, j+1/2, k), J like E (PIC++/correlation.cpp:585-591).  Implicit
+ * runs keep E on nodes (i, j, k) and B on cell centres (i+1/2, j+1/2, k+1/2)
+ * (PIC++/correlation.cpp:23-164).  The reference's ghosted index r maps to
+ * our (r - 2) mod n.  Particles are given by a linear cell index (i fastest),
+ * in-cell offsets in [0,1) and momentum p = m*gamma*v; units are the
+ * reference's normalised units with c = 1.
+ */
+#ifndef PICPP_GB300_H
+#define PICPP_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pic_ctx pic_ctx;
+
+typedef enum {
+    PIC_OK = 0,
+    PIC_ERR_ARG = 1,        /* invalid argument or configuration            */
+    PIC_ERR_CUDA = 2,       /* CUDA runtime error (message in pic_last_error) */
+    PIC_ERR_STATE = 3,      /* call not valid for this solver / state        */
+    PIC_ERR_NOMEM = 4,      /* device allocation failed or capacity exceeded */
+    PIC_ERR_NUMERIC = 5,    /* NaN/Inf detected in an input or a solve       */
+    PIC_ERR_NOT_CONVERGED = 6 /* field solve missed its tolerance            */
+} pic_status;
+
+typedef enum { PIC_SOLVER_BUNEMAN = 0, PIC_SOLVER_IMPLICIT = 1 } pic_solver_type;
+typedef enum { PIC_REAL_F32 = 0, PIC_REAL_F64 = 1 } pic_real;
+
+/* One run's configuration; replaces the input deck and the compile-time
+ * constants of PIC++/constants.h that the hot path reads. */
+typedef struct {
+    int nx, ny, nz;          /* cells per axis (an axis of 1 is a reduced dimension) */
+    double dx, dy, dz, dt;
+    double theta;            /* implicit centring, initialTheta (constants.h:40)       */
+    double eta;              /* mover centring, Simulation::eta (initialization.cpp:320) */
+    double cfix;             /* speed_of_light_correction (constants.h:45), 1.025      */
+    int solver;              /* pic_solver_type                                         */
+    int particle_real;       /* pic_real of particle offsets/momenta and of the push    */
+    int field_real;          /* pic_real of the Yee E and B grids (explicit runs)       */
+    int pressure_compat;     /* 1: reproduce the reference's pressure-tensor indexing
+                                (momentum_collecting.cpp:565,577) and fold
+                                (momentum_exchange.cpp:1643-1741); 0: periodic          */
+    int sort_every;          /* re-sort particles by cell every n steps (0: never)     */
+    int tile[3];             /* tile extents of the sort key / deposit tiles (0: 8)     */
+    int max_species;         /* species slots to reserve (0: 8)                         */
+} pic_config;
+
+/* Field-solve options for the implicit Maxwell system. */
+typedef enum {
+    PIC_GMRES_REFERENCE = 0, /* generalizedMinimalResidualMethod semantics
+                                (specialmath.cpp:367-671): unrestarted, MGS,
+                                stop at |r|/|b| <= tol/(3N) or max_iter vectors */
+    PIC_GMRES_RESTARTED = 1, /* GMRES(restart), classical Gram-Schmidt with
+                                re-orthogonalisation, true FP64 residual checked
+                                against tol at every restart                     */
+    PIC_FGMRES_LEARNED = 2   /* flexible GMRES(restart) with the learned right
+                                preconditioner; plain GMRES when it stalls       */
+} pic_gmres_method;
+
+typedef struct {
+    int method;              /* pic_gmres_method                              */
+    int restart;             /* Krylov vectors per cycle (methods 1, 2)       */
+    int max_iter;            /* total iteration cap                           */
+    double tol;              /* relative residual target                      */
+} pic_solve_opts;
+
+typedef struct {
+    int iterations;          /* Krylov iterations performed                  */
+    int restarts;
+    int used_fallback;       /* 1 if the learned preconditioner was abandoned */
+    double rel_residual;     /* final true |b - A x| / |b| (FP64)             */
+    double seconds;          /* device time of the solve                      */
+} pic_solve_info;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+/* Replaces the Simulation constructor and createArrays
+ * (PIC++/initialization.cpp:204-505, 6618-7395). */
+pic_status pic_create(const pic_config* cfg, pic_ctx** out);
+/* Replaces ~Simulation (PIC++/initialization.cpp:1278). */
+pic_status pic_destroy(pic_ctx* ctx);
+/* Last error message of this context ("" if none). */
+const char* pic_last_error(const pic_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * work around the library's calls. */
+void* pic_stream(pic_ctx* ctx);
+
+/* ---- state -------------------------------------------------------------- */
+/* Adds a particle species (ParticleTypeContainer, PIC++/particle.h:16-43):
+ * charge q, mass m, macro-particle weight w, room for capacity particles. */
+pic_status pic_add_species(pic_ctx* ctx, double q, double m, double w, long capacity, int* species_id);
+/* Replaces the particle list of a species with n particles from host FP64
+ * SoA arrays (the state Simulation::particles holds, PIC++/simulation.h:488).
+ * ids may be NULL (then 0..n-1). */
+pic_status pic_upload_particles(pic_ctx* ctx, int species, long n, const int* cell,
+                                const double* ox, const double* oy, const double* oz,
+                                const double* px, const double* py, const double* pz,
+                                const int* ids);
+/* Copies a species back in the current device order.  Any output pointer may
+ * be NULL.  *n receives the count. */
+pic_status pic_download_particles(pic_ctx* ctx, int species, long* n, int* cell,
+                                  double* ox, double* oy, double* oz,
+                                  double* px, double* py, double* pz, int* ids);
+/* Sets E and B (3*N doubles each, layout above).  Replaces the grids the
+ * initialisers fill (Efield/Bfield or bunemanE/B, PIC++/simulation.h:283-326). */
+pic_status pic_upload_fields(pic_ctx* ctx, const double* E, const double* B);
+/* Copies E, B and the last current J (3*N each; any may be NULL). */
+pic_status pic_download_fields(pic_ctx* ctx, double* E, double* B, double* J);
+
+/* ---- explicit Buneman / Tristan phases (PIC++/simulation.cpp:164-204) ---- */
+/* tristanEvaluateBhalfStep (PIC++/fields.cpp:21-79) */
+pic_status pic_tristan_evaluate_b_half_step(pic_ctx* ctx);
+/* moveParticles (PIC++/mover.cpp:21-55): Boris push (moveParticleTristan,
+ * PIC++/mover.cpp:718-808) for Buneman runs, the implicit mover (moveParticle,
+ * PIC++/mover.cpp:194-491) for implicit runs; periodic wrap included
+ * (exchangeParticles, PIC++/mover.cpp:1002-1210). */
+pic_status pic_move_particles(pic_ctx* ctx);
+/* tristanUpdateFlux (PIC++/momentum_collecting.cpp:20-82) */
+pic_status pic_tristan_update_flux(pic_ctx* ctx);
+/* tristanEvaluateE (PIC++/fields.cpp:81-150) */
+pic_status pic_tristan_evaluate_e(pic_ctx* ctx);
+/* nsteps of the whole Buneman branch of the step loop, fused kernels. */
+pic_status pic_buneman_step(pic_ctx* ctx, int nsteps);
+
+/* ---- implicit phases (PIC++/simulation.cpp:205-259) ---------------------- */
+/* evaluateParticlesRotationTensor + updateElectroMagneticParameters
+ * (PIC++/mover.cpp:810-841, PIC++/momentum_collecting.cpp:365-758):
+ * J-hat, dielectric tensor, rho-hat and pressure tensor with their folds
+ * and divergence corrections. */
+pic_status pic_update_electromagnetic_parameters(pic_ctx* ctx);
+/* evaluateElectricField (PIC++/fields.cpp:152-376) with
+ * evaluateMaxwellEquationMatrix (fields.cpp:441-600) done matrix-free and
+ * generalizedMinimalResidualMethod (specialmath.cpp:367-671) replaced by
+ * the solver chosen in opts.  info may be NULL. */
+pic_status pic_evaluate_electric_field(pic_ctx* ctx, const pic_solve_opts* opts, pic_solve_info* info);
+/* evaluateMagneticField (PIC++/fields.cpp:2717-2773) */
+pic_status pic_evaluate_magnetic_field(pic_ctx* ctx);
+/* updateFields (PIC++/fields.cpp:422-439) */
+pic_status pic_update_fields(pic_ctx* ctx);
+/* One whole implicit step: the four calls above plus moveParticles. */
+pic_status pic_implicit_step(pic_ctx* ctx, const pic_solve_opts* opts, pic_solve_info* info);
+/* Copies the last moments: J-hat (3N), mu (9N, row-major 3x3 per node),
+ * rho-hat with one low ghost layer ((nx+1)(ny+1)(nz+1) for 3-D, an axis of 1
+ * stays 1) and the right part of the Maxwell system (3N).  NULL skips. */
+pic_status pic_download_moments(pic_ctx* ctx, double* J, double* mu, double* rho_ext, double* rhs);
+/* Applies the implicit Maxwell operator built from mu to x (3N each, host). */
+pic_status pic_maxwell_apply(pic_ctx* ctx, const double* mu, const double* x, double* y);
+/* Solves A(mu) x = rhs (host arrays) with the given options. */
+pic_status pic_maxwell_solve(pic_ctx* ctx, const double* mu, const double* rhs, double* x,
+                             const pic_solve_opts* opts, pic_solve_info* info);
+
+/* ---- particle order ----------------------------------------------------- */
+/* Stable counting sort of every species by tile-major cell key (no reference
+ * counterpart; the reference keeps an unordered std::vector<Particle*>). */
+pic_status pic_sort_particles(pic_ctx* ctx);
+/* Source index of every slot after the last sort of a species (n ints). */
+pic_status pic_download_permutation(pic_ctx* ctx, int species, long* n, int* perm);
+
+/* ---- diagnostics -------------------------------------------------------- */
+/* updateEnergy (PIC++/simulation.cpp:1506-1600) in normalised units:
+ * out = {particle kinetic, electric, magnetic energy, px, py, pz momentum}. */
+pic_status pic_energy(pic_ctx* ctx, double out[6]);
+
+/* Phase timing, the GPU counterpart of the reference's per-phase clock()
+ * prints (PIC++/mover.cpp:23-54, simulation.cpp:157-159).  enable = 1 starts
+ * (and clears) recording of CUDA events around every phase on the context
+ * stream; enable = 0 stops.  phase_ms (may be NULL) receives the accumulated
+ * device milliseconds of PIC_PHASE_COUNT phases, launches the number of
+ * kernels launched while recording. */
+typedef enum {
+    PIC_PHASE_SORT = 0, PIC_PHASE_FIELDS = 1, PIC_PHASE_PUSH_DEPOSIT = 2, PIC_PHASE_ASSEMBLE = 3,
+    PIC_PHASE_MOMENTS = 4, PIC_PHASE_SOLVE = 5, PIC_PHASE_MOVER = 6, PIC_PHASE_COUNT = 7
+} pic_phase;
+pic_status pic_profile(pic_ctx* ctx, int enable, double* phase_ms, long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

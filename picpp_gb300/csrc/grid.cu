@@ -1,0 +1,144 @@
+// grid.cu -- launchers of the FP64 grid kernels: cell sort, implicit moment
+// corrections, Maxwell right part and operator, field update, Krylov vectors.
+#include "implicit_grid.cuh"
+#include "kernels.hpp"
+#include "krylov.cuh"
+#include "sort.cuh"
+#include <algorithm>
+
+namespace pic {
+
+// ---------------------------------------------------------------- sort
+void launch_keys_hist(cudaStream_t s, const GridP& g, const TileGeom& t, const int* cell, long long n, int* key,
+                      int* counts) {
+    if (n == 0) return;
+    k_keys_hist<<<grid_for(n, 256, 32), 256, 0, s>>>(g, t, cell, n, key, counts);
+}
+
+void launch_excl_scan(cudaStream_t s, int* a, long long n, int* block_sums, int* grand_total) {
+    const long long per = (long long)kScanThreads * kScanItems;
+    const int nb = (int)((n + per - 1) / per);
+    k_scan_blocks<<<nb, kScanThreads, 0, s>>>(a, n, block_sums);
+    k_scan_top<<<1, kScanThreads, 0, s>>>(block_sums, nb, grand_total);
+    k_scan_add<<<nb, kScanThreads, 0, s>>>(a, n, block_sums);
+}
+
+void launch_scatter_atomic(cudaStream_t s, const int* key, long long n, int* cursor, int* tmp) {
+    if (n == 0) return;
+    k_scatter_atomic<<<grid_for(n, 256, 32), 256, 0, s>>>(key, n, cursor, tmp);
+}
+
+void launch_segsort(cudaStream_t s, const int* off, int nkeys, const int* tmp, int* perm, int* long_count,
+                    int* long_list) {
+    cudaMemsetAsync(long_count, 0, sizeof(int), s);
+    long long warps = nkeys;
+    int blocks = (int)std::min<long long>((warps * 32 + 255) / 256, (long long)kNumSM * 32);
+    k_segsort_warp<<<blocks, 256, 0, s>>>(off, nkeys, tmp, perm, long_count, long_list);
+    k_segsort_block<<<kNumSM, 1024, 0, s>>>(off, long_list, long_count, tmp, perm);
+}
+
+// ---------------------------------------------------------------- moments
+void launch_pi_fold_reference(cudaStream_t s, double* P, const GhostAxes& ga, int axis) {
+    const int ce[3] = {ga.cex, ga.cey, ga.cez};
+    if (ce[axis] == 1) return;   // single-cell axis: nothing to fold
+    const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+    long long total = 9LL * ce[a1] * ce[a2];
+    k_pi_fold_reference<<<grid_for(total, 256), 256, 0, s>>>(P, ga, axis);
+}
+
+void launch_jg_build(cudaStream_t s, const GridP& g, const GhostAxes& ga, const double* J, const double* P,
+                     double* Jg, int nex, int ney, int nez) {
+    long long n = (long long)nex * ney * nez;
+    k_jg_build<<<grid_for(n, 256), 256, 0, s>>>(g, ga, J, P, Jg, nex, ney, nez);
+}
+
+void launch_rho_ext_reference(cudaStream_t s, const GridP& g, const double* Jg, int nex, int ney, int nez,
+                              const double* rho, double* rho_ext, int ex, int ey, int ez) {
+    long long n = (long long)ex * ey * ez;
+    k_rho_ext_reference<<<grid_for(n, 256), 256, 0, s>>>(g, Jg, nex, ney, nez, rho, rho_ext, ex, ey, ez);
+}
+
+void launch_jg_interior(cudaStream_t s, const GridP& g, const double* Jg, int nex, int ney, int nez, int gx, int gy,
+                        int gz, double* J) {
+    k_jg_interior<<<grid_for(g.N, 256), 256, 0, s>>>(g, Jg, nex, ney, nez, gx, gy, gz, J);
+}
+
+void launch_j_minus_divpi(cudaStream_t s, const GridP& g, const double* Pi, const double* Jin, double* Jout) {
+    k_j_minus_divpi<<<grid_for(g.N, 256), 256, 0, s>>>(g, Pi, Jin, Jout);
+}
+
+void launch_rho_ext_periodic(cudaStream_t s, const GridP& g, const double* J, const double* rho, double* rho_ext,
+                             int ex, int ey, int ez) {
+    long long n = (long long)ex * ey * ez;
+    k_rho_ext_periodic<<<grid_for(n, 256), 256, 0, s>>>(g, J, rho, rho_ext, ex, ey, ez);
+}
+
+void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const double* B, const double* J,
+                        const double* rho_ext, int ex, int ey, double* rhs) {
+    k_maxwell_rhs<<<grid_for(g.N, 256), 256, 0, s>>>(g, E, B, J, rho_ext, ex, ey, rhs);
+}
+
+void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
+                          double* y) {
+    k_maxwell_apply<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, mu, x, y);
+}
+
+void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,
+                         double* En, double* Bn, int doE, int doB) {
+    k_field_update<<<grid_for(g.N, 256), 256, 0, s>>>(g, Et, E, B, En, Bn, doE, doB);
+}
+
+// ---------------------------------------------------------------- Krylov
+void launch_finalize(cudaStream_t s, const double* partials, int P, int nvec, double* out, int ostride,
+                     int take_sqrt) {
+    k_finalize<<<nvec, kRedThreads, 0, s>>>(partials, P, out, ostride, take_sqrt);
+}
+
+void launch_dot(cudaStream_t s, const double* a, const double* b, long long n, double* partials, int P, double* out,
+                int take_sqrt) {
+    k_dot_partials<<<P, kRedThreads, 0, s>>>(a, b, n, partials);
+    k_finalize<<<1, kRedThreads, 0, s>>>(partials, P, out, 1, take_sqrt);
+}
+
+void launch_multi_dot(cudaStream_t s, const double* V, long long ld, int k, const double* w, long long n,
+                      double* partials, int P, double* out) {
+    for (int k0 = 0; k0 < k; k0 += 8)
+        k_multi_dot_partials<8><<<P, kRedThreads, 0, s>>>(V, ld, k0, k, w, n, partials, P);
+    k_finalize<<<k, kRedThreads, 0, s>>>(partials, P, out, 1, 0);
+}
+
+void launch_axpy_minus_dev(cudaStream_t s, double* y, const double* x, const double* alpha, long long n) {
+    k_axpy_minus_dev<<<grid_for(n, 256), 256, 0, s>>>(y, x, alpha, n);
+}
+
+void launch_multi_axpy_minus(cudaStream_t s, double* w, const double* V, long long ld, int k, const double* h,
+                             int hstride, long long n) {
+    k_multi_axpy_minus<<<grid_for(n, 256), 256, 0, s>>>(w, V, ld, k, h, hstride, n);
+}
+
+void launch_scale_inv_dev(cudaStream_t s, double* v, const double* w, const double* h, long long n) {
+    k_scale_inv_dev<<<grid_for(n, 256), 256, 0, s>>>(v, w, h, n);
+}
+
+void launch_scale(cudaStream_t s, double* v, const double* w, double sc, long long n) {
+    k_scale<<<grid_for(n, 256), 256, 0, s>>>(v, w, sc, n);
+}
+
+void launch_div(cudaStream_t s, double* v, const double* w, double d, long long n) {
+    k_div<<<grid_for(n, 256), 256, 0, s>>>(v, w, d, n);
+}
+
+void launch_combine(cudaStream_t s, double* x, const double* V, long long ld, int k, const double* y, double scale,
+                    int accumulate, long long n) {
+    k_combine<<<grid_for(n, 256), 256, 0, s>>>(x, V, ld, k, y, scale, accumulate, n);
+}
+
+void launch_residual(cudaStream_t s, double* r, const double* b, const double* Ax, long long n) {
+    k_residual<<<grid_for(n, 256), 256, 0, s>>>(r, b, Ax, n);
+}
+
+void launch_nonfinite(cudaStream_t s, const double* a, long long n, int* flag) {
+    k_nonfinite<<<grid_for(n, 256), 256, 0, s>>>(a, n, flag);
+}
+
+}  // namespace pic

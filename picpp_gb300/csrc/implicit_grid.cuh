@@ -1,0 +1,328 @@
+// implicit_grid.cuh -- FP64 grid kernels of the implicit Maxwell solve:
+// moment corrections, right part, matrix-free operator, field update.
+#pragma once
+#include "common.cuh"
+#include "implicit_particles.cuh"
+
+namespace pic {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// Pressure tensor fold in the reference's ghosted index space
+// (sumCellMatrixParameters{X,Y,Z}, PIC++/momentum_exchange.cpp:1643-1741):
+// the reference pairs ghost cell r with r + n + 1; reproduced exactly.
+// axis: 0 x, 1 y, 2 z.  One thread per (component, line).
+__global__ void k_pi_fold_reference(double* __restrict__ P, GhostAxes ga, int axis) {
+    const int ce[3] = {ga.cex, ga.cey, ga.cez};
+    const long long PN = (long long)ga.cex * ga.cey * ga.cez;
+    const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;   // the two other axes
+    const long long lines = (long long)ce[a1] * ce[a2];
+    const long long total = lines * 9;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int d = (int)(t / lines);
+        long long l = t - d * lines;
+        int u1 = (int)(l % ce[a1]), u2 = (int)(l / ce[a1]);
+        auto at = [&](int r) -> double& {
+            int c[3];
+            c[axis] = r; c[a1] = u1; c[a2] = u2;
+            return P[d * PN + ((long long)c[2] * ga.cey + c[1]) * ga.cex + c[0]];
+        };
+        const int e = ce[axis];
+        for (int s = 0; s < 3; ++s) {
+            double v = at(e - 1 - s) + at(2 - s);
+            at(e - 1 - s) = v;
+            at(2 - s) = v;
+        }
+    }
+}
+
+// evaluateDivPressureTensor (PIC++/fields.cpp:3158-3223) at node (i,j,k),
+// Pi read through PT(a, b, i, j, k).
+template <typename PTf>
+__device__ __forceinline__ void div_pi(const GridP& g, int i, int j, int k, PTf PT, double out[3]) {
+    for (int col = 0; col < 3; ++col) {
+        double rA = (PT(0, col, i, j, k) + PT(0, col, i, j - 1, k) + PT(0, col, i, j, k - 1) + PT(0, col, i, j - 1, k - 1)) * 0.25;
+        double lA = (PT(0, col, i - 1, j, k) + PT(0, col, i - 1, j - 1, k) + PT(0, col, i - 1, j, k - 1) + PT(0, col, i - 1, j - 1, k - 1)) * 0.25;
+        double bA = 0, fA = 0, tA = 0, boA = 0;
+        if (g.y3) {
+            bA = (PT(1, col, i, j, k) + PT(1, col, i - 1, j, k) + PT(1, col, i, j, k - 1) + PT(1, col, i - 1, j, k - 1)) * 0.25;
+            fA = (PT(1, col, i, j - 1, k) + PT(1, col, i - 1, j - 1, k) + PT(1, col, i, j - 1, k - 1) + PT(1, col, i - 1, j - 1, k - 1)) * 0.25;
+        }
+        if (g.z3) {
+            tA = (PT(2, col, i, j, k) + PT(2, col, i, j - 1, k) + PT(2, col, i - 1, j, k) + PT(2, col, i - 1, j - 1, k)) * 0.25;
+            boA = (PT(2, col, i, j, k - 1) + PT(2, col, i, j - 1, k - 1) + PT(2, col, i - 1, j, k - 1) + PT(2, col, i - 1, j - 1, k - 1)) * 0.25;
+        }
+        out[col] = ((rA - lA) / g.dx) + ((bA - fA) / g.dy) + ((tA - boA) / g.dz);
+    }
+}
+
+// evaluateDivFlux (PIC++/fields.cpp:3060-3156) at cell (i,j,k), J through JF.
+template <typename JFf>
+__device__ __forceinline__ double div_j(const GridP& g, int i, int j, int k, JFf JF) {
+    double rX = (JF(0, i + 1, j, k) + JF(0, i + 1, j + 1, k) + JF(0, i + 1, j, k + 1) + JF(0, i + 1, j + 1, k + 1)) * 0.25;
+    double lX = (JF(0, i, j, k) + JF(0, i, j + 1, k) + JF(0, i, j, k + 1) + JF(0, i, j + 1, k + 1)) * 0.25;
+    double rY = 0, lY = 0, rZ = 0, lZ = 0;
+    if (g.y3) {
+        rY = (JF(1, i, j + 1, k) + JF(1, i + 1, j + 1, k) + JF(1, i, j + 1, k + 1) + JF(1, i + 1, j + 1, k + 1)) * 0.25;
+        lY = (JF(1, i, j, k) + JF(1, i + 1, j, k) + JF(1, i, j, k + 1) + JF(1, i + 1, j, k + 1)) * 0.25;
+    }
+    if (g.z3) {
+        rZ = (JF(2, i + 1, j, k + 1) + JF(2, i, j, k + 1) + JF(2, i, j + 1, k + 1) + JF(2, i + 1, j + 1, k + 1)) * 0.25;
+        lZ = (JF(2, i + 1, j, k) + JF(2, i, j, k) + JF(2, i, j + 1, k) + JF(2, i + 1, j + 1, k)) * 0.25;
+    }
+    return ((rX - lX) / g.dx) + ((rY - lY) / g.dy) + ((rZ - lZ) / g.dz);
+}
+
+__device__ __forceinline__ int gphys(int r, int n) { return n > 1 ? wrap_any(r - 2, n) : 0; }
+__device__ __forceinline__ int gcl(int r, int n) { return n > 1 ? r : 0; }
+
+// Reference layout: J-hat on ghosted nodes (n + 5 per axis) = periodic fold
+// result minus eta dt div(Pi) (momentum_collecting.cpp:622-631).
+__global__ void k_jg_build(GridP g, GhostAxes ga, const double* __restrict__ J, const double* __restrict__ P,
+                           double* __restrict__ Jg, int nex, int ney, int nez) {
+    const long long JN = (long long)nex * ney * nez;
+    const long long PN = (long long)ga.cex * ga.cey * ga.cez;
+    const bool single = (g.nx == 1 || !g.y3 || !g.z3);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < JN;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t % nex);
+        long long q = t / nex;
+        int j = (int)(q % ney), k = (int)(q / ney);
+        long long src = lin(g, gphys(i, g.nx), gphys(j, g.ny), gphys(k, g.nz));
+        double out[3] = {0, 0, 0};
+        bool edge = (i == 0 || i == nex - 1 || j == 0 || j == ney - 1 || k == 0 || k == nez - 1);
+        if (!single && !edge) {
+            auto PT = [&](int a, int b, int ii, int jj, int kk) -> double {
+                return P[(3 * a + b) * PN + ((long long)gcl(kk, g.nz) * ga.cey + gcl(jj, g.ny)) * ga.cex + gcl(ii, g.nx)];
+            };
+            div_pi(g, i, j, k, PT, out);
+        }
+        for (int d = 0; d < 3; ++d) Jg[d * JN + t] = J[d * g.N + src] - out[d] * g.eta * g.dt;
+    }
+}
+
+// Reference layout: rho-hat -= theta dt div(J-hat) (momentum_collecting.cpp
+// 645-657), written with one low ghost layer (ext index 0 = reference cell 1).
+__global__ void k_rho_ext_reference(GridP g, const double* __restrict__ Jg, int nex, int ney, int nez,
+                                    const double* __restrict__ rho, double* __restrict__ rho_ext,
+                                    int ex, int ey, int ez) {
+    const long long JN = (long long)nex * ney * nez;
+    const long long EN = (long long)ex * ey * ez;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < EN;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t % ex);
+        long long q = t / ex;
+        int j = (int)(q % ey), k = (int)(q / ey);
+        int ri = g.nx > 1 ? i + 1 : 0, rj = g.ny > 1 ? j + 1 : 0, rk = g.nz > 1 ? k + 1 : 0;
+        auto JF = [&](int d, int ii, int jj, int kk) -> double {
+            return Jg[d * JN + ((long long)gcl(kk, g.nz) * ney + gcl(jj, g.ny)) * nex + gcl(ii, g.nx)];
+        };
+        double div = div_j(g, ri, rj, rk, JF);
+        long long src = lin(g, gphys(ri, g.nx), gphys(rj, g.ny), gphys(rk, g.nz));
+        rho_ext[t] = rho[src] - g.dt * g.theta * div;
+    }
+}
+
+// Interior nodes of the reference-layout J-hat back to the periodic array.
+__global__ void k_jg_interior(GridP g, const double* __restrict__ Jg, int nex, int ney, int nez,
+                              int gx, int gy, int gz, double* __restrict__ J) {
+    const long long JN = (long long)nex * ney * nez;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
+         c += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, (int)c, i, j, k);
+        long long s = ((long long)(k + gz) * ney + (j + gy)) * nex + (i + gx);
+        for (int d = 0; d < 3; ++d) J[d * g.N + c] = Jg[d * JN + s];
+    }
+}
+
+// Periodic layout: J-hat -= eta dt div(Pi) on the box.
+__global__ void k_j_minus_divpi(GridP g, const double* __restrict__ Pi, const double* __restrict__ Jin,
+                                double* __restrict__ Jout) {
+    const bool single = (g.nx == 1 || !g.y3 || !g.z3);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
+         c += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, (int)c, i, j, k);
+        double out[3] = {0, 0, 0};
+        if (!single) {
+            auto PT = [&](int a, int b, int ii, int jj, int kk) -> double {
+                return Pi[(3 * a + b) * g.N + linw(g, ii, jj, kk)];
+            };
+            div_pi(g, i, j, k, PT, out);
+        }
+        for (int d = 0; d < 3; ++d) Jout[d * g.N + c] = Jin[d * g.N + c] - out[d] * g.eta * g.dt;
+    }
+}
+
+// Periodic layout: rho_ext from rho-hat -= theta dt div(J-hat).
+__global__ void k_rho_ext_periodic(GridP g, const double* __restrict__ J, const double* __restrict__ rho,
+                                   double* __restrict__ rho_ext, int ex, int ey, int ez) {
+    const long long EN = (long long)ex * ey * ez;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < EN;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t % ex);
+        long long q = t / ex;
+        int j = (int)(q % ey), k = (int)(q / ey);
+        int ii = g.nx > 1 ? i - 1 : 0, jj = g.ny > 1 ? j - 1 : 0, kk = g.nz > 1 ? k - 1 : 0;
+        auto JF = [&](int d, int a, int b, int c) -> double { return J[d * g.N + linw(g, a, b, c)]; };
+        double div = div_j(g, ii, jj, kk, JF);
+        rho_ext[t] = rho[linw(g, ii, jj, kk)] - g.dt * g.theta * div;
+    }
+}
+
+// createInternalEquation right part (PIC++/fields.cpp:2635-2658), evaluateRotB
+// (fields.cpp:2799-2860), evaluateGradDensity (fields.cpp:3229-3259).
+__global__ void __launch_bounds__(256) k_maxwell_rhs(GridP g, const double* __restrict__ E, const double* __restrict__ B,
+                                                     const double* __restrict__ J, const double* __restrict__ rho_ext,
+                                                     int ex, int ey, double* __restrict__ rhs) {
+    const double cf = g.cfix, cf2 = g.cfix * g.cfix, td = g.theta * g.dt;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
+         c += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, (int)c, i, j, k);
+        const int pi_ = i - 1, pj = j - 1, pk = k - 1;
+        auto BF = [&](int d, int a, int b, int cc) -> double { return B[d * g.N + linw(g, a, b, cc)]; };
+        auto RH = [&](int a, int b, int cc) -> double {
+            return rho_ext[((long long)(g.nz > 1 ? cc + 1 : 0) * ey + (g.ny > 1 ? b + 1 : 0)) * ex + (g.nx > 1 ? a + 1 : 0)];
+        };
+        double BrX[3], BlX[3], BrY[3], BlY[3], BrZ[3], BlZ[3];
+        for (int d = 0; d < 3; ++d) {
+            BrX[d] = (BF(d, i, j, k) + BF(d, i, pj, k) + BF(d, i, j, pk) + BF(d, i, pj, pk)) / 4.0;
+            BlX[d] = (BF(d, pi_, j, k) + BF(d, pi_, pj, k) + BF(d, pi_, j, pk) + BF(d, pi_, pj, pk)) / 4.0;
+            BrY[d] = (BF(d, i, j, k) + BF(d, pi_, j, k) + BF(d, i, j, pk) + BF(d, pi_, j, pk)) / 4.0;
+            BlY[d] = (BF(d, i, pj, k) + BF(d, pi_, pj, k) + BF(d, i, pj, pk) + BF(d, pi_, pj, pk)) / 4.0;
+            BrZ[d] = (BF(d, i, j, k) + BF(d, pi_, j, k) + BF(d, i, pj, k) + BF(d, pi_, pj, k)) / 4.0;
+            BlZ[d] = (BF(d, i, j, pk) + BF(d, pi_, j, pk) + BF(d, i, pj, pk) + BF(d, pi_, pj, pk)) / 4.0;
+            if (!g.y3) { BrY[d] = 0; BlY[d] = 0; }
+            if (!g.z3) { BrZ[d] = 0; BlZ[d] = 0; }
+        }
+        double rot[3];
+        rot[0] = (BrY[2] - BlY[2]) / g.dy - (BrZ[1] - BlZ[1]) / g.dz;
+        rot[1] = (BrZ[0] - BlZ[0]) / g.dz - (BrX[2] - BlX[2]) / g.dx;
+        rot[2] = (BrX[1] - BlX[1]) / g.dx - (BrY[0] - BlY[0]) / g.dy;
+        double dRX = (RH(i, j, k) + RH(i, pj, k) + RH(i, j, pk) + RH(i, pj, pk)) * 0.25;
+        double dLX = (RH(pi_, j, k) + RH(pi_, pj, k) + RH(pi_, j, pk) + RH(pi_, pj, pk)) * 0.25;
+        double dRY = (RH(i, j, k) + RH(pi_, j, k) + RH(i, j, pk) + RH(pi_, j, pk)) * 0.25;
+        double dLY = (RH(i, pj, k) + RH(pi_, pj, k) + RH(i, pj, pk) + RH(pi_, pj, pk)) * 0.25;
+        double dRZ = (RH(i, j, k) + RH(i, pj, k) + RH(pi_, j, k) + RH(pi_, pj, k)) * 0.25;
+        double dLZ = (RH(i, j, pk) + RH(i, pj, pk) + RH(pi_, j, pk) + RH(pi_, pj, pk)) * 0.25;
+        double grad[3] = {(dRX - dLX) / g.dx, (dRY - dLY) / g.dy, (dRZ - dLZ) / g.dz};
+        for (int d = 0; d < 3; ++d)
+            rhs[d * g.N + c] = E[d * g.N + c] + (rot[d] * cf - (J[d * g.N + c] * 4 * kPi)) * td -
+                               (grad[d] * cf2 * g.theta * g.theta * g.dt * g.dt * 4 * kPi);
+    }
+}
+
+// Matrix-free implicit Maxwell operator, the rows of createInternalEquationX/
+// Y/Z (PIC++/fields.cpp:1396-1509, 1961-2073, 2521-2633), K = (theta dt c')^2
+// (fields.cpp:888).  Factored per node as
+//   y_a = c0_a x_a - c1_a (mu x)_a + sum_{+-a} K/da^2 ((mu x)_a - x_a)
+//         - sum_{d != a, +-d} K/dd^2 x_a
+//         + sum_{d != a} K/(4 da dd) [w_d(++) + w_d(--) - w_d(-+) - w_d(+-)]
+// with w = mu x evaluated at the neighbour nodes: the same terms as the
+// reference's 37-entry rows regrouped (so FP64 results agree to rounding).
+__device__ __forceinline__ void mu_times(const double* __restrict__ mu, long long N, long long id,
+                                         const double* __restrict__ x, double w[3]) {
+    double x0 = x[id], x1 = x[N + id], x2 = x[2 * N + id];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        w[a] = mu[(3 * a) * N + id] * x0 + mu[(3 * a + 1) * N + id] * x1 + mu[(3 * a + 2) * N + id] * x2;
+}
+
+__global__ void __launch_bounds__(256) k_maxwell_apply(GridP g, OpCoef oc, const double* __restrict__ mu,
+                                                       const double* __restrict__ x, double* __restrict__ y) {
+    const long long N = g.N;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        int p[3];
+        decode(g, (int)c, p[0], p[1], p[2]);
+        const int n[3] = {g.nx, g.ny, g.nz};
+        double xc[3] = {x[c], x[N + c], x[2 * N + c]};
+        double wc[3];
+        mu_times(mu, N, c, x, wc);
+        double acc[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            double diag = 1.0;
+            for (int ax = 0; ax < 3; ++ax)
+                if (oc.has[ax]) diag += 2.0 * oc.kd2[ax];
+            double c1 = oc.has[a] ? 1.0 + 2.0 * oc.kd2[a] : 1.0;
+            acc[a] = diag * xc[a] - c1 * wc[a];
+        }
+        // neighbours along each axis: +-a term for row a, Laplacian for the others
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            if (!oc.has[ax]) continue;
+            for (int s = -1; s <= 1; s += 2) {
+                int q[3] = {p[0], p[1], p[2]};
+                q[ax] = wrap_any(q[ax] + s, n[ax]);
+                long long cn = lin(g, q[0], q[1], q[2]);
+                double wn[3];
+                mu_times(mu, N, cn, x, wn);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    double xa = x[a * N + cn];
+                    if (a == ax) acc[a] += oc.kd2[ax] * (wn[a] - xa);
+                    else acc[a] -= oc.kd2[ax] * xa;
+                }
+            }
+        }
+        // mixed derivatives in the (a, d) planes: row a reads w_d at the corners
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (d == a || !oc.has[a] || !oc.has[d]) continue;
+                double sum = 0.0;
+                for (int sa = -1; sa <= 1; sa += 2)
+                    for (int sd = -1; sd <= 1; sd += 2) {
+                        int q[3] = {p[0], p[1], p[2]};
+                        q[a] = wrap_any(q[a] + sa, n[a]);
+                        q[d] = wrap_any(q[d] + sd, n[d]);
+                        long long cn = lin(g, q[0], q[1], q[2]);
+                        double xn0 = x[cn], xn1 = x[N + cn], xn2 = x[2 * N + cn];
+                        double wd = mu[(3 * d) * N + cn] * xn0 + mu[(3 * d + 1) * N + cn] * xn1 + mu[(3 * d + 2) * N + cn] * xn2;
+                        sum += (sa * sd > 0) ? wd : -wd;
+                    }
+                acc[a] += oc.kx4[a][d] * sum;
+            }
+        y[c] = acc[0]; y[N + c] = acc[1]; y[2 * N + c] = acc[2];
+    }
+}
+
+// evaluateElectricField (fields.cpp:326-339) and evaluateMagneticField
+// (fields.cpp:2717-2738) with evaluateRotEgeneral (fields.cpp:2862-2953).
+__global__ void __launch_bounds__(256) k_field_update(GridP g, const double* __restrict__ Et, const double* __restrict__ E,
+                                                      const double* __restrict__ B, double* __restrict__ En,
+                                                      double* __restrict__ Bn, int doE, int doB) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
+         c += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decode(g, (int)c, i, j, k);
+        if (doE)
+            for (int d = 0; d < 3; ++d) En[d * g.N + c] = (Et[d * g.N + c] - E[d * g.N + c] * (1 - g.theta)) / g.theta;
+        if (!doB) continue;
+        auto EF = [&](int d, int a, int b, int cc) -> double { return Et[d * g.N + linw(g, a, b, cc)]; };
+        double rX[3], lX[3], rY[3], lY[3], rZ[3], lZ[3];
+        for (int d = 0; d < 3; ++d) {
+            rX[d] = (EF(d, i + 1, j, k) + EF(d, i + 1, j + 1, k) + EF(d, i + 1, j, k + 1) + EF(d, i + 1, j + 1, k + 1)) / 4.0;
+            lX[d] = (EF(d, i, j, k) + EF(d, i, j + 1, k) + EF(d, i, j, k + 1) + EF(d, i, j + 1, k + 1)) / 4.0;
+            rY[d] = (EF(d, i, j + 1, k) + EF(d, i + 1, j + 1, k) + EF(d, i, j + 1, k + 1) + EF(d, i + 1, j + 1, k + 1)) / 4.0;
+            lY[d] = (EF(d, i, j, k) + EF(d, i + 1, j, k) + EF(d, i, j, k + 1) + EF(d, i + 1, j, k + 1)) / 4.0;
+            rZ[d] = (EF(d, i, j, k + 1) + EF(d, i + 1, j, k + 1) + EF(d, i, j + 1, k + 1) + EF(d, i + 1, j + 1, k + 1)) / 4.0;
+            lZ[d] = (EF(d, i, j, k) + EF(d, i + 1, j, k) + EF(d, i, j + 1, k) + EF(d, i + 1, j + 1, k)) / 4.0;
+            if (!g.y3) { rY[d] = 0; lY[d] = 0; }
+            if (!g.z3) { rZ[d] = 0; lZ[d] = 0; }
+        }
+        double rot[3];
+        rot[0] = (rY[2] - lY[2]) / g.dy - (rZ[1] - lZ[1]) / g.dz;
+        rot[1] = (rZ[0] - lZ[0]) / g.dz - (rX[2] - lX[2]) / g.dx;
+        rot[2] = (rX[1] - lX[1]) / g.dx - (rY[0] - lY[0]) / g.dy;
+        for (int d = 0; d < 3; ++d) Bn[d * g.N + c] = B[d * g.N + c] - rot[d] * (g.cfix * g.dt);
+    }
+}
+
+}  // namespace pic

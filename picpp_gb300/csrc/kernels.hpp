@@ -1,0 +1,99 @@
+// kernels.hpp -- host-side launchers of the CUDA kernels, shared by the C ABI
+// (api.cu).  Particle kernels exist for FP32 and FP64 particle state
+// (kernels_f32.cu, kernels_f64.cu); grid and Krylov kernels are FP64 only
+// (grid.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+#include "types.cuh"
+
+namespace pic {
+
+constexpr int kNumSM = 152;
+
+inline int grid_for(long long n, int threads, int per_sm = 16) {
+    long long b = (n + threads - 1) / threads;
+    long long cap = (long long)kNumSM * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// Number of partial sums used by every deterministic reduction of n items.
+inline int red_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 1024) b = 1024;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+template <typename T>
+struct PK {
+    static void yee_b_half(cudaStream_t s, const GridP& g, const void* E, void* B);
+    static void yee_e(cudaStream_t s, const GridP& g, void* E, const void* B, const double* J);
+    static void boris_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const void* E,
+                           const void* B);
+    static void zigzag(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w, double* J);
+    // fused gather/push/deposit over tiles (boris_tile.cuh); smem bytes and
+    // grid size chosen by the caller
+    static void push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh,
+                                   const SpeciesSet<T>& S, const void* E, const void* B, T* Jpart, double* Jfix,
+                                   int grid, size_t smem);
+    static void assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const T* Jpart,
+                           const double* Jfix, double* J);
+    static size_t tile_smem_bytes(const TileShape& sh);
+    static void implicit_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w,
+                                 const double* E, const double* B, double* J, double* mu, double* rho, double* Pi,
+                                 int compat, const GhostAxes& ga);
+    static void implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const double* E,
+                              const double* B, const double* Et);
+    static void gather_payload(cudaStream_t s, const int* perm, long long n, PartView<T> src, PartView<T> dst);
+    static void particle_sums(cudaStream_t s, PartView<T> p, double m, double w, double* partials, int P);
+    static void field_sq_partials(cudaStream_t s, const void* F, long long n, double* partials, int P);
+    static void to_real(cudaStream_t s, const double* src, void* dst, long long n);
+    static void from_real(cudaStream_t s, const void* src, double* dst, long long n);
+    static void validate(cudaStream_t s, const GridP& g, PartView<T> p, int* flag);
+    static void iota(cudaStream_t s, int* a, long long n);
+};
+
+// grid.cu
+void launch_keys_hist(cudaStream_t s, const GridP& g, const TileGeom& t, const int* cell, long long n, int* key,
+                      int* counts);
+void launch_excl_scan(cudaStream_t s, int* a, long long n, int* block_sums, int* grand_total);
+void launch_scatter_atomic(cudaStream_t s, const int* key, long long n, int* cursor, int* tmp);
+void launch_segsort(cudaStream_t s, const int* off, int nkeys, const int* tmp, int* perm, int* long_count,
+                    int* long_list);
+void launch_pi_fold_reference(cudaStream_t s, double* P, const GhostAxes& ga, int axis);
+void launch_jg_build(cudaStream_t s, const GridP& g, const GhostAxes& ga, const double* J, const double* P,
+                     double* Jg, int nex, int ney, int nez);
+void launch_rho_ext_reference(cudaStream_t s, const GridP& g, const double* Jg, int nex, int ney, int nez,
+                              const double* rho, double* rho_ext, int ex, int ey, int ez);
+void launch_jg_interior(cudaStream_t s, const GridP& g, const double* Jg, int nex, int ney, int nez, int gx, int gy,
+                        int gz, double* J);
+void launch_j_minus_divpi(cudaStream_t s, const GridP& g, const double* Pi, const double* Jin, double* Jout);
+void launch_rho_ext_periodic(cudaStream_t s, const GridP& g, const double* J, const double* rho, double* rho_ext,
+                             int ex, int ey, int ez);
+void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const double* B, const double* J,
+                        const double* rho_ext, int ex, int ey, double* rhs);
+void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
+                          double* y);
+void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,
+                         double* En, double* Bn, int doE, int doB);
+// Krylov
+void launch_dot(cudaStream_t s, const double* a, const double* b, long long n, double* partials, int P, double* out,
+                int take_sqrt);
+void launch_multi_dot(cudaStream_t s, const double* V, long long ld, int k, const double* w, long long n,
+                      double* partials, int P, double* out);
+void launch_axpy_minus_dev(cudaStream_t s, double* y, const double* x, const double* alpha, long long n);
+void launch_multi_axpy_minus(cudaStream_t s, double* w, const double* V, long long ld, int k, const double* h,
+                             int hstride, long long n);
+void launch_scale_inv_dev(cudaStream_t s, double* v, const double* w, const double* h, long long n);
+void launch_scale(cudaStream_t s, double* v, const double* w, double sc, long long n);
+void launch_div(cudaStream_t s, double* v, const double* w, double d, long long n);
+void launch_combine(cudaStream_t s, double* x, const double* V, long long ld, int k, const double* y, double scale,
+                    int accumulate, long long n);
+void launch_residual(cudaStream_t s, double* r, const double* b, const double* Ax, long long n);
+void launch_nonfinite(cudaStream_t s, const double* a, long long n, int* flag);
+void launch_finalize(cudaStream_t s, const double* partials, int P, int nvec, double* out, int ostride, int take_sqrt);
+
+}  // namespace pic

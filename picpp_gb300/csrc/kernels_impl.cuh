@@ -1,0 +1,194 @@
+// kernels_impl.cuh -- launchers of the particle and Yee kernels for one
+// particle precision T; instantiated by kernels_f32.cu and kernels_f64.cu.
+#pragma once
+#include "boris.cuh"
+#include "boris_tile.cuh"
+#include "implicit_particles.cuh"
+#include "kernels.hpp"
+#include "yee.cuh"
+
+namespace pic {
+
+template <typename T>
+__global__ void k_gather_payload(const int* __restrict__ perm, long long n, PartView<T> src, PartView<T> dst) {
+    for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n; d += (long long)gridDim.x * blockDim.x) {
+        int s = perm[d];
+        dst.cell[d] = src.cell[s];
+        dst.ox[d] = src.ox[s]; dst.oy[d] = src.oy[s]; dst.oz[d] = src.oz[s];
+        dst.px[d] = src.px[s]; dst.py[d] = src.py[s]; dst.pz[d] = src.pz[s];
+        dst.id[d] = src.id[s];
+    }
+}
+
+// Kinetic energy and momentum of one species: partials[q*P + block],
+// q = 0: sum w (gamma - 1) m, 1..3: sum w p (updateEnergy,
+// PIC++/simulation.cpp:1590-1600).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_particle_sums(PartView<T> p, double m, double w, double* __restrict__ partials,
+                                                               int P) {
+    __shared__ double sh[32];
+    double s[4] = {0, 0, 0, 0};
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n; n += (long long)gridDim.x * blockDim.x) {
+        double px = p.px[n], py = p.py[n], pz = p.pz[n];
+        double p2 = px * px + py * py + pz * pz;
+        double gam = sqrt(p2 / (m * m) + 1.0);
+        s[0] += (gam - 1) * m * w;
+        s[1] += px * w; s[2] += py * w; s[3] += pz * w;
+    }
+    for (int q = 0; q < 4; ++q) {
+        double r = block_sum(s[q], sh);
+        if (threadIdx.x == 0) partials[q * P + blockIdx.x] = r;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_sq_partials(const T* __restrict__ a, long long n, double* __restrict__ partials) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double v = double(a[i]);
+        s += v * v;
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void k_convert(const double* __restrict__ s, T* __restrict__ d, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = T(s[i]);
+}
+template <typename T>
+__global__ void k_convert_back(const T* __restrict__ s, double* __restrict__ d, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = double(s[i]);
+}
+
+// flag bits: 1 cell out of range, 2 offset outside [0,1), 4 non-finite momentum
+template <typename T>
+__global__ void k_validate(GridP g, PartView<T> p, int* __restrict__ flag) {
+    int bad = 0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n; n += (long long)gridDim.x * blockDim.x) {
+        int c = p.cell[n];
+        if (c < 0 || c >= g.N) bad |= 1;
+        T o[3] = {p.ox[n], p.oy[n], p.oz[n]};
+        for (int a = 0; a < 3; ++a)
+            if (!(o[a] >= T(0) && o[a] < T(1))) bad |= 2;
+        T m[3] = {p.px[n], p.py[n], p.pz[n]};
+        for (int a = 0; a < 3; ++a)
+            if (!isfinite(m[a])) bad |= 4;
+    }
+    if (bad) atomicOr(flag, bad);
+}
+
+template <typename T>
+__global__ void k_iota(int* __restrict__ a, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        a[i] = (int)i;
+}
+
+template <typename T>
+void PK<T>::validate(cudaStream_t s, const GridP& g, PartView<T> p, int* flag) {
+    if (p.n == 0) return;
+    k_validate<T><<<grid_for(p.n, 256, 16), 256, 0, s>>>(g, p, flag);
+}
+
+template <typename T>
+void PK<T>::iota(cudaStream_t s, int* a, long long n) {
+    if (n == 0) return;
+    k_iota<T><<<grid_for(n, 256, 16), 256, 0, s>>>(a, n);
+}
+
+template <typename T>
+void PK<T>::yee_b_half(cudaStream_t s, const GridP& g, const void* E, void* B) {
+    const T cdtd2 = T(g.cfix * g.dt / 2.0);
+    k_yee_b_half<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, (const T*)E, (T*)B, cdtd2, T(g.dx), T(g.dy), T(g.dz),
+                                                      T(g.idx), T(g.idy), T(g.idz));
+}
+
+template <typename T>
+void PK<T>::yee_e(cudaStream_t s, const GridP& g, void* E, const void* B, const double* J) {
+    k_yee_e<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, (T*)E, (const T*)B, J, T(g.cfix), T(g.dt), T(g.dx), T(g.dy),
+                                                 T(g.dz), T(g.idx), T(g.idy), T(g.idz));
+}
+
+template <typename T>
+void PK<T>::boris_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const void* E, const void* B) {
+    if (p.n == 0) return;
+    k_boris_push<T, T><<<grid_for(p.n, 256, 32), 256, 0, s>>>(g, p, T(q), T(m), (const T*)E, (const T*)B);
+}
+
+template <typename T>
+void PK<T>::zigzag(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w, double* J) {
+    if (p.n == 0) return;
+    k_zigzag<T><<<grid_for(p.n, 256, 32), 256, 0, s>>>(g, p, T(q), T(m), T(w), J);
+}
+
+template <typename T>
+size_t PK<T>::tile_smem_bytes(const TileShape& sh) {
+    size_t F = (size_t)sh.fx * sh.fy * sh.fz;
+    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + 3 * (size_t)sh.jcells * sizeof(T);
+}
+
+template <typename T>
+void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh,
+                               const SpeciesSet<T>& S, const void* E, const void* B, T* Jpart, double* Jfix,
+                               int grid, size_t smem) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_push_deposit_tile<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_push_deposit_tile<T, T><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix);
+}
+
+template <typename T>
+void PK<T>::assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const T* Jpart,
+                       const double* Jfix, double* J) {
+    k_assemble_j<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, t, sh, Jpart, Jfix, J);
+}
+
+template <typename T>
+void PK<T>::implicit_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w,
+                             const double* E, const double* B, double* J, double* mu, double* rho, double* Pi,
+                             int compat, const GhostAxes& ga) {
+    if (p.n == 0) return;
+    k_implicit_deposit<T><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, w, E, B, J, mu, rho, Pi, compat, ga);
+}
+
+template <typename T>
+void PK<T>::implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const double* E,
+                          const double* B, const double* Et) {
+    if (p.n == 0) return;
+    k_implicit_push<T><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, E, B, Et);
+}
+
+template <typename T>
+void PK<T>::gather_payload(cudaStream_t s, const int* perm, long long n, PartView<T> src, PartView<T> dst) {
+    if (n == 0) return;
+    k_gather_payload<T><<<grid_for(n, 256, 32), 256, 0, s>>>(perm, n, src, dst);
+}
+
+template <typename T>
+void PK<T>::particle_sums(cudaStream_t s, PartView<T> p, double m, double w, double* partials, int P) {
+    k_particle_sums<T><<<P, kRedThreads, 0, s>>>(p, m, w, partials, P);
+}
+
+template <typename T>
+void PK<T>::field_sq_partials(cudaStream_t s, const void* F, long long n, double* partials, int P) {
+    k_sq_partials<T><<<P, kRedThreads, 0, s>>>((const T*)F, n, partials);
+}
+
+template <typename T>
+void PK<T>::to_real(cudaStream_t s, const double* src, void* dst, long long n) {
+    if (n == 0) return;
+    k_convert<T><<<grid_for(n, 256), 256, 0, s>>>(src, (T*)dst, n);
+}
+
+template <typename T>
+void PK<T>::from_real(cudaStream_t s, const void* src, double* dst, long long n) {
+    if (n == 0) return;
+    k_convert_back<T><<<grid_for(n, 256), 256, 0, s>>>((const T*)src, dst, n);
+}
+
+}  // namespace pic

@@ -1,0 +1,40 @@
+// solver.hpp -- FP64 Krylov solvers of the implicit Maxwell system on the GPU.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/picpp_gb300.h"
+#include "kernels.hpp"
+
+namespace pic {
+
+// Device workspace, grown on demand and kept for the context's lifetime.
+struct Krylov {
+    double* V = nullptr;      // basis, cap vectors of length L
+    double* Z = nullptr;      // preconditioned directions (flexible GMRES)
+    double* w = nullptr;      // scratch vector
+    double* r = nullptr;      // residual
+    double* hdev = nullptr;   // Hessenberg column (device), 2 * (cap + 1)
+    double* ydev = nullptr;   // combination coefficients
+    double* part = nullptr;   // reduction partials, (cap + 2) * 1024
+    double* scal = nullptr;   // scalar results
+    int cap = 0;
+    int zcap = 0;
+    long long L = 0;
+};
+
+struct SolveCtx {
+    cudaStream_t s;
+    const GridP* g;
+    const double* mu;
+    double* partials;   // >= 8 * 1024 doubles
+    int* flag;
+    Krylov* k;
+    std::string* err;
+};
+
+OpCoef make_opcoef(const GridP& g);
+pic_status krylov_solve(SolveCtx& c, const double* rhs, double* x, const pic_solve_opts& o, pic_solve_info* info);
+void krylov_free(Krylov& k);
+
+}  // namespace pic

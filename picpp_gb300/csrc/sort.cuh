@@ -1,0 +1,163 @@
+// sort.cuh -- stable, deterministic counting sort of particles by cell.
+//
+// The reference keeps particles in an unordered std::vector<Particle*>; the
+// GPU keeps each species in SoA arrays ordered by a tile-major cell key so
+// that a tile's particles are contiguous.  The sort is bit-exact with the
+// oracle's stable counting sort:
+//   1. key per particle, histogram (integer atomics: exact counts)
+//   2. exclusive scan of the counts (3-phase block scan)
+//   3. scatter of source indices with one atomic cursor per key
+//      (arbitrary order inside a key), then
+//   4. per-key segment sort of the source indices by rank counting, which
+//      restores input order inside every key: stable and run-independent
+//   5. gather of the payload arrays through the permutation.
+#pragma once
+#include "common.cuh"
+#include "types.cuh"
+
+namespace pic {
+
+__device__ __forceinline__ int sort_key(const GridP& g, const TileGeom& t, int cell) {
+    int i, j, k;
+    decode(g, cell, i, j, k);
+    int ti = i / t.tx, tj = j / t.ty, tk = k / t.tz;
+    int li = i - ti * t.tx, lj = j - tj * t.ty, lk = k - tk * t.tz;
+    int tile = (tk * t.nty + tj) * t.ntx + ti;
+    int local = (lk * t.ty + lj) * t.tx + li;
+    return tile * (t.tx * t.ty * t.tz) + local;
+}
+
+__global__ void k_keys_hist(GridP g, TileGeom t, const int* __restrict__ cell, long long n, int* __restrict__ key,
+                            int* __restrict__ counts) {
+    for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < n; a += (long long)gridDim.x * blockDim.x) {
+        int kk = sort_key(g, t, cell[a]);
+        key[a] = kk;
+        atomicAdd(&counts[kk], 1);
+    }
+}
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;   // per thread -> 2048 per block
+
+__device__ __forceinline__ int block_excl_scan(int v, int* sh, int& total) {
+    // warp inclusive scan
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int s = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sh[lane] = s;   // inclusive warp totals
+    }
+    __syncthreads();
+    int warp_off = wid > 0 ? sh[wid - 1] : 0;
+    total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_off + x - v;
+}
+
+// in-place exclusive scan, phase 1: per-block scan, block totals out.
+__global__ void __launch_bounds__(kScanThreads) k_scan_blocks(int* __restrict__ a, long long n, int* __restrict__ block_sums) {
+    __shared__ int sh[32];
+    long long base = (long long)blockIdx.x * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        v[q] = (base + q < n) ? a[base + q] : 0;
+        s += v[q];
+    }
+    int total;
+    int off = block_excl_scan(s, sh, total);
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        if (base + q < n) a[base + q] = off;
+        off += v[q];
+    }
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// phase 2: exclusive scan of the block totals by one block (any count).
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(int* __restrict__ s, int nb, int* __restrict__ grand_total) {
+    __shared__ int sh[32];
+    int carry = 0;
+    for (int base = 0; base < nb; base += kScanThreads) {
+        int idx = base + threadIdx.x;
+        int v = idx < nb ? s[idx] : 0;
+        int total;
+        int off = block_excl_scan(v, sh, total);
+        if (idx < nb) s[idx] = carry + off;
+        carry += total;
+    }
+    if (threadIdx.x == 0 && grand_total) *grand_total = carry;
+}
+
+// phase 3: add block offsets.
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(int* __restrict__ a, long long n, const int* __restrict__ block_sums) {
+    long long base = (long long)blockIdx.x * kScanThreads * kScanItems;
+    int add = block_sums[blockIdx.x];
+    for (int q = threadIdx.x; q < kScanThreads * kScanItems; q += kScanThreads)
+        if (base + q < n) a[base + q] += add;
+}
+
+__global__ void k_scatter_atomic(const int* __restrict__ key, long long n, int* __restrict__ cursor, int* __restrict__ tmp) {
+    for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < n; a += (long long)gridDim.x * blockDim.x) {
+        int pos = atomicAdd(&cursor[key[a]], 1);
+        tmp[pos] = (int)a;
+    }
+}
+
+// Rank-count sort of each key segment [off[k], off[k+1]) of tmp into perm:
+// element x goes to off[k] + #{y in segment : y < x}.  Segments up to
+// kWarpSeg elements use one warp; longer ones are left to k_segsort_block.
+constexpr int kWarpSeg = 256;
+__global__ void k_segsort_warp(const int* __restrict__ off, int nkeys, const int* __restrict__ tmp, int* __restrict__ perm,
+                               int* __restrict__ long_count, int* __restrict__ long_list) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long kk = warp; kk < nkeys; kk += nwarps) {
+        int b = off[kk], e = off[kk + 1];
+        int len = e - b;
+        if (len <= 0) continue;
+        if (len == 1) { if (lane == 0) perm[b] = tmp[b]; continue; }
+        if (len > kWarpSeg) {
+            if (lane == 0) { int slot = atomicAdd(long_count, 1); long_list[slot] = (int)kk; }
+            continue;
+        }
+        for (int a = lane; a < len; a += 32) {
+            int x = tmp[b + a];
+            int r = 0;
+            for (int c = 0; c < len; ++c) r += tmp[b + c] < x;
+            perm[b + r] = x;
+        }
+    }
+}
+
+__global__ void k_segsort_block(const int* __restrict__ off, const int* __restrict__ long_list, const int* __restrict__ long_count,
+                                const int* __restrict__ tmp, int* __restrict__ perm) {
+    const int cnt = *long_count;
+    for (int s = blockIdx.x; s < cnt; s += gridDim.x) {
+        int kk = long_list[s];
+        int b = off[kk], e = off[kk + 1];
+        int len = e - b;
+        for (int a = threadIdx.x; a < len; a += blockDim.x) {
+            int x = tmp[b + a];
+            int r = 0;
+            for (int c = 0; c < len; ++c) r += tmp[b + c] < x;
+            perm[b + r] = x;
+        }
+    }
+}
+
+}  // namespace pic

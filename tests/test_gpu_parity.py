@@ -1,0 +1,346 @@
+"""CUDA path against the oracle, through the C ABI.  Needs a GB300."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from fixtures import copy_species, golden_names, load, periodic_dist, rel_err
+from picpp_gb300 import initstate as I
+
+pytestmark = pytest.mark.gpu
+
+# Tolerances.  FP64 path: rounding-level differences only (different
+# summation order in deposits and reductions).  FP32 push: relative to the
+# field/momentum scale after the stated number of steps.
+TOL64 = 1e-11
+TOL32 = 2e-5
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import picpp_gb300 as P
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    P.load_library()
+    return P
+
+
+def noisy(st, amp=0.05, seed=9):
+    rng = np.random.default_rng(seed)
+    st.E = st.E + amp * rng.standard_normal(st.E.shape)
+    st.B = st.B + amp * rng.standard_normal(st.B.shape)
+    return st
+
+
+def by_id(d):
+    o = np.argsort(d["id"])
+    return {k: v[o] for k, v in d.items()}
+
+
+def oracle_buneman(st, steps):
+    g = O.make_grid(st.box)
+    sp = copy_species(st.species)
+    E, B = st.E.copy(), st.B.copy()
+    J = None
+    for _ in range(steps):
+        J = O.buneman_step(g, sp, E, B)
+    return sp, E, B, J
+
+
+def compare_particles(box, gpu, ref, tol_p, tol_x):
+    L = (box.nx * box.dx, box.ny * box.dy, box.nz * box.dz)
+    x, y, z = I.positions(box, gpu)
+    xr, yr, zr = I.positions(box, ref)
+    for a, r, l, d in ((x, xr, L[0], box.dx), (y, yr, L[1], box.dy), (z, zr, L[2], box.dz)):
+        assert periodic_dist(a, r, l).max() <= tol_x * d
+    for k in ("px", "py", "pz"):
+        assert rel_err(gpu[k], ref[k]) <= tol_p
+
+
+@pytest.mark.parametrize("real", [1, 0])
+def test_buneman_phase_calls_match_oracle(pg, real):
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=4, seed=31))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real, sort_every=0)
+    sim.upload_state(st)
+    steps = 2
+    for _ in range(steps):
+        sim.tristanEvaluateBhalfStep()
+        sim.moveParticles()
+        sim.tristanEvaluateBhalfStep()
+        sim.tristanUpdateFlux()
+        sim.tristanEvaluateE()
+    E, B, J = sim.download_fields()
+    sp, Eo, Bo, Jo = oracle_buneman(st, steps)
+    tol = TOL64 if real else TOL32
+    assert rel_err(E, Eo) < tol
+    assert rel_err(B, Bo) < tol
+    assert rel_err(J, Jo.reshape(J.shape)) < tol
+    for s in range(2):
+        compare_particles(st.box, sim.download_particles(s), sp[s], tol, 1e-10 if real else 1e-5)
+
+
+def test_buneman_fp64_push_is_bit_identical_to_oracle(pg):
+    """With the same fields, the FP64 Boris push reproduces the oracle bit for
+    bit: every multiply/add is separately rounded in both (no FMA)."""
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=4, seed=32))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=0)
+    sim.upload_state(st)
+    sim.moveParticles()
+    g = O.make_grid(st.box)
+    for s, sp in enumerate(copy_species(st.species)):
+        ps = O._as_particles(sp)
+        O.lib().orc_boris_push(O.C.byref(g), O.C.byref(ps), O._d(st.E), O._d(st.B))
+        out = sim.download_particles(s)
+        assert np.array_equal(out["cell"], sp["cell"])
+        for k in ("ox", "oy", "oz", "px", "py", "pz"):
+            assert np.array_equal(out[k], sp[k]), k
+
+
+@pytest.mark.parametrize("real,steps", [(1, 3), (0, 3)])
+def test_buneman_fused_step_matches_oracle(pg, real, steps):
+    st = noisy(I.buneman_plasma(16, 8, 8, ppc=4, seed=33))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real, sort_every=1, tile=(8, 4, 4))
+    sim.upload_state(st)
+    sim.buneman_step(steps)
+    E, B, J = sim.download_fields()
+    sp, Eo, Bo, Jo = oracle_buneman(st, steps)
+    tol = TOL64 if real else 1e-4
+    assert rel_err(E, Eo) < tol
+    assert rel_err(B, Bo) < tol
+    assert rel_err(J, Jo.reshape(J.shape)) < tol
+    for s in range(2):
+        got = by_id(sim.download_particles(s))
+        compare_particles(st.box, got, sp[s], tol, 1e-10 if real else 2e-5)
+
+
+def test_buneman_reduced_dimension_matches_oracle(pg):
+    st = noisy(I.buneman_plasma(16, 8, 1, ppc=4, seed=34))
+    for sort_every in (0, 1):
+        sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=sort_every, tile=(8, 8, 1))
+        sim.upload_state(st)
+        sim.buneman_step(2)
+        E, B, J = sim.download_fields()
+        sp, Eo, Bo, Jo = oracle_buneman(st, 2)
+        assert rel_err(E, Eo) < TOL64
+        assert rel_err(B, Bo) < TOL64
+        for s in range(2):
+            got = by_id(sim.download_particles(s))
+            for k in ("px", "py", "pz"):
+                assert rel_err(got[k], sp[s][k]) < TOL64
+
+
+@pytest.mark.parametrize("name", golden_names("buneman"))
+def test_buneman_golden_vectors(pg, name):
+    """The GPU FP64 path against outputs of the reference itself."""
+    f = load(name)
+    st = f["state"]
+    t = tuple(min(8, n) for n in (st.box.nx, st.box.ny, st.box.nz))
+    t = tuple(tt if n % tt == 0 else 1 for tt, n in zip(t, (st.box.nx, st.box.ny, st.box.nz)))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=1, tile=t)
+    sim.upload_state(st)
+    sim.buneman_step(f["steps"])
+    E, B, J = sim.download_fields()
+    assert rel_err(E, f["E"]) < 1e-10
+    assert rel_err(B, f["B"]) < 1e-10
+    assert rel_err(J, f["extra"]["J"]) < 1e-10
+    L = (st.box.nx * st.box.dx, st.box.ny * st.box.dy, st.box.nz * st.box.dz)
+    for s, o in enumerate(f["out"]):
+        got = by_id(sim.download_particles(s))
+        x, y, z = I.positions(st.box, got)
+        assert periodic_dist(x, o["x"], L[0]).max() < 1e-11
+        for k in ("px", "py", "pz"):
+            assert rel_err(got[k], o[k]) < 1e-10
+
+
+def test_sort_is_bit_exact_with_oracle(pg):
+    box = I.Box(16, 8, 8, 0.1, 0.1, 0.1, 0.01)
+    rng = np.random.default_rng(5)
+    n = 20000
+    sp = dict(q=-1.0, m=1.0, w=1.0, cell=rng.integers(0, box.ncells, n).astype(np.int32),
+              ox=rng.random(n), oy=rng.random(n), oz=rng.random(n),
+              px=rng.standard_normal(n), py=rng.standard_normal(n), pz=rng.standard_normal(n))
+    # a crowded cell, longer than one warp's segment
+    sp["cell"][:700] = 37
+    sim = pg.GpuSimulation(box, pg.BUNEMAN, particle_real=1, sort_every=0, tile=(8, 4, 4))
+    sid = sim.add_species(sp["q"], sp["m"], sp["w"], n)
+    sim.upload_particles(sid, sp)
+    sim.sort()
+    perm = sim.download_permutation(sid)
+    g = O.make_grid(box, tile=(8, 4, 4))
+    ref = O.counting_sort(g, sp["cell"])
+    assert np.array_equal(perm.astype(np.int64), ref)
+    out = sim.download_particles(sid)
+    assert np.array_equal(out["cell"], sp["cell"][ref])
+    assert np.array_equal(out["id"], ref.astype(np.int32))
+    assert np.array_equal(out["px"], sp["px"][ref])
+
+
+def implicit_state(nx=8, ny=6, nz=5, ppc=3, seed=41, gamma=2.0):
+    return noisy(I.beams_plasma(nx, ny, nz, ppc=ppc, beam_gamma=gamma, dt=0.2, seed=seed), seed=seed + 1)
+
+
+@pytest.mark.parametrize("compat", [1, 0])
+def test_implicit_moments_and_rhs_match_oracle(pg, compat):
+    st = implicit_state()
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, pressure_compat=compat, sort_every=0)
+    sim.upload_state(st)
+    sim.updateElectroMagneticParameters()
+    J, mu, rho, rhs = sim.download_moments()
+    g = O.make_grid(st.box, pressure_compat=compat)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    Jo, muo, rhoo, Pio, raw = O.implicit_moments(g, copy_species(st.species), E, B)
+    rhso = O.maxwell_rhs(g, E, B, Jo, rhoo)
+    assert rel_err(mu, muo) < 1e-12
+    assert rel_err(J, Jo) < 1e-12
+    assert rel_err(rho, rhoo) < 1e-12
+    assert rel_err(rhs, rhso) < 1e-12
+
+
+def test_maxwell_operator_matches_oracle(pg):
+    box = I.Box(7, 6, 5, 0.5, 0.5, 0.5, 0.5)
+    rng = np.random.default_rng(2)
+    N = box.ncells
+    mu = -0.2 * rng.random(9 * N)
+    x = rng.standard_normal(3 * N)
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    y = sim.maxwell_apply(mu, x)
+    yo = O.maxwell_apply(O.make_grid(box), mu, x)
+    assert rel_err(y, yo) < 1e-13
+
+
+def test_gmres_reference_semantics_match_oracle(pg):
+    box = I.Box(6, 6, 6, 0.5, 0.5, 0.5, 0.5)
+    rng = np.random.default_rng(3)
+    N = box.ncells
+    mu = np.zeros(9 * N)
+    for a in range(3):
+        mu[4 * a * N:(4 * a + 1) * N] = -0.5 * rng.random(N)
+    mu += -0.02 * rng.random(9 * N)
+    rhs = rng.standard_normal(3 * N)
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    x, info = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.GMRES_REFERENCE, max_iter=50, tol=1e-8))
+    xo, it, relo = O.gmres(O.make_grid(box), mu, rhs)
+    assert info["iterations"] == it
+    assert rel_err(x, xo) < 1e-9
+
+
+def test_gmres_restarted_reaches_true_residual(pg):
+    box = I.Box(8, 8, 8, 0.5, 0.5, 0.5, 0.5)
+    rng = np.random.default_rng(4)
+    N = box.ncells
+    mu = np.zeros(9 * N)
+    for a in range(3):
+        mu[4 * a * N:(4 * a + 1) * N] = -0.8 * rng.random(N)
+    rhs = rng.standard_normal(3 * N)
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    x, info = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.GMRES_RESTARTED, restart=10, max_iter=2000, tol=1e-8))
+    r = O.maxwell_apply(O.make_grid(box), mu, x) - rhs
+    assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1e-8 * 1.01
+    assert info["rel_residual"] <= 1e-8
+    assert info["restarts"] >= 1
+
+
+@pytest.mark.parametrize("real", [1, 0])
+def test_implicit_step_matches_oracle(pg, real):
+    st = implicit_state(ppc=2)
+    steps = 2
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, sort_every=1, tile=(8, 6, 5))
+    sim.upload_state(st)
+    for _ in range(steps):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    E, B, _ = sim.download_fields()
+    g = O.make_grid(st.box)
+    sp = copy_species(st.species)
+    Eo, Bo = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(steps):
+        O.implicit_step(g, sp, Eo, Bo)
+    tol = 1e-9 if real else 1e-4
+    assert rel_err(E.reshape(-1), Eo) < tol
+    assert rel_err(B.reshape(-1), Bo) < tol
+    for s in range(2):
+        got = by_id(sim.download_particles(s))
+        compare_particles(st.box, got, sp[s], tol, 1e-8 if real else 1e-4)
+
+
+@pytest.mark.parametrize("name", golden_names("implicit"))
+def test_implicit_golden_vectors(pg, name):
+    f = load(name)
+    st = f["state"]
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, sort_every=0)
+    sim.upload_state(st)
+    for _ in range(f["steps"]):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    E, B, _ = sim.download_fields()
+    assert rel_err(E, f["E"]) < 1e-9
+    assert rel_err(B, f["B"]) < 1e-9
+    for s, o in enumerate(f["out"]):
+        got = by_id(sim.download_particles(s))
+        for k in ("px", "py", "pz"):
+            assert rel_err(got[k], o[k]) < 1e-9
+
+
+def test_energy_matches_oracle(pg):
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=4, seed=35))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=0)
+    sim.upload_state(st)
+    e = sim.updateEnergy()
+    eo = O.energy(O.make_grid(st.box), copy_species(st.species), st.E, st.B)
+    assert np.allclose(e, eo, rtol=1e-12, atol=1e-14)
+
+
+def test_bad_inputs_are_rejected(pg):
+    box = I.Box(8, 8, 8, 0.1, 0.1, 0.1, 0.01)
+    sim = pg.GpuSimulation(box, pg.BUNEMAN, particle_real=0)
+    sid = sim.add_species(-1.0, 1.0, 1.0, 10)
+    n = 10
+    good = dict(cell=np.zeros(n, np.int32), ox=np.full(n, 0.5), oy=np.full(n, 0.5), oz=np.full(n, 0.5),
+                px=np.zeros(n), py=np.zeros(n), pz=np.zeros(n))
+    sim.upload_particles(sid, good)
+    bad = dict(good, ox=np.full(n, 1.0))
+    with pytest.raises(pg.PicError) as e:
+        sim.upload_particles(sid, bad)
+    assert e.value.status == 1
+    bad = dict(good, cell=np.full(n, box.ncells, np.int32))
+    with pytest.raises(pg.PicError) as e:
+        sim.upload_particles(sid, bad)
+    assert e.value.status == 1
+    bad = dict(good, px=np.full(n, np.nan))
+    with pytest.raises(pg.PicError) as e:
+        sim.upload_particles(sid, bad)
+    assert e.value.status == 5
+    big = {k: np.concatenate([v, v]) for k, v in good.items()}
+    with pytest.raises(pg.PicError) as e:
+        sim.upload_particles(sid, big)
+    assert e.value.status == 4
+    E = np.zeros((3, 8, 8, 8)); E[0, 0, 0, 0] = np.inf
+    with pytest.raises(pg.PicError) as e:
+        sim.upload_fields(E, np.zeros_like(E))
+    assert e.value.status == 5
+
+
+def test_empty_species_and_no_particles(pg):
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=1, seed=36))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=1)
+    sim.add_species(-1.0, 1.0, 1.0, 0)
+    sim.upload_fields(st.E, st.B)
+    sim.buneman_step(2)
+    E, B, J = sim.download_fields()
+    g = O.make_grid(st.box)
+    Eo, Bo = st.E.copy(), st.B.copy()
+    for _ in range(2):
+        O.buneman_step(g, [], Eo, Bo)
+    assert rel_err(E, Eo) < TOL64
+    assert np.all(J == 0)
+
+
+def test_implicit_solver_rejects_nonfinite_rhs(pg):
+    box = I.Box(5, 5, 5, 0.5, 0.5, 0.5, 0.5)
+    N = box.ncells
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    rhs = np.ones(3 * N); rhs[7] = np.nan
+    with pytest.raises(pg.PicError) as e:
+        sim.maxwell_solve(np.zeros(9 * N), rhs)
+    assert e.value.status == 5
+    # the context stays usable
+    x, info = sim.maxwell_solve(np.zeros(9 * N), np.ones(3 * N))
+    assert np.all(np.isfinite(x))

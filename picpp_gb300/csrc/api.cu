@@ -333,7 +333,11 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     int tile[3];
     const int n3[3] = {c.nx, c.ny, c.nz};
     for (int a = 0; a < 3; ++a) {
-        int t = c.tile[a] > 0 ? c.tile[a] : 8;
+        int t = c.tile[a];
+        if (t <= 0) {   // default: the largest of 8, 4, 2, 1 dividing the axis
+            t = 8;
+            while (t > 1 && n3[a] % t != 0) t /= 2;
+        }
         if (t > n3[a]) t = n3[a];
         if (n3[a] % t != 0) return PIC_ERR_ARG;
         tile[a] = t;
@@ -487,6 +491,9 @@ pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, 
     }
     const double* src[6] = {ox, oy, oz, px, py, pz};
     const long long chunk = std::min<long long>(kStageChunk, ctx->stage_len);
+    // validation on the device: cell range, offsets in [0,1), finite momenta;
+    // FP32 conversion checks the FP64 values before rounding
+    CK(cudaMemsetAsync(ctx->flag, 0, sizeof(int), s));
     for (int q = 0; q < 6; ++q) {
         if (ctx->preal) {
             CK(cudaMemcpyAsync(sp.a[q], src[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -495,11 +502,9 @@ pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, 
         for (long long b = 0; b < n; b += chunk) {
             long long len = std::min<long long>(chunk, n - b);
             CK(cudaMemcpyAsync(ctx->stage, src[q] + b, sizeof(double) * len, cudaMemcpyHostToDevice, s));
-            PK<float>::to_real(s, ctx->stage, (float*)sp.a[q] + b, len);
+            PK<float>::to_real_checked(s, ctx->stage, (float*)sp.a[q] + b, len, q < 3 ? 0 : 1, ctx->flag);
         }
     }
-    // validate on the device: cell range, offsets in [0,1), finite momenta
-    CK(cudaMemsetAsync(ctx->flag, 0, sizeof(int), s));
     sp.n = n;
     if (ctx->preal) PK<double>::validate(s, ctx->g, view<double>(sp), ctx->flag);
     else PK<float>::validate(s, ctx->g, view<float>(sp), ctx->flag);

@@ -161,20 +161,25 @@ __global__ void __launch_bounds__(256) k_assemble_j(GridP g, TileGeom t, TileSha
         const int nt[3] = {t.ntx, t.nty, t.ntz};
         const int je[3] = {s.jx, s.jy, s.jz};
         const int hg[3] = {s.gx, s.gy, s.gz};
-        // per axis: up to 6 (tile, local) candidates
-        int cand_t[3][6], cand_l[3][6], cnt[3];
+        // per axis: every (tile, local index) whose current block holds this
+        // cell or one of its periodic images, in increasing image order
+        constexpr int kCand = 16;
+        int cand_t[3][kCand], cand_l[3][kCand], cnt[3];
         for (int ax = 0; ax < 3; ++ax) {
             cnt[ax] = 0;
-            for (int T = 0; T < nt[ax]; ++T) {
-                // only tiles near the cell can cover it; test a small window
-                int tc = p[ax] / te[ax];
-                int dT = T - tc;
-                if (nt[ax] > 4 && !(dT >= -1 && dT <= 1) && !(dT == nt[ax] - 1) && !(dT == -(nt[ax] - 1))) continue;
-                for (int sh = -1; sh <= 1; ++sh) {
-                    int local = p[ax] + sh * n[ax] - (T * te[ax] - hg[ax]);
-                    if (local >= 0 && local < je[ax] && cnt[ax] < 6) {
-                        cand_t[ax][cnt[ax]] = T; cand_l[ax][cnt[ax]] = local; cnt[ax]++;
-                    }
+            for (int sh = -1; sh <= 1; ++sh) {
+                const int q = p[ax] + sh * n[ax];
+                // block of tile T spans [T*te - hg, T*te - hg + je)
+                int tlo = q + hg[ax] - je[ax] + 1;
+                tlo = tlo >= 0 ? (tlo + te[ax] - 1) / te[ax] : -((-tlo) / te[ax]);
+                int thi = q + hg[ax];
+                thi = thi >= 0 ? thi / te[ax] : -((-thi + te[ax] - 1) / te[ax]);
+                if (tlo < 0) tlo = 0;
+                if (thi > nt[ax] - 1) thi = nt[ax] - 1;
+                for (int T = tlo; T <= thi && cnt[ax] < kCand; ++T) {
+                    cand_t[ax][cnt[ax]] = T;
+                    cand_l[ax][cnt[ax]] = q - (T * te[ax] - hg[ax]);
+                    cnt[ax]++;
                 }
             }
         }

@@ -51,6 +51,7 @@ struct PK {
     static void particle_sums(cudaStream_t s, PartView<T> p, double m, double w, double* partials, int P);
     static void field_sq_partials(cudaStream_t s, const void* F, long long n, double* partials, int P);
     static void to_real(cudaStream_t s, const double* src, void* dst, long long n);
+    static void to_real_checked(cudaStream_t s, const double* src, void* dst, long long n, int mode, int* flag);
     static void from_real(cudaStream_t s, const void* src, double* dst, long long n);
     static void validate(cudaStream_t s, const GridP& g, PartView<T> p, int* flag);
     static void iota(cudaStream_t s, int* a, long long n);

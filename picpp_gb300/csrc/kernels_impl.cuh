@@ -58,6 +58,28 @@ __global__ void k_convert(const double* __restrict__ s, T* __restrict__ d, long 
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         d[i] = T(s[i]);
 }
+// FP64 host values to the particle precision with the range checks of
+// k_validate done on the FP64 values: mode 0 in-cell offsets (must lie in
+// [0,1); an offset that rounds up to 1 in T is kept just below 1), mode 1
+// momenta (must be finite).
+template <typename T>
+__global__ void k_convert_checked(const double* __restrict__ s, T* __restrict__ d, long long n, int mode,
+                                  int* __restrict__ flag) {
+    int bad = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double v = s[i];
+        T t = T(v);
+        if (mode == 0) {
+            if (!(v >= 0.0 && v < 1.0)) bad |= 2;
+            if (t >= T(1)) t = T(1) - T(1) / T(1 << 24);   // largest float below 1 (0.99999994)
+        } else if (!isfinite(v)) {
+            bad |= 4;
+        }
+        d[i] = t;
+    }
+    if (bad) atomicOr(flag, bad);
+}
+
 template <typename T>
 __global__ void k_convert_back(const T* __restrict__ s, double* __restrict__ d, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -183,6 +205,12 @@ template <typename T>
 void PK<T>::to_real(cudaStream_t s, const double* src, void* dst, long long n) {
     if (n == 0) return;
     k_convert<T><<<grid_for(n, 256), 256, 0, s>>>(src, (T*)dst, n);
+}
+
+template <typename T>
+void PK<T>::to_real_checked(cudaStream_t s, const double* src, void* dst, long long n, int mode, int* flag) {
+    if (n == 0) return;
+    k_convert_checked<T><<<grid_for(n, 256), 256, 0, s>>>(src, (T*)dst, n, mode, flag);
 }
 
 template <typename T>

@@ -1,0 +1,100 @@
+// picpp_gb300_simulation.hpp -- header-only C++ mirror of the hot-path member
+// functions of PIC++'s class Simulation (PIC++/simulation.h:32-1152) over the
+// C ABI of picpp_gb300.h.  A C++ caller that used Simulation's step loop
+// (PIC++/simulation.cpp:164-259) keeps the same call sequence:
+//
+//   picpp::GpuSimulation sim(cfg);
+//   sim.addSpecies(q, m, w, n); sim.uploadParticles(0, ...); sim.uploadFields(E, B);
+//   sim.tristanEvaluateBhalfStep(); sim.moveParticles(); sim.tristanEvaluateBhalfStep();
+//   sim.tristanUpdateFlux(); sim.tristanEvaluateE();
+//
+// Errors throw picpp::Error (status + message) instead of the reference's
+// print-and-exit (PIC++/util.cpp:119-129).
+#pragma once
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "picpp_gb300.h"
+
+namespace picpp {
+
+class Error : public std::runtime_error {
+public:
+    Error(pic_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+    pic_status status;
+};
+
+class GpuSimulation {
+public:
+    explicit GpuSimulation(const pic_config& cfg) {
+        pic_status s = pic_create(&cfg, &ctx_);
+        if (s != PIC_OK) throw Error(s, "pic_create failed");
+    }
+    ~GpuSimulation() { pic_destroy(ctx_); }
+    GpuSimulation(const GpuSimulation&) = delete;
+    GpuSimulation& operator=(const GpuSimulation&) = delete;
+
+    pic_ctx* handle() const { return ctx_; }
+
+    int addSpecies(double q, double m, double w, long capacity) {
+        int id = -1;
+        check(pic_add_species(ctx_, q, m, w, capacity, &id));
+        return id;
+    }
+    void uploadParticles(int species, long n, const int* cell, const double* ox, const double* oy, const double* oz,
+                         const double* px, const double* py, const double* pz, const int* ids = nullptr) {
+        check(pic_upload_particles(ctx_, species, n, cell, ox, oy, oz, px, py, pz, ids));
+    }
+    long downloadParticles(int species, int* cell, double* ox, double* oy, double* oz, double* px, double* py,
+                           double* pz, int* ids = nullptr) {
+        long n = 0;
+        check(pic_download_particles(ctx_, species, &n, cell, ox, oy, oz, px, py, pz, ids));
+        return n;
+    }
+    void uploadFields(const double* E, const double* B) { check(pic_upload_fields(ctx_, E, B)); }
+    void downloadFields(double* E, double* B, double* J) { check(pic_download_fields(ctx_, E, B, J)); }
+
+    // explicit Buneman / Tristan phases (PIC++/simulation.cpp:164-204)
+    void tristanEvaluateBhalfStep() { check(pic_tristan_evaluate_b_half_step(ctx_)); }
+    void moveParticles() { check(pic_move_particles(ctx_)); }
+    void tristanUpdateFlux() { check(pic_tristan_update_flux(ctx_)); }
+    void tristanEvaluateE() { check(pic_tristan_evaluate_e(ctx_)); }
+    void bunemanSteps(int n) { check(pic_buneman_step(ctx_, n)); }
+
+    // implicit phases (PIC++/simulation.cpp:205-259).  The rotation tensor
+    // of evaluateParticlesRotationTensor is recomputed inside the deposit and
+    // the mover, so that call has nothing left to do on its own.
+    void evaluateParticlesRotationTensor() {}
+    void updateElectroMagneticParameters() { check(pic_update_electromagnetic_parameters(ctx_)); }
+    pic_solve_info evaluateElectricField(const pic_solve_opts& opts = defaultSolve()) {
+        pic_solve_info info{};
+        pic_status s = pic_evaluate_electric_field(ctx_, &opts, &info);
+        if (s != PIC_OK && s != PIC_ERR_NOT_CONVERGED) check(s);
+        return info;
+    }
+    void evaluateMagneticField() { check(pic_evaluate_magnetic_field(ctx_)); }
+    void updateFields() { check(pic_update_fields(ctx_)); }
+    // correlation maps and the periodic particle exchange are folded into
+    // the kernels (cell index + offset, wrap on every move)
+    void updateParticleCorrelationMaps() {}
+    void exchangeParticles() {}
+    void sortParticles() { check(pic_sort_particles(ctx_)); }
+
+    // updateEnergy (PIC++/simulation.cpp:1506-1600)
+    std::vector<double> updateEnergy() {
+        std::vector<double> out(6);
+        check(pic_energy(ctx_, out.data()));
+        return out;
+    }
+
+    static pic_solve_opts defaultSolve() { return pic_solve_opts{PIC_GMRES_REFERENCE, 30, 50, 1e-8}; }
+
+private:
+    void check(pic_status s) {
+        if (s != PIC_OK) throw Error(s, pic_last_error(ctx_));
+    }
+    pic_ctx* ctx_ = nullptr;
+};
+
+}  // namespace picpp

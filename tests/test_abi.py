@@ -46,6 +46,18 @@ def test_python_wrapper_binds_every_export(lib_path):
     P.load_library(lib_path)
 
 
+def test_cpp_mirror_compiles_against_the_header(tmp_path):
+    """The C++ Simulation mirror (include/picpp_gb300_simulation.hpp) is
+    valid C++17 against the C header."""
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "picpp_gb300_simulation.hpp"\n'
+                   'void f(const pic_config& c) { picpp::GpuSimulation s(c); s.tristanEvaluateBhalfStep();'
+                   ' s.moveParticles(); s.tristanUpdateFlux(); s.tristanEvaluateE(); s.updateEnergy(); }\n')
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_null_arguments_fail_without_a_device(lib_path):
     lib = ctypes.CDLL(lib_path)
     lib.pic_create.restype = ctypes.c_int

@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "libpicpp_gb300.so")
 PIC_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_STATE", 4: "ERR_NOMEM", 5: "ERR_NUMERIC",
           6: "ERR_NOT_CONVERGED"}
+PIC_NOALLOC_MAX_SPECIES = 16
 BUNEMAN, IMPLICIT = 0, 1
 F32, F64 = 0, 1
 GMRES_REFERENCE, GMRES_RESTARTED, FGMRES_LEARNED = 0, 1, 2
@@ -28,7 +29,7 @@ EXPORTS = [
     "pic_move_particles", "pic_tristan_update_flux", "pic_tristan_evaluate_e", "pic_buneman_step",
     "pic_update_electromagnetic_parameters", "pic_evaluate_electric_field", "pic_evaluate_magnetic_field",
     "pic_update_fields", "pic_implicit_step", "pic_download_moments", "pic_maxwell_apply", "pic_maxwell_solve",
-    "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile",
+    "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile", "pic_energy_noalloc",
 ]
 PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover"]
 
@@ -103,6 +104,9 @@ def load_library(path: str | None = None):
     L.pic_download_permutation.argtypes = [vp, C.c_int, C.POINTER(C.c_long), _ip]
     L.pic_energy.argtypes = [vp, _dp]
     L.pic_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_long)]
+    ptrs = C.POINTER(C.c_void_p)
+    L.pic_energy_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, C.c_int,
+                                     C.POINTER(C.c_long), _dp, _dp, ptrs, ptrs, ptrs, vp, _dp]
     for name in EXPORTS:
         if name not in ("pic_last_error", "pic_stream"):
             getattr(L, name).restype = C.c_int

@@ -27,6 +27,7 @@ UNITS = {
     "grid.cu": [],
     "kernels_f32.cu": [],
     "kernels_f64.cu": ["--fmad=false"],
+    "energy_noalloc.cu": [],
 }
 
 

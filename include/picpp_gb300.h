@@ -114,6 +114,15 @@ pic_status pic_upload_particles(pic_ctx* ctx, int species, long n, const int* ce
                                 const double* ox, const double* oy, const double* oz,
                                 const double* px, const double* py, const double* pz,
                                 const int* ids);
+/* Fills a species on the device with ppc particles per cell: uniform in-cell
+ * offsets, Maxwell-Juttner momenta of temperature theta (kT/mc^2), boosted
+ * along x with Lorentz factor drift_gamma (> 1) -- every other particle
+ * towards -x when alternate_drift is set.  Seeded and independent of the
+ * launch shape.  A workload generator for runs too large to build on the
+ * host; no reference counterpart (the reference's initialisers,
+ * PIC++/initialization.cpp:8145-8574, are out of scope). */
+pic_status pic_fill_species(pic_ctx* ctx, int species, int ppc, unsigned long long seed, double theta,
+                            double drift_gamma, int alternate_drift);
 /* Copies a species back in the current device order.  Any output pointer may
  * be NULL.  *n receives the count. */
 pic_status pic_download_particles(pic_ctx* ctx, int species, long* n, int* cell,

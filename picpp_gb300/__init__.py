@@ -30,6 +30,7 @@ EXPORTS = [
     "pic_update_electromagnetic_parameters", "pic_evaluate_electric_field", "pic_evaluate_magnetic_field",
     "pic_update_fields", "pic_implicit_step", "pic_download_moments", "pic_maxwell_apply", "pic_maxwell_solve",
     "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile", "pic_energy_noalloc",
+    "pic_fill_species",
 ]
 PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover"]
 
@@ -104,6 +105,7 @@ def load_library(path: str | None = None):
     L.pic_download_permutation.argtypes = [vp, C.c_int, C.POINTER(C.c_long), _ip]
     L.pic_energy.argtypes = [vp, _dp]
     L.pic_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_long)]
+    L.pic_fill_species.argtypes = [vp, C.c_int, C.c_int, C.c_ulonglong, C.c_double, C.c_double, C.c_int]
     ptrs = C.POINTER(C.c_void_p)
     L.pic_energy_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, C.c_int,
                                      C.POINTER(C.c_long), _dp, _dp, ptrs, ptrs, ptrs, vp, _dp]
@@ -213,6 +215,11 @@ class GpuSimulation:
         if with_ids:
             out["id"] = ids
         return out
+
+    def fill_species(self, sid, ppc, seed, theta, drift_gamma=1.0, alternate_drift=False):
+        """Device-side seeded loading (pic_fill_species)."""
+        self._ck(self.L.pic_fill_species(self.ctx, sid, int(ppc), int(seed), float(theta), float(drift_gamma),
+                                         1 if alternate_drift else 0))
 
     def upload_state(self, state):
         """Species (adding them on first use) and fields of an initstate.State."""

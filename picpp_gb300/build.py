@@ -20,7 +20,9 @@ LIB = os.path.join(HERE, "libpicpp_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-                 "--expt-relaxed-constexpr", "-I", os.path.join(HERE, os.pardir, "include")]
+                 "--expt-relaxed-constexpr", "-I", os.path.join(HERE, os.pardir, "include"),
+                 # register budget of the fused explicit kernel: CTAs per SM
+                 f"-DPIC_TILE_MIN_BLOCKS={int(os.environ.get('PICPP_TILE_MIN_BLOCKS', '3'))}"]
 UNITS = {
     "api.cu": [],
     "solver.cu": [],
@@ -28,6 +30,7 @@ UNITS = {
     "kernels_f32.cu": [],
     "kernels_f64.cu": ["--fmad=false"],
     "energy_noalloc.cu": [],
+    "init.cu": [],
 }
 
 

@@ -353,6 +353,8 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     g.idx = 1.0 / c.dx; g.idy = 1.0 / c.dy; g.idz = 1.0 / c.dz;
     g.theta = c.theta; g.eta = c.eta; g.cfix = ctx->cfg.cfix;
     g.y3 = c.ny > 1; g.z3 = c.nz > 1;
+    g.divx = FastDiv((unsigned)c.nx);
+    g.divy = FastDiv((unsigned)c.ny);
     ctx->preal = c.particle_real;
     ctx->rsz = ctx->preal ? sizeof(double) : sizeof(float);
     TileGeom& t = ctx->tg;
@@ -362,7 +364,7 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     ctx->T3 = t.tx * t.ty * t.tz;
     ctx->nkeys = (int)N;
     TileShape& ts = ctx->ts;
-    ts.hx = 1; ts.hy = g.y3 ? 1 : 0; ts.hz = g.z3 ? 1 : 0;
+    ts.hx = 2; ts.hy = g.y3 ? 2 : 0; ts.hz = g.z3 ? 2 : 0;
     ts.gx = 2; ts.gy = g.y3 ? 2 : 0; ts.gz = g.z3 ? 2 : 0;
     ts.fx = t.tx + 2 * ts.hx; ts.fy = t.ty + 2 * ts.hy; ts.fz = t.tz + 2 * ts.hz;
     ts.jx = t.tx + 2 * ts.gx; ts.jy = t.ty + 2 * ts.gy; ts.jz = t.tz + 2 * ts.gz;
@@ -520,6 +522,35 @@ pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, 
     sp.sorted = false;
     ctx->moments_ready = false;
     return sync(ctx, "upload particles");
+}
+
+pic_status pic_fill_species(pic_ctx* ctx, int sid, int ppc, unsigned long long seed, double theta, double drift_gamma,
+                            int alternate_drift) {
+    if (!ctx) return PIC_ERR_ARG;
+    if (pic_status st = check_species(ctx, sid)) return st;
+    Species& sp = ctx->sp[sid];
+    if (ppc < 0 || !(theta >= 0) || !(drift_gamma >= 1.0)) return fail(ctx, PIC_ERR_ARG, "bad fill parameters");
+    const long long n = (long long)ppc * ctx->g.N;
+    if (n > sp.cap) return fail(ctx, PIC_ERR_NOMEM, "particle count exceeds species capacity");
+    const int ntab = 4096;
+    std::vector<double> us, cdf;
+    if (theta > 0) cdf = juttner_table(theta, ntab, us);
+    double* du = ctx->stage;
+    double* dc = ctx->stage + ntab;
+    if (theta > 0) {
+        CK(cudaMemcpyAsync(du, us.data(), sizeof(double) * ntab, cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(dc, cdf.data(), sizeof(double) * ntab, cudaMemcpyHostToDevice, ctx->s));
+    }
+    sp.n = n;
+    const unsigned long long sseed = seed * 0x100000001B3ull + (unsigned long long)sid * 0x9E3779B97F4A7C15ull;
+    if (ctx->preal) launch_fill<double>(ctx->s, view<double>(sp), ppc, sseed, du, dc, theta > 0 ? ntab : 0, sp.m,
+                                        drift_gamma, alternate_drift);
+    else launch_fill<float>(ctx->s, view<float>(sp), ppc, sseed, du, dc, theta > 0 ? ntab : 0, sp.m, drift_gamma,
+                            alternate_drift);
+    CKL(ctx, "fill species");
+    sp.sorted = false;
+    ctx->moments_ready = false;
+    return sync(ctx, "fill species");
 }
 
 pic_status pic_download_particles(pic_ctx* ctx, int sid, long* n_out, int* cell, double* ox, double* oy, double* oz,

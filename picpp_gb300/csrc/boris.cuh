@@ -71,6 +71,47 @@ __device__ __forceinline__ void velocity(const TP mom[3], TP m, TP v[3]) {
     v[0] = mom[0] / (m * gam); v[1] = mom[1] / (m * gam); v[2] = mom[2] / (m * gam);
 }
 
+// FP32 forms of the same kinematics with the hardware reciprocal square root:
+// m gamma = sqrt(m^2 + p^2), so 1/(m gamma) and beta/gamma = beta m/(m gamma)
+// need no division.  Used by the FP32 push (the FP64 path keeps the
+// reference's operation sequence).
+__device__ __forceinline__ void boris_fast(float q, float m, float dt, float beta, const float e[3], const float b[3],
+                                           float mom[3]) {
+    const float s = q * dt * 0.5f;
+    const float dp[3] = {e[0] * s, e[1] * s, e[2] * s};
+    mom[0] += dp[0]; mom[1] += dp[1]; mom[2] += dp[2];
+    const float p2 = mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2];
+    const float bs = beta * m * rsqrtf(m * m + p2);
+    const float b2 = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    const float f = 2.0f * rsqrtf(1.0f + bs * bs * b2);
+    const float pxb[3] = {mom[1] * b[2] - mom[2] * b[1], -mom[0] * b[2] + mom[2] * b[0], mom[0] * b[1] - mom[1] * b[0]};
+    const float tm[3] = {mom[0] + pxb[0] * bs, mom[1] + pxb[1] * bs, mom[2] + pxb[2] * bs};
+    const float txb[3] = {tm[1] * b[2] - tm[2] * b[1], -tm[0] * b[2] + tm[2] * b[0], tm[0] * b[1] - tm[1] * b[0]};
+    const float fb = f * bs;
+    mom[0] += txb[0] * fb + dp[0];
+    mom[1] += txb[1] * fb + dp[1];
+    mom[2] += txb[2] * fb + dp[2];
+}
+__device__ __forceinline__ void velocity_fast(const float mom[3], float m, float v[3]) {
+    const float r = rsqrtf(m * m + mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2]);
+    v[0] = mom[0] * r; v[1] = mom[1] * r; v[2] = mom[2] * r;
+}
+
+// Dispatch: fast forms for FP32 state, reference sequence for FP64.
+template <typename TP>
+__device__ __forceinline__ void boris_t(TP q, TP m, TP dt, TP beta, const TP e[3], const TP b[3], TP mom[3]) {
+    boris<TP>(q, m, dt, beta, e, b, mom);
+}
+template <>
+__device__ __forceinline__ void boris_t<float>(float q, float m, float dt, float beta, const float e[3],
+                                               const float b[3], float mom[3]) {
+    boris_fast(q, m, dt, beta, e, b, mom);
+}
+template <typename TP>
+__device__ __forceinline__ void velocity_t(const TP mom[3], TP m, TP v[3]) { velocity<TP>(mom, m, v); }
+template <>
+__device__ __forceinline__ void velocity_t<float>(const float mom[3], float m, float v[3]) { velocity_fast(mom, m, v); }
+
 template <typename TP, typename TF>
 __global__ void __launch_bounds__(256) k_boris_push(GridP g, PartView<TP> p, TP q, TP m,
                                                     const TF* __restrict__ E, const TF* __restrict__ B) {

@@ -2,20 +2,25 @@
 // tile of cells (the whole-step path of the explicit Buneman/Tristan solver).
 //
 // Particles are ordered by a tile-major cell key (sort.cuh), so tile t owns
-// the contiguous range [off[t*T3], off[(t+1)*T3]).  A CTA
-//   1. stages the six Yee components of the tile plus one cell of halo in
-//      shared memory (the gather of a particle in cell c reads nodes c, c+1
-//      and cell centres c-1..c+1),
-//   2. pushes every particle of the tile, gathering from shared memory, and
-//      accumulates its 24 zigzag current terms into a shared-memory current
-//      block covering the tile plus two cells of halo (a particle moves at
-//      most one cell per step; the zigzag touches new cell -1 .. +2),
-//   3. writes that block, unreduced, to a per-tile partial buffer.
-// k_assemble_j then sums the (up to 27) partials of every cell in a fixed
-// order into the FP64 current grid: no global floating-point atomics.
-// A particle that has drifted out of its tile since the last sort (or that
-// moves more than one cell) takes the global path: global gather and FP64
-// global atomics into a separate correction grid.
+// the contiguous range [off[t*T3], off[(t+1)*T3]) of every species.  A CTA
+//   1. stages the six Yee components of the tile plus two cells of halo in
+//      shared memory: the gather of a particle in cell c reads nodes c, c+1
+//      and cell centres c-1..c+1, so particles up to one cell outside their
+//      tile (drift since the last sort) still gather from shared memory;
+//   2. walks the tile's particles in chunks of 32 consecutive particles per
+//      warp (coalesced loads and stores) and pushes them.  The zigzag current
+//      of a particle is two segments, each with 12 terms at fixed positions
+//      relative to one cell: the segment from the old position to the relay
+//      point (in the old cell) and the one from the relay point to the new
+//      position (in the new cell).  Lanes of a warp holding the same cell
+//      (particles are sorted by cell) sum each segment's 12 values with a
+//      segmented shuffle reduction, and the first lane of each run adds them
+//      to a shared-memory current block (tile plus two cells of halo);
+//   3. writes the block, unreduced, to a per-tile partial buffer.
+// k_assemble_j then sums the partials of every cell in a fixed order into
+// the FP64 current grid: no global floating-point atomics on the fast path.
+// A particle more than one cell outside its tile takes the global path
+// (global gather, FP64 global atomics into a correction grid).
 #pragma once
 #include "boris.cuh"
 #include "types.cuh"
@@ -23,29 +28,133 @@
 namespace pic {
 
 constexpr int kTileThreads = 256;
+#ifndef PIC_TILE_MIN_BLOCKS
+#define PIC_TILE_MIN_BLOCKS 3   // CTAs per SM the register budget is sized for
+#endif
+
+template <typename TP>
+__device__ __forceinline__ TP lerp(TP a, TP b, TP w) { return a + w * (b - a); }
+
+// Trilinear value of one staggered component from the staged block: base is
+// the block index of the lower corner, sy/sz the strides, (wx, wy, wz) the
+// weights of the upper corner.
 template <typename TP, typename TF>
-__global__ void __launch_bounds__(kTileThreads) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
-                                                                    const TF* __restrict__ E, const TF* __restrict__ B,
-                                                                    TP* __restrict__ Jpart, double* __restrict__ Jfix) {
+__device__ __forceinline__ TP tri(const TF* __restrict__ F, int base, int sy, int sz, TP wx, TP wy, TP wz) {
+    TP v000 = TP(F[base]), v100 = TP(F[base + 1]);
+    TP v010 = TP(F[base + sy]), v110 = TP(F[base + sy + 1]);
+    TP v001 = TP(F[base + sz]), v101 = TP(F[base + sz + 1]);
+    TP v011 = TP(F[base + sy + sz]), v111 = TP(F[base + sy + sz + 1]);
+    TP a = lerp(lerp(v000, v100, wx), lerp(v010, v110, wx), wy);
+    TP b = lerp(lerp(v001, v101, wx), lerp(v011, v111, wx), wy);
+    return lerp(a, b, wz);
+}
+
+// Global gather for particles far from their tile (out of line: rare).
+template <typename TP, typename TF>
+__device__ __noinline__ void gather_global(const GridP& g, int cell, TP ox, TP oy, TP oz, const TF* __restrict__ E,
+                                           const TF* __restrict__ B, TP* e, TP* b) {
+    yee_gather<TP, TF>(g, cell, ox, oy, oz, E, B, e, b);
+}
+
+// The 24 zigzag terms of a particle straight into the FP64 correction grid
+// (particles whose segments fall outside the shared block; rare).
+template <typename TP>
+__device__ __noinline__ void deposit_global(const GridP& g, TP fcd, TP ox, TP oy, TP oz, TP vx, TP vy, TP vz, int ni,
+                                            int nj, int nk, double* __restrict__ Jfix) {
+    const TP v[3] = {vx, vy, vz};
+    zigzag_terms<TP>(g, fcd, ox, oy, oz, v, [&](int comp, int di, int dj, int dk, TP val) {
+        atomicAdd(&Jfix[comp * g.N + linw(g, ni + di, nj + dj, nk + dk)], double(val));
+    });
+}
+
+// One zigzag segment's 12 terms relative to its cell
+// (momentum_collecting.cpp:200-230): Jx at (c, j+dj, k+dk) -> slot 2dk+dj,
+// Jy at (i+di, c, k+dk) -> 4+2dk+di, Jz at (i+di, j+dj, c) -> 8+2dj+di.
+template <typename TP>
+__device__ __forceinline__ void segment_slots(TP Fx, TP Fy, TP Fz, TP Wx, TP Wy, TP Wz, TP a[12]) {
+    const TP ux = TP(1) - Wx, uy = TP(1) - Wy, uz = TP(1) - Wz;
+    a[0] = Fx * uy * uz; a[1] = Fx * Wy * uz; a[2] = Fx * uy * Wz; a[3] = Fx * Wy * Wz;
+    a[4] = Fy * ux * uz; a[5] = Fy * Wx * uz; a[6] = Fy * ux * Wz; a[7] = Fy * Wx * Wz;
+    a[8] = Fz * ux * uy; a[9] = Fz * Wx * uy; a[10] = Fz * ux * Wy; a[11] = Fz * Wx * Wy;
+}
+
+// Segmented sum of a[] over runs of lanes with equal key; returns true in the
+// first lane of each run, which then holds the run's totals.
+template <typename TP>
+__device__ __forceinline__ bool run_sum(int key, TP a[12]) {
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || key != prev;
+    const unsigned H = __ballot_sync(0xffffffffu, head);
+    if (H != 0xffffffffu) {
+        const unsigned after = H & ~((2u << lane) - 1u);
+        const int seg_end = after ? (__ffs(after) - 2) : 31;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const bool take = lane + d <= seg_end;
+#pragma unroll
+            for (int q = 0; q < 12; ++q) {
+                TP o = __shfl_down_sync(0xffffffffu, a[q], d);
+                if (take) a[q] += o;
+            }
+        }
+    }
+    return head;
+}
+
+// Adds one run's 12 totals at block cell c (strides X0, XY).
+template <typename TP>
+__device__ __forceinline__ void add_slots(TP* __restrict__ sJ, long long JC, int c, int X0, int XY, int ey, int ez,
+                                          const TP a[12]) {
+    TP* jx = sJ;
+    TP* jy = sJ + JC;
+    TP* jz = sJ + 2 * JC;
+    atomicAdd(&jx[c], a[0]);
+    if (ey) atomicAdd(&jx[c + X0], a[1]);
+    if (ez) atomicAdd(&jx[c + XY], a[2]);
+    if (ey && ez) atomicAdd(&jx[c + X0 + XY], a[3]);
+    atomicAdd(&jy[c], a[4]);
+    atomicAdd(&jy[c + 1], a[5]);
+    if (ez) atomicAdd(&jy[c + XY], a[6]);
+    if (ez) atomicAdd(&jy[c + 1 + XY], a[7]);
+    atomicAdd(&jz[c], a[8]);
+    atomicAdd(&jz[c + 1], a[9]);
+    if (ey) atomicAdd(&jz[c + X0], a[10]);
+    if (ey) atomicAdd(&jz[c + 1 + X0], a[11]);
+}
+
+// CT: compile-time tile extent of a cubic 3-D tile (8), or 0 for shapes read
+// from TileShape at run time.
+template <typename TP, typename TF, int CT>
+__global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
+                                                                       const TF* __restrict__ E, const TF* __restrict__ B,
+                                                                       TP* __restrict__ Jpart, double* __restrict__ Jfix) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int F = s.fx * s.fy * s.fz;
-    TF* sF = reinterpret_cast<TF*>(smem_raw);                 // 6 * F
-    TP* sJ = reinterpret_cast<TP*>(smem_raw + ((6 * F * sizeof(TF) + 15) & ~size_t(15)));   // 3 * jcells
-    const long long JC = s.jcells;
+    const int fx = CT ? CT + 4 : s.fx, fy = CT ? CT + 4 : s.fy, fz = CT ? CT + 4 : s.fz;
+    const int jx = fx, jy = fy, jz = fz;                 // both blocks: tile + 2 halo on active axes
+    const int tx = CT ? CT : t.tx, ty = CT ? CT : t.ty, tz = CT ? CT : t.tz;
+    const int hx = 2, hy = CT ? 2 : s.hy, hz = CT ? 2 : s.hz;
+    const int F = fx * fy * fz;
+    const long long JC = (long long)jx * jy * jz;
+    TF* sF = reinterpret_cast<TF*>(smem_raw);   // 6 * F
+    TP* sJ = reinterpret_cast<TP*>(smem_raw + ((6 * F * sizeof(TF) + 15) & ~size_t(15)));   // 3 * JC
     const int ntiles = t.ntx * t.nty * t.ntz;
-    const int T3 = t.tx * t.ty * t.tz;
+    const int T3 = tx * ty * tz;
     const long long N = g.N;
-    const TP dt = TP(g.dt);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const TP dt = TP(g.dt), idt = TP(1.0 / g.dt);
+    const TP dx = TP(g.dx), dy = TP(g.dy), dz = TP(g.dz);
     const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
-    const TP vol = TP(g.dx) * TP(g.dy) * TP(g.dz);
+    const TP vol = dx * dy * dz;
+    const int ey = CT ? 1 : (g.y3 ? 1 : 0), ez = CT ? 1 : (g.z3 ? 1 : 0);
+    const int fsy = ey ? fx : 0, fsz = ez ? fx * fy : 0;
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
-        const int lox = ti * t.tx, loy = tj * t.ty, loz = tk * t.tz;
-        // 1. stage fields
+        const int lox = ti * tx, loy = tj * ty, loz = tk * tz;
         for (int e = threadIdx.x; e < F; e += blockDim.x) {
-            int a = e % s.fx, b = (e / s.fx) % s.fy, c = e / (s.fx * s.fy);
-            long long gi = linw(g, lox - s.hx + a, loy - s.hy + b, loz - s.hz + c);
+            int a = e % fx, b = (e / fx) % fy, c = e / (fx * fy);
+            long long gi = linw(g, lox - hx + a, loy - hy + b, loz - hz + c);
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 sF[comp * F + e] = E[comp * N + gi];
@@ -55,91 +164,122 @@ __global__ void __launch_bounds__(kTileThreads) k_push_deposit_tile(GridP g, Til
         for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) sJ[e] = TP(0);
         __syncthreads();
 
-        // 2. particles of every species in this tile
         for (int sp = 0; sp < S.ns; ++sp) {
             const PartView<TP> P = S.p[sp];
             const TP q = S.q[sp], m = S.m[sp];
             const TP beta = q * dt / (TP(2) * m);
             const TP fcd = q * S.w[sp] / vol;
             const long long pb = S.off[sp][(long long)tile * T3], pe = S.off[sp][(long long)(tile + 1) * T3];
-            for (long long base = pb; base < pe; base += kTileThreads) {
-                // spread consecutive lanes over the chunk so that lanes of a
-                // warp hit different cells in the shared-memory atomics
-                const int tid = threadIdx.x;
-                const long long n = base + (tid & 31) * (kTileThreads / 32) + (tid >> 5);
-                if (n >= pe) continue;
-                int cell = P.cell[n];
-                TP ox = P.ox[n], oy = P.oy[n], oz = P.oz[n];
-                int i, j, k;
-                decode(g, cell, i, j, k);
-                const int li = i - lox, lj = j - loy, lk = k - loz;
-                const bool inside = (li >= 0 && li < t.tx && lj >= 0 && lj < t.ty && lk >= 0 && lk < t.tz);
-                TP e3[3], b3[3];
-                if (inside) {
-                    // staged gather (correlation.cpp:441-600 with local indices)
-                    int nX[2], cX[2], nY[2], cY[2], nZ[2], cZ[2];
-                    TP wnX[2], wcX[2], wnY[2], wcY[2], wnZ[2], wcZ[2];
-                    node_w(ox, li + s.hx, 1 << 30, nX, wnX); cell_w(ox, li + s.hx, 1 << 30, cX, wcX);
-                    if (g.y3) { node_w(oy, lj + s.hy, 1 << 30, nY, wnY); cell_w(oy, lj + s.hy, 1 << 30, cY, wcY); }
-                    else { node_w(oy, 0, 1, nY, wnY); cell_w(oy, 0, 1, cY, wcY); }
-                    if (g.z3) { node_w(oz, lk + s.hz, 1 << 30, nZ, wnZ); cell_w(oz, lk + s.hz, 1 << 30, cZ, wcZ); }
-                    else { node_w(oz, 0, 1, nZ, wnZ); cell_w(oz, 0, 1, cZ, wcZ); }
-                    e3[0] = e3[1] = e3[2] = TP(0); b3[0] = b3[1] = b3[2] = TP(0);
-                    auto L = [&](int a, int b, int c) { return (c * s.fy + b) * s.fx + a; };
-#pragma unroll
-                    for (int a = 0; a < 2; ++a)
-#pragma unroll
-                        for (int bb = 0; bb < 2; ++bb)
-#pragma unroll
-                            for (int cc = 0; cc < 2; ++cc) {
-                                e3[0] += TP(sF[0 * F + L(cX[a], nY[bb], nZ[cc])]) * wcX[a] * wnY[bb] * wnZ[cc];
-                                e3[1] += TP(sF[1 * F + L(nX[a], cY[bb], nZ[cc])]) * wnX[a] * wcY[bb] * wnZ[cc];
-                                e3[2] += TP(sF[2 * F + L(nX[a], nY[bb], cZ[cc])]) * wnX[a] * wnY[bb] * wcZ[cc];
-                                b3[0] += TP(sF[3 * F + L(nX[a], cY[bb], cZ[cc])]) * wnX[a] * wcY[bb] * wcZ[cc];
-                                b3[1] += TP(sF[4 * F + L(cX[a], nY[bb], cZ[cc])]) * wcX[a] * wnY[bb] * wcZ[cc];
-                                b3[2] += TP(sF[5 * F + L(cX[a], cY[bb], nZ[cc])]) * wcX[a] * wcY[bb] * wnZ[cc];
-                            }
-                } else {
-                    yee_gather<TP, TF>(g, cell, ox, oy, oz, E, B, e3, b3);
+            for (long long base = pb + 32LL * warp; base < pe; base += 32LL * nwarps) {
+                const long long n = base + lane;
+                TP aB[12];
+                TP s1[6] = {TP(0), TP(0), TP(0), TP(0), TP(0), TP(0)};   // F1 and W1 of the old-side segment
+                int keyA = -1 - lane, keyB = -1 - lane;   // lanes outside a reduction keep unique keys
+                if (n < pe) {
+                    const int cell = P.cell[n];
+                    TP ox = P.ox[n], oy = P.oy[n], oz = P.oz[n];
+                    TP mom[3] = {P.px[n], P.py[n], P.pz[n]};
+                    int i, j, k;
+                    decode(g, cell, i, j, k);
+                    auto local = [](int c, int lo, int te, int nn) {
+                        int l = c - lo;
+                        if (l > te) l -= nn;
+                        if (l < -1) l += nn;
+                        return l;
+                    };
+                    const int li = local(i, lox, tx, g.nx);
+                    const int lj = ey ? local(j, loy, ty, g.ny) : 0;
+                    const int lk = ez ? local(k, loz, tz, g.nz) : 0;
+                    const bool fast = li >= -1 && li <= tx && lj >= -ey && lj <= ty * ey && lk >= -ez && lk <= tz * ez;
+                    TP e3[3], b3[3];
+                    if (fast) {
+                        // upper-neighbour weights: node grids (c, c+1) with weight u;
+                        // cell-centred grids (c-1, c) with u + 1/2 below the centre,
+                        // (c, c+1) with u - 1/2 above it (correlation.cpp:471-496)
+                        const int c0 = (lk + hz) * fsz + (lj + hy) * fsy + (li + hx);
+                        const int cxs = ox < TP(0.5) ? -1 : 0;
+                        const int cys = (ey && oy < TP(0.5)) ? -fsy : 0;
+                        const int czs = (ez && oz < TP(0.5)) ? -fsz : 0;
+                        const TP wcx = ox < TP(0.5) ? ox + TP(0.5) : ox - TP(0.5);
+                        const TP wcy = ey ? (oy < TP(0.5) ? oy + TP(0.5) : oy - TP(0.5)) : TP(0);
+                        const TP wcz = ez ? (oz < TP(0.5) ? oz + TP(0.5) : oz - TP(0.5)) : TP(0);
+                        const TP wny = ey ? oy : TP(0), wnz = ez ? oz : TP(0);
+                        e3[0] = tri<TP, TF>(sF + 0 * F, c0 + cxs, fsy, fsz, wcx, wny, wnz);
+                        e3[1] = tri<TP, TF>(sF + 1 * F, c0 + cys, fsy, fsz, ox, wcy, wnz);
+                        e3[2] = tri<TP, TF>(sF + 2 * F, c0 + czs, fsy, fsz, ox, wny, wcz);
+                        b3[0] = tri<TP, TF>(sF + 3 * F, c0 + cys + czs, fsy, fsz, ox, wcy, wcz);
+                        b3[1] = tri<TP, TF>(sF + 4 * F, c0 + cxs + czs, fsy, fsz, wcx, wny, wcz);
+                        b3[2] = tri<TP, TF>(sF + 5 * F, c0 + cxs + cys, fsy, fsz, wcx, wcy, wnz);
+                    } else {
+                        gather_global<TP, TF>(g, cell, ox, oy, oz, E, B, e3, b3);
+                    }
+                    boris_t<TP>(q, m, dt, beta, e3, b3, mom);
+                    TP v[3];
+                    velocity_t<TP>(mom, m, v);
+                    int ni = i, nj = j, nk = k;
+                    advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
+                    advance_axis<TP>(oy, nj, (v[1] * dt) * idy, g.ny);
+                    advance_axis<TP>(oz, nk, (v[2] * dt) * idz, g.nz);
+                    P.px[n] = mom[0]; P.py[n] = mom[1]; P.pz[n] = mom[2];
+                    P.ox[n] = ox; P.oy[n] = oy; P.oz[n] = oz;
+                    P.cell[n] = (int)lin(g, ni, nj, nk);
+                    auto shift = [](int nw, int old, int nn) {
+                        int d = nw - old;
+                        if (d > 1) d -= nn;
+                        if (d < -1) d += nn;
+                        return d;
+                    };
+                    // block cell of the new position
+                    const int bx = li + shift(ni, i, g.nx) + hx;
+                    const int by = (ey ? lj + shift(nj, j, g.ny) : 0) + hy;
+                    const int bz = (ez ? lk + shift(nk, k, g.nz) : 0) + hz;
+                    // zigzag split (zig_axis, momentum_collecting.cpp:91-221) in the
+                    // new cell's frame: old position P, relay R, relay shift r
+                    const TP X = ox * dx, Y = oy * dy, Z = oz * dz;
+                    const TP PX = X - v[0] * dt, PY = Y - v[1] * dt, PZ = Z - v[2] * dt;
+                    const int rx = (int)dev_floor(divd<TP>(PX, dx, idx));
+                    const int ry = ey ? (int)dev_floor(divd<TP>(PY, dy, idy)) : 0;
+                    const int rz = ez ? (int)dev_floor(divd<TP>(PZ, dz, idz)) : 0;
+                    const TP RX = rx == 0 ? (X + PX) / TP(2) : TP(rx > 0 ? rx : 0) * dx;
+                    const TP RY = ry == 0 ? (Y + PY) / TP(2) : TP(ry > 0 ? ry : 0) * dy;
+                    const TP RZ = rz == 0 ? (Z + PZ) / TP(2) : TP(rz > 0 ? rz : 0) * dz;
+                    const int ax = bx + rx, ay = by + ry, az = bz + rz;   // block cell of the old-side segment
+                    const bool inblock = fast && rx >= -1 && rx <= 1 && ry >= -1 && ry <= 1 && rz >= -1 && rz <= 1 &&
+                                         ax >= 0 && bx >= 0 && ax + 1 < jx && bx + 1 < jx && ay >= 0 && by >= 0 &&
+                                         ay + ey < jy && by + ey < jy && az >= 0 && bz >= 0 && az + ez < jz &&
+                                         bz + ez < jz;
+                    if (inblock) {
+                        const TP F1x = divd<TP>(fcd * (RX - PX), dt, idt);
+                        const TP F1y = divd<TP>(fcd * (RY - PY), dt, idt);
+                        const TP F1z = divd<TP>(fcd * (RZ - PZ), dt, idt);
+                        const TP F2x = divd<TP>(fcd * (X - RX), dt, idt);
+                        const TP F2y = fcd * v[1] - F1y, F2z = fcd * v[2] - F1z;
+                        const TP hxx = TP(0.5) * idx, hyy = TP(0.5) * idy, hzz = TP(0.5) * idz;
+                        const TP W1x = divd<TP>(PX + RX, TP(2) * dx, hxx) - TP(rx);
+                        const TP W1y = ey ? divd<TP>(PY + RY, TP(2) * dy, hyy) - TP(ry) : TP(0);
+                        const TP W1z = ez ? divd<TP>(PZ + RZ, TP(2) * dz, hzz) - TP(rz) : TP(0);
+                        const TP W2x = divd<TP>(X + RX, TP(2) * dx, hxx);
+                        const TP W2y = ey ? divd<TP>(Y + RY, TP(2) * dy, hyy) : TP(0);
+                        const TP W2z = ez ? divd<TP>(Z + RZ, TP(2) * dz, hzz) : TP(0);
+                        segment_slots<TP>(F2x, F2y, F2z, W2x, W2y, W2z, aB);
+                        s1[0] = F1x; s1[1] = F1y; s1[2] = F1z; s1[3] = W1x; s1[4] = W1y; s1[5] = W1z;
+                        keyA = (az * jy + ay) * jx + ax;
+                        keyB = (bz * jy + by) * jx + bx;
+                    } else {
+                        deposit_global<TP>(g, fcd, ox, oy, oz, v[0], v[1], v[2], ni, nj, nk, Jfix);
+                    }
                 }
-                TP mom[3] = {P.px[n], P.py[n], P.pz[n]};
-                boris<TP>(q, m, dt, beta, e3, b3, mom);
-                P.px[n] = mom[0]; P.py[n] = mom[1]; P.pz[n] = mom[2];
-                TP v[3];
-                velocity<TP>(mom, m, v);
-                int ni = i, nj = j, nk = k;
-                advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
-                advance_axis<TP>(oy, nj, (v[1] * dt) * idy, g.ny);
-                advance_axis<TP>(oz, nk, (v[2] * dt) * idz, g.nz);
-                P.ox[n] = ox; P.oy[n] = oy; P.oz[n] = oz;
-                P.cell[n] = (int)lin(g, ni, nj, nk);
-                // unwrapped shift of the new cell relative to the old one
-                auto shift = [](int nw, int old, int nn) {
-                    int d = nw - old;
-                    if (d > nn / 2) d -= nn;
-                    if (d < -nn / 2) d += nn;
-                    return d;
-                };
-                const int sx = shift(ni, i, g.nx), sy = shift(nj, j, g.ny), sz = shift(nk, k, g.nz);
-                const bool local_dep = inside && sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
-                if (local_dep) {
-                    const int bx = li + s.gx + sx, by = (g.y3 ? lj + sy : 0) + s.gy, bz = (g.z3 ? lk + sz : 0) + s.gz;
-                    zigzag_terms<TP>(g, fcd, ox, oy, oz, v, [&](int comp, int di, int dj, int dk, TP val) {
-                        int a = bx + di, b = by + dj, c = bz + dk;
-                        if (a >= 0 && a < s.jx && b >= 0 && b < s.jy && c >= 0 && c < s.jz)
-                            atomicAdd(&sJ[comp * JC + ((long long)c * s.jy + b) * s.jx + a], val);
-                        else
-                            atomicAdd(&Jfix[comp * N + linw(g, ni + di, nj + dj, nk + dk)], double(val));
-                    });
-                } else {
-                    zigzag_terms<TP>(g, fcd, ox, oy, oz, v, [&](int comp, int di, int dj, int dk, TP val) {
-                        atomicAdd(&Jfix[comp * N + linw(g, ni + di, nj + dj, nk + dk)], double(val));
-                    });
+                if (keyB < 0) {
+#pragma unroll
+                    for (int q2 = 0; q2 < 12; ++q2) aB[q2] = TP(0);
                 }
+                if (run_sum<TP>(keyB, aB) && keyB >= 0) add_slots<TP>(sJ, JC, keyB, jx, jx * jy, ey, ez, aB);
+                TP aA[12];
+                segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);   // zeros off the reduction
+                if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);
             }
         }
         __syncthreads();
-        // 3. unreduced tile partials, coalesced
         TP* dst = Jpart + (long long)tile * 3 * JC;
         for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) dst[e] = sJ[e];
         __syncthreads();

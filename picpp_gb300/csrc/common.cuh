@@ -9,6 +9,18 @@
 
 namespace pic {
 
+// Division of non-negative ints below 2^31 by a fixed divisor with a multiply
+// and a shift (Granlund & Montgomery, PLDI 1994): q = (umulhi(m, n) + n) >> l.
+struct FastDiv {
+    unsigned m = 1, l = 0;
+    FastDiv() = default;
+    explicit FastDiv(unsigned d) {
+        l = 0;
+        while ((1u << l) < d) ++l;
+        m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+};
+
 struct GridP {
     int nx, ny, nz;
     long long N;          // nx*ny*nz
@@ -16,7 +28,12 @@ struct GridP {
     double idx, idy, idz; // 1/dx ...
     double theta, eta, cfix;
     int y3, z3;           // ny > 1, nz > 1
+    FastDiv divx, divy;   // by nx, by ny
 };
+
+__device__ __forceinline__ int fast_div(int n, const FastDiv& f) {
+    return (int)((__umulhi(f.m, (unsigned)n) + (unsigned)n) >> f.l);
+}
 
 __host__ __device__ __forceinline__ int wrap_p(int a, int n) { return a >= n ? a - n : a; }
 __host__ __device__ __forceinline__ int wrap_m(int a, int n) { return a < 0 ? a + n : a; }
@@ -33,10 +50,17 @@ __host__ __device__ __forceinline__ long long linw(const GridP& g, int i, int j,
     return ((long long)k * g.ny + j) * g.nx + i;
 }
 __host__ __device__ __forceinline__ void decode(const GridP& g, int cell, int& i, int& j, int& k) {
+#ifdef __CUDA_ARCH__
+    int q = fast_div(cell, g.divx);
+    i = cell - q * g.nx;
+    k = fast_div(q, g.divy);
+    j = q - k * g.ny;
+#else
     int q = cell / g.nx;
     i = cell - q * g.nx;
     k = q / g.ny;
     j = q - k * g.ny;
+#endif
 }
 
 // Division that is exact in FP64 (to match the oracle operation by
@@ -92,7 +116,9 @@ __device__ __forceinline__ void advance_axis(T& u, int& c, T du, int n) {
     int ci = c + (int)s;
     if (un >= T(1)) { un -= T(1); ci += 1; }
     u = un;
-    c = wrap_any(ci, n);
+    int w = ci < 0 ? ci + n : (ci >= n ? ci - n : ci);
+    if ((unsigned)w >= (unsigned)n) w = wrap_any(ci, n);   // moved farther than one box length
+    c = w;
 }
 
 constexpr int kRedThreads = 256;

@@ -4,6 +4,7 @@
 // (grid.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <vector>
 #include "common.cuh"
 #include "types.cuh"
 
@@ -56,6 +57,12 @@ struct PK {
     static void validate(cudaStream_t s, const GridP& g, PartView<T> p, int* flag);
     static void iota(cudaStream_t s, int* a, long long n);
 };
+
+// init.cu
+std::vector<double> juttner_table(double theta, int n, std::vector<double>& us);
+template <typename T>
+void launch_fill(cudaStream_t s, PartView<T> p, long long ppc, unsigned long long seed, const double* u, const double* c,
+                 int ntab, double mass, double drift_gamma, int alternate);
 
 // grid.cu
 void launch_keys_hist(cudaStream_t s, const GridP& g, const TileGeom& t, const int* cell, long long n, int* key,

@@ -158,10 +158,16 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
                                int grid, size_t smem) {
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_push_deposit_tile<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_push_deposit_tile<T, T><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix);
+    const bool cube8 = t.tx == 8 && t.ty == 8 && t.tz == 8 && g.y3 && g.z3 && sh.fx == 12 && sh.fy == 12 &&
+                       sh.fz == 12 && sh.jx == 12 && sh.jy == 12 && sh.jz == 12;
+    if (cube8)
+        k_push_deposit_tile<T, T, 8><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix);
+    else
+        k_push_deposit_tile<T, T, 0><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix);
 }
 
 template <typename T>

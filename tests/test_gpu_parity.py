@@ -363,6 +363,35 @@ def test_empty_species_and_no_particles(pg):
     assert np.all(J == 0)
 
 
+def test_device_fill_matches_the_distribution(pg):
+    """pic_fill_species: every cell gets ppc particles, offsets uniform,
+    momenta with the Maxwell-Juttner mean kinetic energy (drift off) and the
+    drift momentum gamma*beta*m (drift on), same seed -> same particles."""
+    box = I.Box(16, 16, 8, 0.1, 0.1, 0.1, 0.01)
+    sim = pg.GpuSimulation(box, pg.BUNEMAN, particle_real=1, sort_every=0)
+    sid = sim.add_species(-1.0, 1.0, 1.0, box.ncells * 8)
+    theta = 0.05
+    sim.fill_species(sid, 8, 123, theta)
+    a = sim.download_particles(sid)
+    assert np.array_equal(np.bincount(a["cell"], minlength=box.ncells), np.full(box.ncells, 8))
+    for k in ("ox", "oy", "oz"):
+        assert a[k].min() >= 0 and a[k].max() < 1 and abs(a[k].mean() - 0.5) < 0.01
+    gam = np.sqrt(1 + a["px"] ** 2 + a["py"] ** 2 + a["pz"] ** 2)
+    # mean kinetic energy of a Maxwell-Juttner gas from the oracle-side table
+    u = np.linspace(0, 6, 200001)
+    g = np.sqrt(1 + u * u)
+    f = u * u * np.exp(-(g - 1) / theta)
+    ek = np.sum((g - 1) * f) / np.sum(f)   # uniform grid: the trapezoid weights cancel
+    assert abs((gam - 1).mean() / ek - 1) < 0.02
+    sim.fill_species(sid, 8, 123, theta)
+    b = sim.download_particles(sid)
+    assert np.array_equal(a["px"], b["px"])
+    sim.fill_species(sid, 8, 7, 0.001, drift_gamma=3.0, alternate_drift=True)
+    c = sim.download_particles(sid)
+    ub = np.sqrt(3.0 ** 2 - 1)
+    assert abs(c["px"][0::2].mean() / ub - 1) < 0.02 and abs(c["px"][1::2].mean() / ub + 1) < 0.02
+
+
 def test_implicit_solver_rejects_nonfinite_rhs(pg):
     box = I.Box(5, 5, 5, 0.5, 0.5, 0.5, 0.5)
     N = box.ncells

@@ -67,7 +67,9 @@ def implicit_section(a):
     box = I.Box(nx, ny, nz, 0.5, 0.5, 0.5, 0.5, theta=0.5)
     n_e = 1.0 / (4 * math.pi)
     w = I.density_weight(box, n_e, ppc)
-    sim = P.GpuSimulation(box, P.IMPLICIT, particle_real=P.F32, sort_every=4)
+    # pressure tensor deposited at the particle's own cells (the reference's
+    # loop-index placement is the parity mode pressure_compat=1)
+    sim = P.GpuSimulation(box, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=1)
     N = box.ncells
     sim.add_species(-1.0, 1.0, w, N * ppc)
     sim.add_species(1.0, 25.0, w, N * ppc)

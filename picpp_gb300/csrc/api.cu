@@ -268,9 +268,25 @@ pic_status implicit_moments(pic_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->rho, 0, sizeof(double) * N, s));
     CK(cudaMemsetAsync(ctx->Pi, 0, sizeof(double) * ctx->pi_len, s));
     const int compat = ctx->cfg.pressure_compat;
-    for (auto& sp : ctx->sp)
-        PK<T>::implicit_deposit(s, g, view<T>(sp), sp.q, sp.m, sp.w, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu, ctx->rho,
-                                ctx->Pi, compat, ctx->ga);
+    // tiled shared-memory deposit when the particles are in tile order and
+    // the pressure tensor goes to the particle's cells; halo of one cell when
+    // the block fits in shared memory
+    ImpBlock bk = PK<T>::implicit_block(g, ctx->tg, 1);
+    if (PK<T>::implicit_tile_smem(bk) > 227 * 1024) bk = PK<T>::implicit_block(g, ctx->tg, 0);
+    if (!compat && all_sorted(ctx) && PK<T>::implicit_tile_smem(bk) <= 227 * 1024) {
+        ImpSpecies<T> S{};
+        S.ns = (int)ctx->sp.size();
+        for (int q = 0; q < S.ns; ++q) {
+            S.p[q] = view<T>(ctx->sp[q]);
+            S.q[q] = ctx->sp[q].q; S.m[q] = ctx->sp[q].m; S.w[q] = ctx->sp[q].w;
+            S.off[q] = ctx->sp[q].off;
+        }
+        PK<T>::implicit_deposit_tiled(s, g, ctx->tg, bk, S, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu, ctx->rho, ctx->Pi);
+    } else {
+        for (auto& sp : ctx->sp)
+            PK<T>::implicit_deposit(s, g, view<T>(sp), sp.q, sp.m, sp.w, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu,
+                                    ctx->rho, ctx->Pi, compat, ctx->ga);
+    }
     if (compat) {
         for (int ax = 0; ax < 3; ++ax) launch_pi_fold_reference(s, ctx->Pi, ctx->ga, ax);
         launch_jg_build(s, g, ctx->ga, ctx->Jh, ctx->Pi, ctx->Jg, ctx->nex, ctx->ney, ctx->nez);

@@ -46,6 +46,13 @@ struct PK {
     static void implicit_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w,
                                  const double* E, const double* B, double* J, double* mu, double* rho, double* Pi,
                                  int compat, const GhostAxes& ga);
+    // tiled deposit (implicit_tile.cuh), periodic pressure placement; needs
+    // tile-major sorted particles
+    static ImpBlock implicit_block(const GridP& g, const TileGeom& t, int h);
+    static size_t implicit_tile_smem(const ImpBlock& bk);
+    static void implicit_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const ImpBlock& bk,
+                                       const ImpSpecies<T>& S, const double* E, const double* B, double* J,
+                                       double* mu, double* rho, double* Pi);
     static void implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const double* E,
                               const double* B, const double* Et);
     static void gather_payload(cudaStream_t s, const int* perm, long long n, PartView<T> src, PartView<T> dst);

@@ -4,6 +4,7 @@
 #include "boris.cuh"
 #include "boris_tile.cuh"
 #include "implicit_particles.cuh"
+#include "implicit_tile.cuh"
 #include "kernels.hpp"
 #include "yee.cuh"
 
@@ -182,6 +183,42 @@ void PK<T>::implicit_deposit(cudaStream_t s, const GridP& g, PartView<T> p, doub
                              int compat, const GhostAxes& ga) {
     if (p.n == 0) return;
     k_implicit_deposit<T><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, w, E, B, J, mu, rho, Pi, compat, ga);
+}
+
+template <typename T>
+ImpBlock PK<T>::implicit_block(const GridP& g, const TileGeom& t, int h) {
+    ImpBlock b{};
+    b.h = h;
+    b.nbx = g.nx > 1 ? t.tx + 2 * h + 1 : 1;
+    b.nby = g.y3 ? t.ty + 2 * h + 1 : 1;
+    b.nbz = g.z3 ? t.tz + 2 * h + 1 : 1;
+    b.cbx = g.nx > 1 ? t.tx + 2 * h + 2 : 1;
+    b.cby = g.y3 ? t.ty + 2 * h + 2 : 1;
+    b.cbz = g.z3 ? t.tz + 2 * h + 2 : 1;
+    b.NB = b.nbx * b.nby * b.nbz;
+    b.CB = b.cbx * b.cby * b.cbz;
+    return b;
+}
+
+template <typename T>
+size_t PK<T>::implicit_tile_smem(const ImpBlock& bk) {
+    return (12 * (size_t)bk.NB + 7 * (size_t)bk.CB) * sizeof(T);
+}
+
+template <typename T>
+void PK<T>::implicit_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const ImpBlock& bk,
+                                   const ImpSpecies<T>& S, const double* E, const double* B, double* J, double* mu,
+                                   double* rho, double* Pi) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_implicit_deposit_tile<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    const size_t smem = implicit_tile_smem(bk);
+    const int per_sm = (int)((227 * 1024) / (smem + 1024));
+    const int ntiles = t.ntx * t.nty * t.ntz;
+    const int grid = ntiles < kNumSM * (per_sm > 0 ? per_sm : 1) ? ntiles : kNumSM * (per_sm > 0 ? per_sm : 1);
+    k_implicit_deposit_tile<T, T><<<grid, kImpThreads, smem, s>>>(g, t, bk, S, E, B, J, mu, rho, Pi);
 }
 
 template <typename T>

@@ -37,6 +37,24 @@ struct SpeciesSet {
     int ns;
 };
 
+// Species of the tiled implicit deposit (implicit_tile.cuh).
+template <typename T>
+struct ImpSpecies {
+    PartView<T> p[kMaxSpecies];
+    double q[kMaxSpecies], m[kMaxSpecies], w[kMaxSpecies];
+    const int* off[kMaxSpecies];   // sort offsets by key (nkeys + 1)
+    int ns;
+};
+
+// Shared accumulator blocks of the tiled implicit deposit: node block
+// extent t + 2h + 1 and cell block extent t + 2h + 2 on active axes, 1 on a
+// single-cell axis.
+struct ImpBlock {
+    int h;
+    int nbx, nby, nbz, NB;
+    int cbx, cby, cbz, CB;
+};
+
 // Coefficients of the matrix-free Maxwell operator (implicit_grid.cuh).
 struct OpCoef {
     double K;

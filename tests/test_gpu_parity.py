@@ -226,6 +226,51 @@ def test_implicit_moments_and_rhs_match_oracle(pg, compat):
     assert rel_err(rhs, rhso) < 1e-12
 
 
+@pytest.mark.parametrize("real,tile,ppc", [(1, (4, 3, 5), 6), (0, (8, 6, 5), 6), (1, (2, 2, 1), 2),
+                                           (1, (1, 1, 1), 5), (0, (8, 3, 5), 2)])
+def test_implicit_tiled_moments_match_oracle(pg, real, tile, ppc):
+    """Tile-order deposit (shared-memory blocks, transpose-reduced runs and
+    direct adds) against the oracle; pressure tensor at the particle's cells."""
+    st = implicit_state(ppc=ppc)
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1, tile=tile)
+    sim.upload_state(st)
+    sim.updateElectroMagneticParameters()
+    J, mu, rho, rhs = sim.download_moments()
+    g = O.make_grid(st.box, pressure_compat=0)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    Jo, muo, rhoo, Pio, raw = O.implicit_moments(g, copy_species(st.species), E, B)
+    rhso = O.maxwell_rhs(g, E, B, Jo, rhoo)
+    tol = 1e-12 if real else TOL32
+    assert rel_err(mu, muo) < tol
+    assert rel_err(J, Jo) < tol
+    assert rel_err(rho, rhoo) < tol
+    assert rel_err(rhs, rhso) < tol
+
+
+@pytest.mark.parametrize("real,tile", [(1, (4, 3, 5)), (1, (1, 1, 1)), (0, (8, 6, 5))])
+def test_implicit_steps_with_drift_since_sort_match_oracle(pg, real, tile):
+    """Sorting every third step: particles that left their tile since the
+    sort deposit through the halo block or the global path."""
+    st = implicit_state(ppc=3, gamma=6.0)
+    steps = 4
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=3, tile=tile)
+    sim.upload_state(st)
+    for _ in range(steps):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    E, B, _ = sim.download_fields()
+    g = O.make_grid(st.box, pressure_compat=0)
+    sp = copy_species(st.species)
+    Eo, Bo = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(steps):
+        O.implicit_step(g, sp, Eo, Bo)
+    tol = 1e-9 if real else 1e-4
+    assert rel_err(E.reshape(-1), Eo) < tol
+    assert rel_err(B.reshape(-1), Bo) < tol
+    for s in range(2):
+        got = by_id(sim.download_particles(s))
+        compare_particles(st.box, got, sp[s], tol, 1e-8 if real else 1e-4)
+
+
 def test_maxwell_operator_matches_oracle(pg):
     box = I.Box(7, 6, 5, 0.5, 0.5, 0.5, 0.5)
     rng = np.random.default_rng(2)

@@ -46,6 +46,7 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--implicit-grid", type=int, nargs=3, default=[256, 256, 64])
     p.add_argument("--implicit-ppc", type=int, default=64)
+    p.add_argument("--nn-steps", type=int, default=1500, help="training steps of the learned preconditioner")
     p.add_argument("--no-implicit", action="store_true")
     return p.parse_args()
 
@@ -99,9 +100,64 @@ def implicit_section(a):
     out["plain"] = {"solver": "GMRES(30), CGS2, FP64", "iterations": info["iterations"],
                     "restarts": info["restarts"], "rel_residual": info["rel_residual"],
                     "seconds": info["seconds"]}
-    out["learned"] = None
+    if a.nn_steps > 0:
+        out["learned_vs_plain"] = learned_solve(a, sim, box, w, opts)
     sim.close()
     return out
+
+
+NET_LAYERS = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1),
+              (32, 32, 1), (48, 16, 0), (16, 16, 0), (16, 16, 0)]   # (cin, cout, level) of the network
+
+
+def learned_solve(a, sim, box, w, opts):
+    """Trains the learned preconditioner on a 64x64x16 box of the same
+    plasma (the network is convolutional: its parameters carry over), then
+    solves the full box's next implicit system to an FP64 relative residual
+    of 1e-8 with plain GMRES(30) and with FGMRES(30) + the network."""
+    import math
+    import numpy as np
+    import picpp_gb300 as P
+    from picpp_gb300 import initstate as I
+    tb = I.Box(64, 64, 16, box.dx, box.dy, box.dz, box.dt, theta=box.theta)
+    ppc = a.implicit_ppc
+    tsim = P.GpuSimulation(tb, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=1)
+    N = tb.ncells
+    tsim.add_species(-1.0, 1.0, w, N * ppc)
+    tsim.add_species(1.0, 25.0, w, N * ppc)
+    tsim.fill_species(0, ppc, 13, 0.01, 10.0, True)
+    tsim.fill_species(1, ppc, 14, 0.01 / 25.0, 10.0, True)
+    E = np.zeros((3, tb.nz, tb.ny, tb.nx))
+    B = np.zeros((3, tb.nz, tb.ny, tb.nx))
+    B[2] = math.sqrt(4 * math.pi * 0.01 * (1.0 / (4 * math.pi)) * 26.0 * 10.0)
+    tsim.upload_fields(E, B)
+    tsim.implicit_step(opts)
+    tsim.updateElectroMagneticParameters()
+    tsim.nn_init(1)
+    tr = tsim.nn_train(steps=a.nn_steps, batch=2, lr=1e-3, seed=3, smooth_max=2)
+    params = tsim.nn_get_params()
+    tsim.close()
+    sim.nn_set_params(params)
+    sim.updateElectroMagneticParameters()
+    _, mu, _, rhs = sim.download_moments()
+    plain_opts = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=600, tol=1e-8)
+    learned_opts = P.solve_opts(P.FGMRES_LEARNED, restart=30, max_iter=600, tol=1e-8)
+    sim.maxwell_solve(mu, rhs, plain_opts)   # warm-up of both paths
+    sim.maxwell_solve(mu, rhs, learned_opts)
+    _, ip = sim.maxwell_solve(mu, rhs, plain_opts)
+    _, il = sim.maxwell_solve(mu, rhs, learned_opts)
+    n = box.ncells
+    flop = sum(2 * 27 * ci * co * n / 8 ** lv for ci, co, lv in NET_LAYERS)
+    per_it = ip["seconds"] / max(ip["iterations"], 1)
+    apply_s = max(il["seconds"] - il["iterations"] * per_it, 0.0) / max(il["iterations"], 1)
+    return {"system": "next implicit step of the full box", "tol": 1e-8,
+            "plain": {k: ip[k] for k in ("iterations", "restarts", "rel_residual", "seconds")},
+            "learned": {k: il[k] for k in ("iterations", "restarts", "used_fallback", "rel_residual", "seconds")},
+            "speedup": ip["seconds"] / il["seconds"] if il["seconds"] > 0 else None,
+            "network": {"flop_per_apply": flop, "apply_ms_est": apply_s * 1e3,
+                        "tflops_est": flop / apply_s / 1e12 if apply_s > 0 else None,
+                        "train": {"box": [64, 64, 16], "steps": tr["steps"], "seconds": tr["seconds"],
+                                  "first_loss": tr["first_loss"], "last_loss": tr["last_loss"]}}}
 
 
 def _dist():

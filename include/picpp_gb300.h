@@ -172,9 +172,53 @@ pic_status pic_implicit_step(pic_ctx* ctx, const pic_solve_opts* opts, pic_solve
 pic_status pic_download_moments(pic_ctx* ctx, double* J, double* mu, double* rho_ext, double* rhs);
 /* Applies the implicit Maxwell operator built from mu to x (3N each, host). */
 pic_status pic_maxwell_apply(pic_ctx* ctx, const double* mu, const double* x, double* y);
+/* Applies the transpose A(mu)^T to y (no reference counterpart; the
+ * learned preconditioner's training back-propagates through it). */
+pic_status pic_maxwell_apply_transpose(pic_ctx* ctx, const double* mu, const double* y, double* out);
 /* Solves A(mu) x = rhs (host arrays) with the given options. */
 pic_status pic_maxwell_solve(pic_ctx* ctx, const double* mu, const double* rhs, double* x,
                              const pic_solve_opts* opts, pic_solve_info* info);
+
+/* ---- learned preconditioner --------------------------------------------- */
+/* No counterpart in the reference (PIC++ solves with plain GMRES,
+ * specialmath.cpp:367-671).  A 3-level encoder-decoder of 3x3x3
+ * convolutions (16/32/64 channels, ReLU, 2x2x2 average pooling, nearest
+ * upsampling with skip concatenation) maps (r / s, mu_xx, mu_yy, mu_zz) to
+ * x / s, s = rms(r), approximating A(mu)^-1 r; used by PIC_FGMRES_LEARNED.
+ * Activations BF16, FP32 accumulation.  Input tensors have 16 channels
+ * (0-2 residual, 3-5 mu diagonal, 6-15 zero), outputs 16 (0-2 used).
+ * Parameters: one FP32 vector, per layer W[27][cout][cin] then b[cout]. */
+typedef struct {
+    int steps;                    /* Adam steps                                   */
+    int batch;                    /* random fields per step                       */
+    double lr;                    /* Adam step size                               */
+    unsigned long long seed;      /* random fields                                */
+    int smooth_max;               /* fields get 0..smooth_max binomial passes     */
+} pic_train_opts;
+typedef struct {
+    double first_loss, last_loss; /* relative residual loss of the first / last step */
+    double seconds;               /* device time                                  */
+    int steps;
+} pic_train_info;
+/* Number of FP32 parameters. */
+long pic_nn_param_count(void);
+/* He-normal initialisation (seeded), zero biases, zero output layer. */
+pic_status pic_nn_init(pic_ctx* ctx, unsigned long long seed);
+pic_status pic_nn_set_params(pic_ctx* ctx, const float* params);
+pic_status pic_nn_get_params(pic_ctx* ctx, float* params);
+/* Trains on the operator of the last pic_update_electromagnetic_parameters
+ * (or the mu of the last pic_maxwell_apply / pic_maxwell_solve): random
+ * fields r of unit rms on the whole box, loss |A(mu) z - r|^2 / |r|^2 for
+ * z = network(r, mu diagonal), back-propagated through A^T.  Box axes must
+ * be multiples of 4. */
+pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info* info);
+/* Forward pass on host input x0[n][d][h][w][16] (FP32, rounded to BF16),
+ * out[n][d][h][w][16] FP32.  d, h, w multiples of 4. */
+pic_status pic_nn_forward(pic_ctx* ctx, int n, int d, int h, int w, const float* x0, float* out);
+/* Mean squared error against target[n][d][h][w][3] and its gradient with
+ * respect to every parameter (grad: pic_nn_param_count() floats). */
+pic_status pic_nn_loss_grad(pic_ctx* ctx, int n, int d, int h, int w, const float* x0, const float* target,
+                            double* loss, float* grad);
 
 /* ---- particle order ----------------------------------------------------- */
 /* Stable counting sort of every species by tile-major cell key (no reference
@@ -187,6 +231,16 @@ pic_status pic_download_permutation(pic_ctx* ctx, int species, long* n, int* per
 /* updateEnergy (PIC++/simulation.cpp:1506-1600) in normalised units:
  * out = {particle kinetic, electric, magnetic energy, px, py, pz momentum}. */
 pic_status pic_energy(pic_ctx* ctx, double out[6]);
+
+/* updateDensityParameters (PIC++/momentum_collecting.cpp:760-1020) on the
+ * current particles: per species the concentration sum w S / V, the energy
+ * density sum w gamma m S / V (fullEnergy, PIC++/particle.cpp:398-401) and
+ * the bulk velocity (sum w p S / V) / energy density (0 where that is 0), with
+ * the cell-centred weights S; and the charge density sum_s q_s conc_s. */
+pic_status pic_update_density_parameters(pic_ctx* ctx);
+/* Copies one species' conc (N), energy (N) and vel (3N) and the charge
+ * density rho (N) of the last update; any pointer may be NULL. */
+pic_status pic_download_density(pic_ctx* ctx, int species, double* conc, double* energy, double* vel, double* rho);
 
 /* Phase timing, the GPU counterpart of the reference's per-phase clock()
  * prints (PIC++/mover.cpp:23-54, simulation.cpp:157-159).  enable = 1 starts

@@ -81,11 +81,32 @@ public:
     void exchangeParticles() {}
     void sortParticles() { check(pic_sort_particles(ctx_)); }
 
+    // updateDensityParameters (PIC++/momentum_collecting.cpp:760-1020)
+    void updateDensityParameters() { check(pic_update_density_parameters(ctx_)); }
+
     // updateEnergy (PIC++/simulation.cpp:1506-1600)
     std::vector<double> updateEnergy() {
         std::vector<double> out(6);
         check(pic_energy(ctx_, out.data()));
         return out;
+    }
+
+    // learned right preconditioner of PIC_FGMRES_LEARNED (no reference
+    // counterpart): initialise or load, train on the current operator
+    void initPreconditioner(unsigned long long seed) { check(pic_nn_init(ctx_, seed)); }
+    void loadPreconditioner(const std::vector<float>& p) {
+        if ((long)p.size() != pic_nn_param_count()) throw Error(PIC_ERR_ARG, "wrong parameter count");
+        check(pic_nn_set_params(ctx_, p.data()));
+    }
+    std::vector<float> savePreconditioner() {
+        std::vector<float> p((size_t)pic_nn_param_count());
+        check(pic_nn_get_params(ctx_, p.data()));
+        return p;
+    }
+    pic_train_info trainPreconditioner(const pic_train_opts& opts) {
+        pic_train_info info{};
+        check(pic_nn_train(ctx_, &opts, &info));
+        return info;
     }
 
     static pic_solve_opts defaultSolve() { return pic_solve_opts{PIC_GMRES_REFERENCE, 30, 50, 1e-8}; }

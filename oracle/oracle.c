@@ -1056,3 +1056,55 @@ void orc_energy(const orc_grid* g, const orc_particles* sp, int nspecies,
     }
     out[0] = pe; out[1] = ee; out[2] = be; out[3] = mx; out[4] = my; out[5] = mz;
 }
+
+/* updateDensityParameters (PIC++/momentum_collecting.cpp:760-1020) on a
+ * periodic box: per species s the concentration n_s = sum w S / V, the
+ * energy density e_s = sum w gamma m S / V (fullEnergy, particle.cpp:398-401)
+ * and the bulk velocity u_s = (sum w p S / V) / e_s (0 where e_s = 0), with
+ * the cell-centred weights S of the correlation map; the charge density
+ * rho = sum_s q_s n_s.  Outputs: conc[s][N], energy[s][N], vel[s][3][N],
+ * rho[N]. */
+void orc_density_moments(const orc_grid* g, const orc_particles* sp, int nspecies, double* conc, double* energy,
+                         double* vel, double* rho) {
+    const long N = NC(g);
+    const double vol = g->dx * g->dy * g->dz;
+    for (long c = 0; c < N; ++c) rho[c] = 0.0;
+    for (int s = 0; s < nspecies; ++s) {
+        const orc_particles* p = &sp[s];
+        double* cs = conc + s * N;
+        double* es = energy + s * N;
+        double* vs = vel + 3 * s * N;
+        for (long c = 0; c < N; ++c) { cs[c] = 0; es[c] = 0; vs[c] = 0; vs[N + c] = 0; vs[2 * N + c] = 0; }
+        for (long n = 0; n < p->n; ++n) {
+            int i, j, k;
+            decode(g, p->cell[n], &i, &j, &k);
+            int X[2], Y[2], Z[2];
+            double wx[2], wy[2], wz[2];
+            cell_w(p->ox[n], i, g->nx, X, wx);
+            cell_w(p->oy[n], j, g->ny, Y, wy);
+            cell_w(p->oz[n], k, g->nz, Z, wz);
+            const double mom[3] = {p->px[n], p->py[n], p->pz[n]};
+            const double en = gamma_of(mom, p->m) * p->m;
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b)
+                    for (int cc = 0; cc < 2; ++cc) {
+                        if ((g->ny == 1 && b) || (g->nz == 1 && cc)) continue;
+                        const long id = IX(g, X[a], Y[b], Z[cc]);
+                        const double corr = wx[a] * wy[b] * wz[cc] / vol;
+                        cs[id] += p->w * corr;
+                        es[id] += p->w * en * corr;
+                        vs[id] += mom[0] * p->w * corr;
+                        vs[N + id] += mom[1] * p->w * corr;
+                        vs[2 * N + id] += mom[2] * p->w * corr;
+                    }
+        }
+        for (long c = 0; c < N; ++c) {
+            rho[c] += p->q * cs[c];
+            if (es[c] > 0) {
+                vs[c] /= es[c]; vs[N + c] /= es[c]; vs[2 * N + c] /= es[c];
+            } else {
+                vs[c] = vs[N + c] = vs[2 * N + c] = 0.0;
+            }
+        }
+    }
+}

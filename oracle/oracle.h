@@ -91,6 +91,11 @@ long orc_implicit_work_size(const orc_grid* g);
 /* ---- diagnostics ---- */
 void orc_energy(const orc_grid* g, const orc_particles* sp, int nspecies,
                 const double* E, const double* B, double out[6]);
+/* updateDensityParameters (momentum_collecting.cpp:760-1020), periodic box:
+ * conc[s][N], energy[s][N] (gamma m), vel[s][3][N] (momentum / energy
+ * density), rho[N]. */
+void orc_density_moments(const orc_grid* g, const orc_particles* sp, int nspecies, double* conc, double* energy,
+                         double* vel, double* rho);
 
 #ifdef __cplusplus
 }

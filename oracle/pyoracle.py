@@ -80,6 +80,7 @@ def lib():
         L.orc_implicit_work_size.argtypes = [g]
         L.orc_implicit_work_size.restype = C.c_long
         L.orc_energy.argtypes = [g, p, C.c_int, _dp, _dp, _dp]
+        L.orc_density_moments.argtypes = [g, p, C.c_int, _dp, _dp, _dp, _dp]
     return _lib
 
 
@@ -195,6 +196,16 @@ def energy(grid, species, E, B):
     return out
 
 
+def density_moments(grid, species):
+    """updateDensityParameters: (conc[s][N], energy[s][N], vel[s][3][N], rho[N])."""
+    N = grid.nx * grid.ny * grid.nz
+    ns = len(species)
+    conc, en, vel, rho = np.zeros(ns * N), np.zeros(ns * N), np.zeros(3 * ns * N), np.zeros(N)
+    arr = _plist(species)
+    lib().orc_density_moments(C.byref(grid), arr, ns, _d(conc), _d(en), _d(vel), _d(rho))
+    return conc.reshape(ns, N), en.reshape(ns, N), vel.reshape(ns, 3, N), rho
+
+
 # ---------------------------------------------------------------- reference
 def reference_available() -> bool:
     return os.path.isdir(REF_SRC)
@@ -205,7 +216,7 @@ def build_reference() -> str:
     return REF_BIN
 
 
-def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = False):
+def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = False, density: bool = False):
     """Runs the PIC++ reference (compiled from its own sources) on the state
     and returns (species positions/momenta by input order, E, B, extras)."""
     from picpp_gb300.initstate import positions
@@ -214,7 +225,7 @@ def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = Fals
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            f.write(struct.pack("<8i", solver, box.nx, box.ny, box.nz, len(species), steps, int(dump), 0))
+            f.write(struct.pack("<8i", solver, box.nx, box.ny, box.nz, len(species), steps, int(dump), int(density)))
             f.write(struct.pack("<4d", box.dx, box.dt, box.theta, box.eta))
             for sp in species:
                 x, y, z = positions(box, sp)
@@ -246,5 +257,11 @@ def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = Fals
     elif dump:
         for name, c in (("J", 3), ("mu", 9), ("rho", 1), ("Pi", 9), ("rhs", 3), ("Etheta", 3)):
             extra[name] = take(c * N)
+    if density:
+        ns = len(species)
+        conc, en, vel = np.zeros((ns, N)), np.zeros((ns, N)), np.zeros((ns, 3, N))
+        for s in range(ns):
+            conc[s], en[s], vel[s] = take(N), take(N), take(3 * N).reshape(3, N)
+        extra["density"] = (conc, en, vel, take(N))
     assert off == raw.nbytes
     return out_sp, Eo, Bo, extra

@@ -52,6 +52,7 @@ int main(int argc, char** argv) {
     int32_t hdr[8];
     for (int a = 0; a < 8; ++a) hdr[a] = rd<int32_t>(f);
     const int solver = hdr[0], nx = hdr[1], ny = hdr[2], nz = hdr[3], ns = hdr[4], steps = hdr[5], dump = hdr[6];
+    const int density = hdr[7];   // 1: append updateDensityParameters' grids after the run
     double dx = rd<double>(f), dt = rd<double>(f), theta = rd<double>(f), eta = rd<double>(f);
     Box bx{nx, ny, nz};
     const long N = (long)nx * ny * nz;
@@ -268,6 +269,29 @@ int main(int argc, char** argv) {
     if (solver == 1 && dump) {
         wrv(o, dJ.data(), 3 * N); wrv(o, dMu.data(), 9 * N); wrv(o, dRho.data(), N);
         wrv(o, dPi.data(), 9 * N); wrv(o, dRhs.data(), 3 * N); wrv(o, dEt.data(), 3 * N);
+    }
+    if (density) {
+        // momentum_collecting.cpp:760-1020 on the final state; every particle
+        // is of type 0 here, whose folds run only for a populated type
+        // (momentum_exchange.cpp:1056)
+        S->types[0].particlesPerBin = 1;
+        S->updateParticleCorrelationMaps();
+        S->updateDensityParameters();
+        std::vector<double> C(N), En(N), V(3 * N), R(N);
+        for (int t = 0; t < ns; ++t) {
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        int ri = i + 2, rj = ny > 1 ? j + 2 : 0, rk = nz > 1 ? k + 2 : 0;
+                        long c = pidx(bx, i, j, k);
+                        C[c] = S->particleConcentrations[t][ri][rj][rk];
+                        En[c] = S->particleEnergies[t][ri][rj][rk];
+                        for (int d = 0; d < 3; ++d) V[d * N + c] = S->particleBulkVelocities[t][ri][rj][rk][d];
+                        R[c] = S->chargeDensity[ri][rj][rk];
+                    }
+            wrv(o, C.data(), N); wrv(o, En.data(), N); wrv(o, V.data(), 3 * N);
+        }
+        wrv(o, R.data(), N);
     }
     fclose(o);
     return 0;

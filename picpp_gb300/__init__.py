@@ -28,9 +28,11 @@ EXPORTS = [
     "pic_download_particles", "pic_upload_fields", "pic_download_fields", "pic_tristan_evaluate_b_half_step",
     "pic_move_particles", "pic_tristan_update_flux", "pic_tristan_evaluate_e", "pic_buneman_step",
     "pic_update_electromagnetic_parameters", "pic_evaluate_electric_field", "pic_evaluate_magnetic_field",
-    "pic_update_fields", "pic_implicit_step", "pic_download_moments", "pic_maxwell_apply", "pic_maxwell_solve",
+    "pic_update_fields", "pic_implicit_step", "pic_download_moments", "pic_maxwell_apply",
+    "pic_maxwell_apply_transpose", "pic_maxwell_solve",
     "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile", "pic_energy_noalloc",
-    "pic_fill_species",
+    "pic_fill_species", "pic_nn_param_count", "pic_nn_init", "pic_nn_set_params", "pic_nn_get_params",
+    "pic_nn_train", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
 ]
 PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover"]
 
@@ -62,8 +64,21 @@ class SolveInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class TrainOpts(C.Structure):
+    _fields_ = [("steps", C.c_int), ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_ulonglong),
+                ("smooth_max", C.c_int)]
+
+
+class TrainInfo(C.Structure):
+    _fields_ = [("first_loss", C.c_double), ("last_loss", C.c_double), ("seconds", C.c_double), ("steps", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
 
 
@@ -101,6 +116,7 @@ def load_library(path: str | None = None):
     L.pic_implicit_step.argtypes = [vp, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]
     L.pic_download_moments.argtypes = [vp, _dp, _dp, _dp, _dp]
     L.pic_maxwell_apply.argtypes = [vp, _dp, _dp, _dp]
+    L.pic_maxwell_apply_transpose.argtypes = [vp, _dp, _dp, _dp]
     L.pic_maxwell_solve.argtypes = [vp, _dp, _dp, _dp, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]
     L.pic_download_permutation.argtypes = [vp, C.c_int, C.POINTER(C.c_long), _ip]
     L.pic_energy.argtypes = [vp, _dp]
@@ -109,8 +125,18 @@ def load_library(path: str | None = None):
     ptrs = C.POINTER(C.c_void_p)
     L.pic_energy_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, C.c_int,
                                      C.POINTER(C.c_long), _dp, _dp, ptrs, ptrs, ptrs, vp, _dp]
+    L.pic_update_density_parameters.argtypes = [vp]
+    L.pic_download_density.argtypes = [vp, C.c_int, _dp, _dp, _dp, _dp]
+    L.pic_nn_param_count.argtypes = []
+    L.pic_nn_param_count.restype = C.c_long
+    L.pic_nn_init.argtypes = [vp, C.c_ulonglong]
+    L.pic_nn_set_params.argtypes = [vp, _fp]
+    L.pic_nn_get_params.argtypes = [vp, _fp]
+    L.pic_nn_train.argtypes = [vp, C.POINTER(TrainOpts), C.POINTER(TrainInfo)]
+    L.pic_nn_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp]
+    L.pic_nn_loss_grad.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _dp, _fp]
     for name in EXPORTS:
-        if name not in ("pic_last_error", "pic_stream"):
+        if name not in ("pic_last_error", "pic_stream", "pic_nn_param_count"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -121,6 +147,13 @@ def _d(a):
         return None
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
+
+
+def _f(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_fp)
 
 
 def _i(a):
@@ -297,6 +330,13 @@ class GpuSimulation:
         self._ck(self.L.pic_maxwell_apply(self.ctx, _d(mu), _d(x), _d(y)))
         return y
 
+    def maxwell_apply_transpose(self, mu, y):
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        out = np.empty_like(y)
+        self._ck(self.L.pic_maxwell_apply_transpose(self.ctx, _d(mu), _d(y), _d(out)))
+        return out
+
     def maxwell_solve(self, mu, rhs, opts=None):
         mu = np.ascontiguousarray(mu, dtype=np.float64)
         rhs = np.ascontiguousarray(rhs, dtype=np.float64)
@@ -307,6 +347,54 @@ class GpuSimulation:
         self.last_solve = info.as_dict()
         self._ck(st)
         return x, self.last_solve
+
+    # -------------------------------------------------------------- diagnostics
+    def updateDensityParameters(self):
+        self._ck(self.L.pic_update_density_parameters(self.ctx))
+
+    def download_density(self, sid):
+        """(conc[N], energy[N], vel[3][N], rho[N]) of one species (rho: all)."""
+        N = self.box.ncells
+        conc, en, vel, rho = np.empty(N), np.empty(N), np.empty(3 * N), np.empty(N)
+        self._ck(self.L.pic_download_density(self.ctx, sid, _d(conc), _d(en), _d(vel), _d(rho)))
+        return conc, en, vel.reshape(3, N), rho
+
+    # -------------------------------------------------------------- learned preconditioner
+    def nn_init(self, seed=1):
+        self._ck(self.L.pic_nn_init(self.ctx, seed))
+
+    def nn_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.L.pic_nn_param_count()
+        self._ck(self.L.pic_nn_set_params(self.ctx, _f(p)))
+
+    def nn_get_params(self):
+        p = np.empty(self.L.pic_nn_param_count(), dtype=np.float32)
+        self._ck(self.L.pic_nn_get_params(self.ctx, _f(p)))
+        return p
+
+    def nn_train(self, steps=200, batch=1, lr=1e-3, seed=1, smooth_max=4):
+        info = TrainInfo()
+        self._ck(self.L.pic_nn_train(self.ctx, C.byref(TrainOpts(steps, batch, lr, seed, smooth_max)),
+                                     C.byref(info)))
+        return info.as_dict()
+
+    def nn_forward(self, x0):
+        x0 = np.ascontiguousarray(x0, dtype=np.float32)
+        n, d, h, w, c = x0.shape
+        assert c == 16
+        out = np.empty_like(x0)
+        self._ck(self.L.pic_nn_forward(self.ctx, n, d, h, w, _f(x0), _f(out)))
+        return out
+
+    def nn_loss_grad(self, x0, target):
+        x0 = np.ascontiguousarray(x0, dtype=np.float32)
+        target = np.ascontiguousarray(target, dtype=np.float32)
+        n, d, h, w, _ = x0.shape
+        loss = np.zeros(1)
+        grad = np.empty(self.L.pic_nn_param_count(), dtype=np.float32)
+        self._ck(self.L.pic_nn_loss_grad(self.ctx, n, d, h, w, _f(x0), _f(target), _d(loss), _f(grad)))
+        return float(loss[0]), grad
 
     # -------------------------------------------------------------- order, diagnostics
     def sort(self):

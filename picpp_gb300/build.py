@@ -31,6 +31,7 @@ UNITS = {
     "kernels_f64.cu": ["--fmad=false"],
     "energy_noalloc.cu": [],
     "init.cu": [],
+    "nn.cu": [],
 }
 
 

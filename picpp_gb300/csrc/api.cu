@@ -8,6 +8,7 @@
 
 #include "../../include/picpp_gb300.h"
 #include "kernels.hpp"
+#include "nn.hpp"
 #include "solver.hpp"
 
 using namespace pic;
@@ -64,6 +65,12 @@ struct pic_ctx {
     long long pi_len = 0, jg_len = 0, rho_ext_len = 0;
     int nex = 1, ney = 1, nez = 1, ex = 1, ey = 1, ez = 1;
     bool moments_ready = false, efield_ready = false;
+    bool mu_valid = false;   // ctx->mu holds an operator (moments or an uploaded mu)
+    Net* net = nullptr;      // learned preconditioner, created by pic_nn_init / pic_nn_set_params
+    // updateDensityParameters grids: per species conc, energy, velocity (5N), charge density (N)
+    double* dens = nullptr;
+    double* dens_rho = nullptr;
+    int dens_ns = 0;
     // sort scratch
     int *key = nullptr, *counts = nullptr, *cursor = nullptr, *tmp = nullptr, *block_sums = nullptr;
     int *long_count = nullptr, *long_list = nullptr;
@@ -301,6 +308,7 @@ pic_status implicit_moments(pic_ctx* ctx) {
     launch_maxwell_rhs(s, g, ctx->Ei, ctx->Bi, ctx->Jh, ctx->rho_ext, ctx->ex, ctx->ey, ctx->rhs);
     CKL(ctx, "implicit moments");
     ctx->moments_ready = true;
+    ctx->mu_valid = true;
     return PIC_OK;
 }
 
@@ -452,6 +460,9 @@ pic_status pic_destroy(pic_ctx* ctx) {
                     ctx->partials, ctx->flag};
     for (void* b : bufs) if (b) cudaFree(b);
     krylov_free(ctx->kry);
+    delete ctx->net;
+    cudaFree(ctx->dens);
+    cudaFree(ctx->dens_rho);
     if (ctx->s) cudaStreamDestroy(ctx->s);
     delete ctx;
     return PIC_OK;
@@ -716,7 +727,7 @@ static pic_status solve_into(pic_ctx* ctx, const double* mu, const double* rhs, 
                              pic_solve_info* info) {
     pic_solve_opts d{PIC_GMRES_REFERENCE, 30, 50, 1e-8};
     const pic_solve_opts& opts = o ? *o : d;
-    SolveCtx sc{ctx->s, &ctx->g, mu, ctx->partials, ctx->flag, &ctx->kry, &ctx->err};
+    SolveCtx sc{ctx->s, &ctx->g, mu, ctx->partials, ctx->flag, &ctx->kry, &ctx->err, ctx->net};
     return krylov_solve(sc, rhs, x, opts, info);
 }
 
@@ -796,9 +807,26 @@ pic_status pic_maxwell_apply(pic_ctx* ctx, const double* mu, const double* x, do
     OpCoef oc = make_opcoef(ctx->g);
     launch_maxwell_apply(s, ctx->g, oc, ctx->mu, ctx->Et, ctx->En);
     CK(cudaMemcpyAsync(y, ctx->En, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    ctx->mu_valid = true;
     ctx->moments_ready = false;
     ctx->efield_ready = false;
     return sync(ctx, "maxwell apply");
+}
+
+pic_status pic_maxwell_apply_transpose(pic_ctx* ctx, const double* mu, const double* y, double* out) {
+    if (!ctx || !mu || !y || !out) return PIC_ERR_ARG;
+    if (is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not an implicit run");
+    const long long N = ctx->g.N;
+    cudaStream_t s = ctx->s;
+    CK(cudaMemcpyAsync(ctx->mu, mu, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->Et, y, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+    OpCoef oc = make_opcoef(ctx->g);
+    launch_maxwell_apply_t(s, ctx->g, oc, ctx->mu, ctx->Et, ctx->En);
+    CK(cudaMemcpyAsync(out, ctx->En, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    ctx->mu_valid = true;
+    ctx->moments_ready = false;
+    ctx->efield_ready = false;
+    return sync(ctx, "maxwell apply transpose");
 }
 
 pic_status pic_maxwell_solve(pic_ctx* ctx, const double* mu, const double* rhs, double* x, const pic_solve_opts* opts,
@@ -809,6 +837,7 @@ pic_status pic_maxwell_solve(pic_ctx* ctx, const double* mu, const double* rhs, 
     cudaStream_t s = ctx->s;
     CK(cudaMemcpyAsync(ctx->mu, mu, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->rhs, rhs, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+    ctx->mu_valid = true;
     pic_status st = solve_into(ctx, ctx->mu, ctx->rhs, ctx->Et, opts, info);
     if (st != PIC_OK && st != PIC_ERR_NOT_CONVERGED) return st;
     CK(cudaMemcpyAsync(x, ctx->Et, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
@@ -881,6 +910,106 @@ pic_status pic_profile(pic_ctx* ctx, int enable, double* phase_ms, long* launche
     }
     ctx->prof_on = enable != 0;
     return sync(ctx, "profile");
+}
+
+// ---------------------------------------------------------------- density diagnostics
+pic_status pic_update_density_parameters(pic_ctx* ctx) {
+    if (!ctx) return PIC_ERR_ARG;
+    const long long N = ctx->g.N;
+    const int ns = (int)ctx->sp.size();
+    cudaStream_t s = ctx->s;
+    if (ctx->dens_ns < ns || !ctx->dens) {
+        cudaFree(ctx->dens);
+        ctx->dens = nullptr;
+        ctx->dens_ns = 0;
+        CK(dalloc(&ctx->dens, sizeof(double) * 5 * (size_t)N * (size_t)(ns > 0 ? ns : 1)));
+        ctx->dens_ns = ns;
+    }
+    if (!ctx->dens_rho) CK(dalloc(&ctx->dens_rho, sizeof(double) * (size_t)N));
+    CK(cudaMemsetAsync(ctx->dens, 0, sizeof(double) * 5 * (size_t)N * (size_t)ns, s));
+    CK(cudaMemsetAsync(ctx->dens_rho, 0, sizeof(double) * (size_t)N, s));
+    for (int q = 0; q < ns; ++q) {
+        Species& sp = ctx->sp[q];
+        double* base = ctx->dens + 5 * N * q;
+        if (ctx->preal) PK<double>::density_deposit(s, ctx->g, view<double>(sp), sp.m, sp.w, base, base + N, base + 2 * N);
+        else PK<float>::density_deposit(s, ctx->g, view<float>(sp), sp.m, sp.w, base, base + N, base + 2 * N);
+        launch_density_finish(s, N, sp.q, base, base + N, base + 2 * N, ctx->dens_rho);
+    }
+    return sync(ctx, "density parameters");
+}
+
+pic_status pic_download_density(pic_ctx* ctx, int species, double* conc, double* energy, double* vel, double* rho) {
+    if (!ctx) return PIC_ERR_ARG;
+    pic_status st = check_species(ctx, species);
+    if (st != PIC_OK) return st;
+    if (!ctx->dens || species >= ctx->dens_ns) return fail(ctx, PIC_ERR_STATE, "update the density parameters first");
+    const long long N = ctx->g.N;
+    const double* base = ctx->dens + 5 * N * species;
+    cudaStream_t s = ctx->s;
+    if (conc) CK(cudaMemcpyAsync(conc, base, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    if (energy) CK(cudaMemcpyAsync(energy, base + N, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    if (vel) CK(cudaMemcpyAsync(vel, base + 2 * N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    if (rho) CK(cudaMemcpyAsync(rho, ctx->dens_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    return sync(ctx, "download density");
+}
+
+// ---------------------------------------------------------------- learned preconditioner
+long pic_nn_param_count(void) { return (long)Net::param_count(); }
+
+static pic_status net_of(pic_ctx* ctx, bool need_ready) {
+    if (!ctx) return PIC_ERR_ARG;
+    if (is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not an implicit run");
+    if (!ctx->net) ctx->net = new Net();
+    if (need_ready && !ctx->net->ready())
+        return fail(ctx, PIC_ERR_STATE, "learned preconditioner not initialised (pic_nn_init / pic_nn_set_params)");
+    return PIC_OK;
+}
+
+pic_status pic_nn_init(pic_ctx* ctx, unsigned long long seed) {
+    pic_status st = net_of(ctx, false);
+    if (st != PIC_OK) return st;
+    st = ctx->net->init(ctx->s, seed, &ctx->err);
+    if (st != PIC_OK) return st;
+    return sync(ctx, "nn init");
+}
+
+pic_status pic_nn_set_params(pic_ctx* ctx, const float* params) {
+    if (!params) return PIC_ERR_ARG;
+    pic_status st = net_of(ctx, false);
+    if (st != PIC_OK) return st;
+    return ctx->net->set_params(ctx->s, params, &ctx->err);
+}
+
+pic_status pic_nn_get_params(pic_ctx* ctx, float* params) {
+    if (!params) return PIC_ERR_ARG;
+    pic_status st = net_of(ctx, true);
+    if (st != PIC_OK) return st;
+    return ctx->net->get_params(ctx->s, params, &ctx->err);
+}
+
+pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info* info) {
+    if (!opts) return PIC_ERR_ARG;
+    pic_status st = net_of(ctx, true);
+    if (st != PIC_OK) return st;
+    if (!ctx->mu_valid) return fail(ctx, PIC_ERR_STATE, "no operator: update the electromagnetic parameters first");
+    st = ctx->net->train(ctx->s, ctx->g, ctx->mu, *opts, info, ctx->partials, &ctx->err);
+    if (st != PIC_OK) return st;
+    return sync(ctx, "nn train");
+}
+
+pic_status pic_nn_forward(pic_ctx* ctx, int n, int d, int h, int w, const float* x0, float* out) {
+    if (!x0 || !out) return PIC_ERR_ARG;
+    pic_status st = net_of(ctx, true);
+    if (st != PIC_OK) return st;
+    return ctx->net->forward_host(ctx->s, n, d, h, w, x0, out, &ctx->err);
+}
+
+pic_status pic_nn_loss_grad(pic_ctx* ctx, int n, int d, int h, int w, const float* x0, const float* target,
+                            double* loss, float* grad) {
+    if (!x0 || !target || !loss || !grad) return PIC_ERR_ARG;
+    pic_status st = net_of(ctx, true);
+    if (st != PIC_OK) return st;
+    return ctx->net->loss_grad_host(ctx->s, n, d, h, w, x0, target, loss, grad, &ctx->err);
 }
 
 }  // extern "C"

@@ -83,6 +83,27 @@ void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, cons
     k_maxwell_apply<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, mu, x, y);
 }
 
+void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* y,
+                            double* out) {
+    k_maxwell_apply_t<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, mu, y, out);
+}
+
+// Bulk velocity = momentum density / energy density (0 where the energy
+// density is 0), rho += q conc (momentum_collecting.cpp:960-1005).
+__global__ void k_density_finish(long long N, double q, const double* __restrict__ conc,
+                                 const double* __restrict__ energy, double* __restrict__ v, double* __restrict__ rho) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N; c += (long long)gridDim.x * blockDim.x) {
+        const double e = energy[c];
+        for (int d = 0; d < 3; ++d) v[d * N + c] = e > 0 ? v[d * N + c] / e : 0.0;
+        rho[c] += q * conc[c];
+    }
+}
+
+void launch_density_finish(cudaStream_t s, long long N, double q, const double* conc, const double* energy,
+                           double* mom_to_vel, double* rho) {
+    k_density_finish<<<grid_for(N, 256), 256, 0, s>>>(N, q, conc, energy, mom_to_vel, rho);
+}
+
 void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,
                          double* En, double* Bn, int doE, int doB) {
     k_field_update<<<grid_for(g.N, 256), 256, 0, s>>>(g, Et, E, B, En, Bn, doE, doB);

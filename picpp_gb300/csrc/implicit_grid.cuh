@@ -293,6 +293,67 @@ __global__ void __launch_bounds__(256) k_maxwell_apply(GridP g, OpCoef oc, const
     }
 }
 
+// Transpose of k_maxwell_apply.  The operator splits as A x = P x + Q (mu x)
+// with P and Q constant-coefficient periodic stencils that are symmetric
+// (P: the diagonal and the -K/d^2 neighbour couplings; Q: -c1 on the node,
+// +K/da^2 along axis a in row a, the K/(4 da dd) corner couplings, whose
+// (a, d) and (d, a) blocks coincide), so A^T y = P y + mu^T (Q y) per node.
+__global__ void __launch_bounds__(256) k_maxwell_apply_t(GridP g, OpCoef oc, const double* __restrict__ mu,
+                                                         const double* __restrict__ y, double* __restrict__ out) {
+    const long long N = g.N;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        int p[3];
+        decode(g, (int)c, p[0], p[1], p[2]);
+        const int n[3] = {g.nx, g.ny, g.nz};
+        double Py[3], Qy[3];
+        double diag = 1.0;
+        for (int ax = 0; ax < 3; ++ax)
+            if (oc.has[ax]) diag += 2.0 * oc.kd2[ax];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double ya = y[a * N + c];
+            const double c1 = oc.has[a] ? 1.0 + 2.0 * oc.kd2[a] : 1.0;
+            Py[a] = diag * ya;
+            Qy[a] = -c1 * ya;
+        }
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            if (!oc.has[ax]) continue;
+            for (int s = -1; s <= 1; s += 2) {
+                int q[3] = {p[0], p[1], p[2]};
+                q[ax] = wrap_any(q[ax] + s, n[ax]);
+                const long long cn = lin(g, q[0], q[1], q[2]);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const double ya = y[a * N + cn];
+                    Py[a] -= oc.kd2[ax] * ya;
+                    if (a == ax) Qy[a] += oc.kd2[ax] * ya;
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (d == a || !oc.has[a] || !oc.has[d]) continue;
+                double sum = 0.0;
+                for (int sa = -1; sa <= 1; sa += 2)
+                    for (int sd = -1; sd <= 1; sd += 2) {
+                        int q[3] = {p[0], p[1], p[2]};
+                        q[a] = wrap_any(q[a] + sa, n[a]);
+                        q[d] = wrap_any(q[d] + sd, n[d]);
+                        const double yd = y[d * N + lin(g, q[0], q[1], q[2])];
+                        sum += (sa * sd > 0) ? yd : -yd;
+                    }
+                Qy[a] += oc.kx4[a][d] * sum;
+            }
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            out[b * N + c] = Py[b] + mu[b * N + c] * Qy[0] + mu[(3 + b) * N + c] * Qy[1] + mu[(6 + b) * N + c] * Qy[2];
+    }
+}
+
 // evaluateElectricField (fields.cpp:326-339) and evaluateMagneticField
 // (fields.cpp:2717-2738) with evaluateRotEgeneral (fields.cpp:2862-2953).
 __global__ void __launch_bounds__(256) k_field_update(GridP g, const double* __restrict__ Et, const double* __restrict__ E,

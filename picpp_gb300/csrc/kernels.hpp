@@ -56,6 +56,9 @@ struct PK {
     static void implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const double* E,
                               const double* B, const double* Et);
     static void gather_payload(cudaStream_t s, const int* perm, long long n, PartView<T> src, PartView<T> dst);
+    // updateDensityParameters deposit of one species (diag.cuh)
+    static void density_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double m, double w, double* conc,
+                                double* energy, double* mom);
     static void particle_sums(cudaStream_t s, PartView<T> p, double m, double w, double* partials, int P);
     static void field_sq_partials(cudaStream_t s, const void* F, long long n, double* partials, int P);
     static void to_real(cudaStream_t s, const double* src, void* dst, long long n);
@@ -92,8 +95,12 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
                         const double* rho_ext, int ex, int ey, double* rhs);
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
                           double* y);
+void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* y,
+                            double* out);
 void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,
                          double* En, double* Bn, int doE, int doB);
+void launch_density_finish(cudaStream_t s, long long N, double q, const double* conc, const double* energy,
+                           double* mom_to_vel, double* rho);
 // Krylov
 void launch_dot(cudaStream_t s, const double* a, const double* b, long long n, double* partials, int P, double* out,
                 int take_sqrt);

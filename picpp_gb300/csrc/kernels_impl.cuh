@@ -3,6 +3,7 @@
 #pragma once
 #include "boris.cuh"
 #include "boris_tile.cuh"
+#include "diag.cuh"
 #include "implicit_particles.cuh"
 #include "implicit_tile.cuh"
 #include "kernels.hpp"
@@ -226,6 +227,13 @@ void PK<T>::implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double 
                           const double* B, const double* Et) {
     if (p.n == 0) return;
     k_implicit_push<T><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, E, B, Et);
+}
+
+template <typename T>
+void PK<T>::density_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double m, double w, double* conc,
+                            double* energy, double* mom) {
+    if (p.n == 0) return;
+    k_density_deposit<T><<<grid_for(p.n, 256, 32), 256, 0, s>>>(g, p, m, w, conc, energy, mom);
 }
 
 template <typename T>

@@ -1,0 +1,69 @@
+// nn.hpp -- the learned right preconditioner: a 3-level 3x3x3-convolution
+// encoder-decoder (16/32/64 channels, 6 input channels: residual and mu
+// diagonal; 3 output channels: the correction), BF16 activations with FP32
+// accumulation, trained on the device with its own forward, backward and
+// Adam kernels.  The FP64 numpy restatement in the oracle defines the same
+// network and parameter layout.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "../../include/picpp_gb300.h"
+#include "common.cuh"
+
+namespace pic {
+
+struct NetLayer {
+    const char* name;
+    int cin, cout, relu;
+    long long woff, boff;   // offsets of W[27][cout][cin] and b[cout] in the parameter vector
+};
+
+struct NetBuffers;   // activations and gradients of one shape (nn.cu)
+
+
+
+class Net {
+public:
+    Net();
+    ~Net();
+    static long long param_count();
+    static const std::vector<NetLayer>& layers();
+
+    pic_status init(cudaStream_t s, unsigned long long seed, std::string* err);
+    pic_status set_params(cudaStream_t s, const float* host, std::string* err);
+    pic_status get_params(cudaStream_t s, float* host, std::string* err);
+    bool ready() const { return ready_; }
+
+    // x0: [n][d][h][w][16] BF16 on the device is packed by the callers below.
+    // Forward on host FP32 input (channels 16), output [..][16] FP32 to host.
+    pic_status forward_host(cudaStream_t s, int n, int d, int h, int w, const float* x0, float* out, std::string* err);
+    // Loss and parameter gradient for host input and target [..][3].
+    pic_status loss_grad_host(cudaStream_t s, int n, int d, int h, int w, const float* x0, const float* target,
+                              double* loss, float* grad, std::string* err);
+    // z = s * net(v / s, mu diagonal) on the box (FP64 planar vectors of 3N).
+    pic_status apply(cudaStream_t s, const GridP& g, const double* mu, const double* v, double* z, double* scal,
+                     double* partials, std::string* err);
+    // Training on the box's operator A(mu): random fields r of unit rms
+    // (white noise after 0 .. smooth_max binomial passes), loss
+    // |A z - r|^2 / |r|^2 with z = net(r, mu diagonal); its gradient
+    // 2 A^T (A z - r) / |r|^2 (k_maxwell_apply_t) seeds the backward pass.
+    pic_status train(cudaStream_t s, const GridP& g, const double* mu, const pic_train_opts& o, pic_train_info* info,
+                     double* partials, std::string* err);
+
+private:
+    pic_status buffers(cudaStream_t s, int n, int d, int h, int w, bool grads, NetBuffers** out, std::string* err);
+    void refresh_bf16(cudaStream_t s);
+    void forward(cudaStream_t s, NetBuffers& b);
+    void backward(cudaStream_t s, NetBuffers& b);   // from b.out gradient in b's loss-gradient buffer
+    float *p_ = nullptr, *g_ = nullptr, *m_ = nullptr, *v_ = nullptr;
+    void* wk_ = nullptr;   // BF16 forward weights, per layer at woff
+    void* wt_ = nullptr;   // BF16 flipped/transposed weights
+    double* loss_ = nullptr;
+    int adam_t_ = 0;
+    bool ready_ = false;
+    std::vector<NetBuffers*> bufs_;
+};
+
+}  // namespace pic

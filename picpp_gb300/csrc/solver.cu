@@ -7,6 +7,7 @@
 #include <cmath>
 #include <vector>
 
+#include "nn.hpp"
 #include "solver.hpp"
 
 namespace pic {
@@ -173,10 +174,25 @@ pic_status gmres_reference(SolveCtx& c, const OpCoef& oc, const double* rhs, dou
     return PIC_OK;
 }
 
+pic_status ensure_z(SolveCtx& c, int m, long long L) {
+    Krylov& k = *c.k;
+    if (k.zcap >= m && k.Z) return PIC_OK;
+    cudaFree(k.Z);
+    k.Z = nullptr;
+    k.zcap = 0;
+    CKS(cudaMalloc(&k.Z, sizeof(double) * (size_t)m * L));
+    k.zcap = m;
+    return PIC_OK;
+}
+
 // Restarted GMRES(m): classical Gram-Schmidt with one re-orthogonalisation,
-// Givens rotations on the host, FP64 true residual at every restart.
+// Givens rotations on the host, FP64 true residual at every restart.  With
+// a network (pc != nullptr) it is flexible GMRES (Saad 1993) with the right
+// preconditioner z_j = pc(v_j), x += Z y; a cycle that does not halve the
+// true residual, or a non-finite preconditioned direction, switches the
+// rest of the solve to plain GMRES from the current iterate.
 pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, double* x, const pic_solve_opts& o,
-                           pic_solve_info* info) {
+                           pic_solve_info* info, Net* pc = nullptr) {
     const GridP& g = *c.g;
     const long long L = 3 * g.N;
     const int P = red_blocks(L);
@@ -185,8 +201,12 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
     const double tol = o.tol > 0 ? o.tol : 1e-8;
     pic_status st = PIC_OK;
     if ((st = ensure(c, m + 1, L)) != PIC_OK) return st;
+    if (pc && (st = ensure_z(c, m, L)) != PIC_OK) return st;
     Krylov& k = *c.k;
     auto Vp = [&](int j) { return k.V + (long long)j * L; };
+    auto Zp = [&](int j) { return k.Z + (long long)j * L; };
+    bool fallback = false;
+    double prev_rel = 1.0;
     launch_dot(c.s, b, b, L, k.part, P,k.scal, 1);
     const double bnorm = read1(c, k.scal, &st);
     if (st != PIC_OK) return st;
@@ -207,13 +227,21 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
         rel = beta / bnorm;
         if (!std::isfinite(rel)) return err(c, PIC_ERR_NUMERIC, "non-finite residual");
         if (rel <= tol || total >= maxIter) break;
+        if (pc && restarts > 0 && rel > 0.5 * prev_rel) { pc = nullptr; fallback = true; }
+        prev_rel = rel;
         launch_div(c.s, Vp(0), k.r, beta, L);
         std::fill(gv.begin(), gv.end(), 0.0);
         gv[0] = beta;
         int j = 0;
+        bool bad = false, degenerate = false;
         for (; j < m; ++j) {
             double* w = Vp(j + 1);
-            launch_maxwell_apply(c.s, g, oc, c.mu, Vp(j), w);
+            if (pc) {
+                if ((st = pc->apply(c.s, g, c.mu, Vp(j), Zp(j), k.scal + 8, c.partials, c.err)) != PIC_OK) return st;
+                launch_maxwell_apply(c.s, g, oc, c.mu, Zp(j), w);
+            } else {
+                launch_maxwell_apply(c.s, g, oc, c.mu, Vp(j), w);
+            }
             launch_multi_dot(c.s, k.V, L, j + 1, w, L, k.part, P,k.hdev);
             launch_multi_axpy_minus(c.s, w, k.V, L, j + 1, k.hdev, 1, L);
             launch_multi_dot(c.s, k.V, L, j + 1, w, L, k.part, P,k.hdev + (m + 2));
@@ -223,6 +251,18 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             CKS(cudaMemcpyAsync(h1.data(), k.hdev, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, c.s));
             CKS(cudaMemcpyAsync(h2.data(), k.hdev + (m + 2), sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, c.s));
             CKS(cudaStreamSynchronize(c.s));
+            if (pc) {
+                // a non-finite direction, or one already in the Krylov space
+                // (|h_{j+1,j}| below 1e-10 |A z_j|), ends the cycle
+                bool fin = std::isfinite(h1[j + 1]);
+                double hn2 = h1[j + 1] * h1[j + 1];
+                for (int i = 0; i <= j; ++i) {
+                    fin = fin && std::isfinite(h1[i]) && std::isfinite(h2[i]);
+                    hn2 += (h1[i] + h2[i]) * (h1[i] + h2[i]);
+                }
+                if (!fin) { bad = true; break; }
+                if (!(h1[j + 1] > 1e-10 * std::sqrt(hn2))) { degenerate = true; break; }
+            }
             for (int i = 0; i <= j; ++i) Hm(i, j) = h1[i] + h2[i];
             Hm(j + 1, j) = h1[j + 1];
             for (int i = 0; i < j; ++i) {
@@ -240,6 +280,12 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             ++total;
             if (std::fabs(gv[j + 1]) / bnorm <= tol || total >= maxIter || h1[j + 1] == 0) { ++j; break; }
         }
+        if (bad) {   // the network produced a non-finite direction: drop the cycle
+            pc = nullptr;
+            fallback = true;
+            ++restarts;
+            continue;
+        }
         const int kk = std::min(j, m);
         for (int i = kk - 1; i >= 0; --i) {
             double s = gv[i];
@@ -247,15 +293,33 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             y[i] = Hm(i, i) != 0 ? s / Hm(i, i) : 0.0;
         }
         CKS(cudaMemcpyAsync(k.ydev, y.data(), sizeof(double) * std::max(kk, 1), cudaMemcpyHostToDevice, c.s));
-        launch_combine(c.s, x, k.V, L, kk, k.ydev, 1.0, 1, L);
+        if (pc) {
+            // keep x and r: a preconditioned cycle that raises the true
+            // residual (rounding with nearly dependent directions) is undone
+            CKS(cudaMemcpyAsync(Vp(0), x, sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
+            CKS(cudaMemcpyAsync(Vp(1), k.r, sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
+        }
+        launch_combine(c.s, x, pc ? k.Z : k.V, L, kk, k.ydev, 1.0, 1, L);
         launch_maxwell_apply(c.s, g, oc, c.mu, x, k.w);
         launch_residual(c.s, k.r, b, k.w, L);
         ++restarts;
+        if (pc) {
+            launch_dot(c.s, k.r, k.r, L, k.part, P, k.scal, 1);
+            const double after = read1(c, k.scal, &st) / bnorm;
+            if (st != PIC_OK) return st;
+            if (!(after < rel)) {
+                CKS(cudaMemcpyAsync(x, Vp(0), sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
+                CKS(cudaMemcpyAsync(k.r, Vp(1), sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
+                degenerate = true;
+            }
+            if (degenerate) { pc = nullptr; fallback = true; }
+        }
     }
     if (info) {
         info->iterations = total;
         info->restarts = restarts;
         info->rel_residual = rel;
+        info->used_fallback = fallback ? 1 : 0;
     }
     return rel <= tol ? PIC_OK : err(c, PIC_ERR_NOT_CONVERGED, "GMRES did not reach the tolerance");
 }
@@ -277,6 +341,15 @@ pic_status krylov_solve(SolveCtx& c, const double* rhs, double* x, const pic_sol
     switch (o.method) {
         case PIC_GMRES_REFERENCE: st = gmres_reference(c, oc, rhs, x, o, info); break;
         case PIC_GMRES_RESTARTED: st = gmres_restarted(c, oc, rhs, x, o, info); break;
+        case PIC_FGMRES_LEARNED:
+            if (!c.net || !c.net->ready()) {
+                st = err(c, PIC_ERR_STATE, "learned preconditioner not initialised (pic_nn_init / pic_nn_set_params)");
+            } else if (c.g->nx % 4 || c.g->ny % 4 || c.g->nz % 4) {
+                st = err(c, PIC_ERR_ARG, "learned preconditioner needs box axes that are multiples of 4");
+            } else {
+                st = gmres_restarted(c, oc, rhs, x, o, info, c.net);
+            }
+            break;
         default: st = err(c, PIC_ERR_ARG, "unknown solver method"); break;
     }
     cudaEventRecord(e1, c.s);

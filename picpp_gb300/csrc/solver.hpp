@@ -23,6 +23,8 @@ struct Krylov {
     long long L = 0;
 };
 
+class Net;
+
 struct SolveCtx {
     cudaStream_t s;
     const GridP* g;
@@ -31,6 +33,7 @@ struct SolveCtx {
     int* flag;
     Krylov* k;
     std::string* err;
+    Net* net = nullptr;   // learned right preconditioner (PIC_FGMRES_LEARNED)
 };
 
 OpCoef make_opcoef(const GridP& g);

@@ -59,6 +59,20 @@ def implicit(name, nx, ny, nz, ppc, steps, seed, beam_gamma=2.0, dt=0.2):
     _save(name, 1, st, steps, out_sp, E, B, extra)
 
 
+def density(name, nx, ny, nz, ppc, seed):
+    """updateDensityParameters of a seeded state, one species per reference
+    run (the harness gives every particle reference type 0)."""
+    st = I.beams_plasma(nx, ny, nz, ppc=ppc, beam_gamma=2.0, dt=0.2, seed=seed)
+    conc, en, vel, rho = [], [], [], 0.0
+    for sp in st.species:
+        _, _, _, extra = O.run_reference(1, st.box, [dict(sp)], st.E, st.B, 0, density=True)
+        c, e, v, r = extra["density"]
+        conc.append(c[0]); en.append(e[0]); vel.append(v[0]); rho = rho + r
+    extra = dict(conc=np.array(conc), energy=np.array(en), vel=np.array(vel), rho=rho)
+    _save(name, 1, st, 0, [dict(x=sp["ox"], y=sp["oy"], z=sp["oz"], px=sp["px"], py=sp["py"], pz=sp["pz"])
+                           for sp in st.species], st.E, st.B, extra)
+
+
 def main():
     if not O.reference_available():
         sys.exit("the PIC++ reference tree is not available here")
@@ -68,6 +82,8 @@ def main():
     implicit("implicit_6x5x7_1step", 6, 5, 7, 2, 1, 21)
     implicit("implicit_8x8x8_3steps", 8, 8, 8, 2, 3, 22)
     implicit("implicit_gamma10_6x6x6_2steps", 6, 6, 6, 2, 2, 23, beam_gamma=10.0, dt=0.5)
+    density("density_8x6x5", 8, 6, 5, 3, 31)
+    density("density_2d_8x8x1", 8, 8, 1, 4, 32)
 
 
 if __name__ == "__main__":

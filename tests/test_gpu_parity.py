@@ -448,3 +448,38 @@ def test_implicit_solver_rejects_nonfinite_rhs(pg):
     # the context stays usable
     x, info = sim.maxwell_solve(np.zeros(9 * N), np.ones(3 * N))
     assert np.all(np.isfinite(x))
+
+
+@pytest.mark.parametrize("name", golden_names("density"))
+@pytest.mark.parametrize("real", [1, 0])
+def test_density_parameters_match_reference(pg, name, real):
+    """updateDensityParameters on the device against the reference's grids."""
+    f = load(name)
+    st = f["state"]
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, sort_every=0)
+    sim.upload_state(st)
+    sim.updateDensityParameters()
+    x = f["extra"]
+    tol = 1e-12 if real else TOL32
+    for s in range(len(st.species)):
+        conc, en, vel, rho = sim.download_density(s)
+        assert rel_err(conc, x["conc"][s]) < tol
+        assert rel_err(en, x["energy"][s]) < tol
+        assert rel_err(vel, x["vel"][s]) < tol
+    assert rel_err(rho, x["rho"]) < tol
+
+
+def test_density_parameters_after_explicit_steps_match_oracle(pg):
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=3, seed=17))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=1, tile=(4, 4, 4))
+    sim.upload_state(st)
+    sim.buneman_step(2)
+    sim.updateDensityParameters()
+    sp, _, _, _ = oracle_buneman(st, 2)
+    conc, en, vel, rho = O.density_moments(O.make_grid(st.box), sp)
+    for s in range(2):
+        c, e, v, r = sim.download_density(s)
+        assert rel_err(c, conc[s]) < 1e-11
+        assert rel_err(e, en[s]) < 1e-11
+        assert rel_err(v, vel[s]) < 1e-11
+    assert rel_err(r, rho) < 1e-11

@@ -102,3 +102,17 @@ def test_gmres_tiny_system_residual():
     x, it, rel = O.gmres(g, mu, rhs)
     r = O.maxwell_apply(g, mu, x) - rhs
     assert np.linalg.norm(r) / np.linalg.norm(rhs) < 1e-7
+
+
+@pytest.mark.parametrize("name", golden_names("density"))
+def test_oracle_density_moments_match_reference(name):
+    """updateDensityParameters of the reference (per species concentration,
+    energy density, bulk velocity; charge density) against the oracle."""
+    f = load(name)
+    st = f["state"]
+    conc, en, vel, rho = O.density_moments(O.make_grid(st.box), copy_species(st.species))
+    x = f["extra"]
+    assert rel_err(conc, x["conc"]) < 1e-13
+    assert rel_err(en, x["energy"]) < 1e-13
+    assert rel_err(vel, x["vel"]) < 1e-13
+    assert rel_err(rho, x["rho"]) < 1e-13

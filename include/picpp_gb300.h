@@ -62,6 +62,12 @@ typedef struct {
     int sort_every;          /* re-sort particles by cell every n steps (0: never)     */
     int tile[3];             /* tile extents of the sort key / deposit tiles (0: 8)     */
     int max_species;         /* species slots to reserve (0: 8)                         */
+    int smoothing_count;     /* smoothingCount: passes of the 3x3x3 smoothing of the
+                                current (explicit, simulation.cpp:186-188) or of
+                                rho-hat, J-hat and mu (implicit, simulation.cpp:213-217;
+                                needs pressure_compat = 0)                              */
+    double smoothing_parameter; /* smoothingParameter s: weights s/2, 1-s, s/2 per axis
+                                (createSmoothingMatrix, smoothing.cpp:105-137)          */
 } pic_config;
 
 /* Field-solve options for the implicit Maxwell system. */
@@ -178,6 +184,19 @@ pic_status pic_maxwell_apply_transpose(pic_ctx* ctx, const double* mu, const dou
 /* Solves A(mu) x = rhs (host arrays) with the given options. */
 pic_status pic_maxwell_solve(pic_ctx* ctx, const double* mu, const double* rhs, double* x,
                              const pic_solve_opts* opts, pic_solve_info* info);
+
+/* ---- checkpoint ---------------------------------------------------------- */
+/* Binary checkpoint of the device state: configuration, step counter, every
+ * species (particles in their device order and precision, ids), the field
+ * grids and the learned preconditioner's parameters when present.  Replaces
+ * the text backup of outputSimulationBackup / readBackup
+ * (PIC++/output.cpp:3432-3601, PIC++/input.cpp:342-624), which rounds to 10
+ * digits (%15.10g) and reads the type table at type - 1 (input.cpp:608).
+ * Loading needs a context of the same configuration (and tile extents); it
+ * adds missing species, restores the particle order and tile offsets of the
+ * last sort, and resumes bit for bit. */
+pic_status pic_save_checkpoint(pic_ctx* ctx, const char* path);
+pic_status pic_load_checkpoint(pic_ctx* ctx, const char* path);
 
 /* ---- learned preconditioner --------------------------------------------- */
 /* No counterpart in the reference (PIC++ solves with plain GMRES,

@@ -81,6 +81,10 @@ public:
     void exchangeParticles() {}
     void sortParticles() { check(pic_sort_particles(ctx_)); }
 
+    // outputBackup / readBackup (PIC++/simulation.cpp:921-933, input.cpp:342-624)
+    void outputBackup(const std::string& path) { check(pic_save_checkpoint(ctx_, path.c_str())); }
+    void readBackup(const std::string& path) { check(pic_load_checkpoint(ctx_, path.c_str())); }
+
     // updateDensityParameters (PIC++/momentum_collecting.cpp:760-1020)
     void updateDensityParameters() { check(pic_update_density_parameters(ctx_)); }
 

@@ -297,8 +297,40 @@ void orc_zigzag(const orc_grid* g, const orc_particles* p, double* J) {
     }
 }
 
-/* The BUNEMAN branch of Simulation::simulate (simulation.cpp:164-204) with
- * smoothingCount = 0: B half step, push, B half step, current, E step. */
+void orc_smooth(const orc_grid* g, double* a, int ncomp) {
+    const long N = NC(g);
+    const double sp = g->smoothing_parameter;
+    double w[3][3];
+    const int n[3] = {g->nx, g->ny, g->nz};
+    for (int ax = 0; ax < 3; ++ax) {
+        w[ax][0] = n[ax] > 1 ? sp / 2 : 0.0;
+        w[ax][1] = n[ax] > 1 ? 1 - sp : 1.0;
+        w[ax][2] = n[ax] > 1 ? sp / 2 : 0.0;
+    }
+    double* t = (double*)malloc(sizeof(double) * (size_t)N);
+    for (int c = 0; c < ncomp; ++c) {
+        double* f = a + (long)c * N;
+        for (int k = 0; k < g->nz; ++k)
+            for (int j = 0; j < g->ny; ++j)
+                for (int i = 0; i < g->nx; ++i) {
+                    double s = 0.0;
+                    for (int di = -1; di <= 1; ++di)
+                        for (int dj = -1; dj <= 1; ++dj)
+                            for (int dk = -1; dk <= 1; ++dk) {
+                                const double wt = w[0][di + 1] * w[1][dj + 1] * w[2][dk + 1];
+                                if (wt == 0.0) continue;
+                                s += f[IX(g, wrapi(i + di, g->nx), wrapi(j + dj, g->ny), wrapi(k + dk, g->nz))] * wt;
+                            }
+                    t[IX(g, i, j, k)] = s;
+                }
+        memcpy(f, t, sizeof(double) * (size_t)N);
+    }
+    free(t);
+}
+
+/* The BUNEMAN branch of Simulation::simulate (simulation.cpp:164-204): B half
+ * step, push, B half step, current (smoothed smoothingCount times,
+ * simulation.cpp:186-188), E step. */
 void orc_buneman_step(const orc_grid* g, orc_particles* sp, int nspecies,
                       double* E, double* B, double* J) {
     orc_yee_b_half(g, E, B);
@@ -306,6 +338,7 @@ void orc_buneman_step(const orc_grid* g, orc_particles* sp, int nspecies,
     orc_yee_b_half(g, E, B);
     memset(J, 0, sizeof(double) * 3 * NC(g));
     for (int s = 0; s < nspecies; ++s) orc_zigzag(g, &sp[s], J);
+    for (int q = 0; q < g->smoothing_count; ++q) orc_smooth(g, J, 3);
     orc_yee_e(g, E, B, J);
 }
 
@@ -999,12 +1032,40 @@ void orc_implicit_push(const orc_grid* g, orc_particles* p, const double* E,
     }
 }
 
+/* smoothChargeDensityHat, smoothFlux, smoothMatrixNodeParameter
+ * (smoothing.cpp:100-103, 251-412) on a periodic box: rho-hat (with its low
+ * ghost layer refilled from the smoothed cells), J-hat and mu. */
+void orc_smooth_moments(const orc_grid* g, double* J, double* mu, double* rho_ext) {
+    const long N = NC(g);
+    orc_smooth(g, J, 3);
+    orc_smooth(g, mu, 9);
+    const int ex = g->nx > 1 ? g->nx + 1 : 1, ey = g->ny > 1 ? g->ny + 1 : 1, ez = g->nz > 1 ? g->nz + 1 : 1;
+    double* r = (double*)malloc(sizeof(double) * (size_t)N);
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j)
+            for (int i = 0; i < g->nx; ++i) {
+                const int ri = g->nx > 1 ? i + 1 : 0, rj = g->ny > 1 ? j + 1 : 0, rk = g->nz > 1 ? k + 1 : 0;
+                r[IX(g, i, j, k)] = rho_ext[((long)rk * ey + rj) * ex + ri];
+            }
+    orc_smooth(g, r, 1);
+    for (int rk = 0; rk < ez; ++rk)
+        for (int rj = 0; rj < ey; ++rj)
+            for (int ri = 0; ri < ex; ++ri) {
+                const int i = g->nx > 1 ? wrapi(ri - 1, g->nx) : 0;
+                const int j = g->ny > 1 ? wrapi(rj - 1, g->ny) : 0;
+                const int k = g->nz > 1 ? wrapi(rk - 1, g->nz) : 0;
+                rho_ext[((long)rk * ey + rj) * ex + ri] = r[IX(g, i, j, k)];
+            }
+    free(r);
+}
+
 long orc_implicit_work_size(const orc_grid* g) {
     return NC(g) * (3 + 9 + 1 + 3 + 3 + 3 + 3) + orc_pi_size(g) + orc_rho_ext_size(g);
 }
 
 /* One implicit step, the IMPLICIT branch of Simulation::simulate
- * (simulation.cpp:205-259) with smoothingCount = 0, followed by the
+ * (simulation.cpp:205-259; smoothingCount passes over rho-hat, J-hat and mu
+ * before the field solve, simulation.cpp:213-217), followed by the
  * particle move and updateFields (fields.cpp:422-439).  work must hold
  * orc_implicit_work_size(g) doubles.  Returns the GMRES iteration count. */
 int orc_implicit_step(const orc_grid* g, orc_particles* sp, int nspecies,
@@ -1022,6 +1083,8 @@ int orc_implicit_step(const orc_grid* g, orc_particles* sp, int nspecies,
     memset(work, 0, sizeof(double) * (size_t)orc_implicit_work_size(g));
     for (int s = 0; s < nspecies; ++s) orc_implicit_deposit(g, &sp[s], E, B, J, mu, rho, Pi);
     orc_implicit_moments_finish(g, J, rho, Pi, rho_ext);
+    if (!g->pressure_compat)
+        for (int q = 0; q < g->smoothing_count; ++q) orc_smooth_moments(g, J, mu, rho_ext);
     orc_maxwell_rhs(g, E, B, J, rho_ext, rhs);
     double rel;
     int it = orc_gmres(g, mu, rhs, Et, &rel);

@@ -39,6 +39,8 @@ typedef struct {
                                loop index (momentum_collecting.cpp:565,577)  */
     int gmres_max_iter;     /* reference: maxGMRESIterations = 50            */
     double gmres_tol;       /* reference: maxErrorLevel = 1e-8               */
+    int smoothing_count;    /* Simulation::smoothingCount passes per step     */
+    double smoothing_parameter; /* Simulation::smoothingParameter             */
 } orc_grid;
 
 typedef struct {
@@ -48,6 +50,15 @@ typedef struct {
     double *ox, *oy, *oz;
     double *px, *py, *pz;
 } orc_particles;
+
+/* One pass of the periodic 3x3x3 smoothing of createSmoothingMatrix /
+ * smooth*Parameter (PIC++/smoothing.cpp:105-137, 251-412, 535-739): weights
+ * s/2, 1-s, s/2 per active axis, on ncomp planar components of N values. */
+void orc_smooth(const orc_grid* g, double* a, int ncomp);
+
+/* The implicit moments' smoothing passes (periodic placement only):
+ * rho-hat with its low ghost layer, J-hat, mu. */
+void orc_smooth_moments(const orc_grid* g, double* J, double* mu, double* rho_ext);
 
 /* ---- explicit Buneman / Tristan path ---- */
 void orc_yee_b_half(const orc_grid* g, const double* E, double* B);

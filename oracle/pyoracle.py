@@ -29,7 +29,8 @@ class Grid(C.Structure):
                 ("tx", C.c_int), ("ty", C.c_int), ("tz", C.c_int),
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
                 ("theta", C.c_double), ("eta", C.c_double), ("cfix", C.c_double),
-                ("pressure_compat", C.c_int), ("gmres_max_iter", C.c_int), ("gmres_tol", C.c_double)]
+                ("pressure_compat", C.c_int), ("gmres_max_iter", C.c_int), ("gmres_tol", C.c_double),
+                ("smoothing_count", C.c_int), ("smoothing_parameter", C.c_double)]
 
 
 class Particles(C.Structure):
@@ -81,6 +82,8 @@ def lib():
         L.orc_implicit_work_size.restype = C.c_long
         L.orc_energy.argtypes = [g, p, C.c_int, _dp, _dp, _dp]
         L.orc_density_moments.argtypes = [g, p, C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_smooth.argtypes = [g, _dp, C.c_int]
+        L.orc_smooth_moments.argtypes = [g, _dp, _dp, _dp]
     return _lib
 
 
@@ -89,10 +92,12 @@ def _d(a: np.ndarray):
     return a.ctypes.data_as(_dp)
 
 
-def make_grid(box, tile=(8, 8, 8), pressure_compat=1, gmres_max_iter=50, gmres_tol=1e-8) -> Grid:
+def make_grid(box, tile=(8, 8, 8), pressure_compat=1, gmres_max_iter=50, gmres_tol=1e-8, smoothing_count=0,
+              smoothing_parameter=0.5) -> Grid:
     t = [min(tile[0], box.nx), min(tile[1], box.ny), min(tile[2], box.nz)]
     return Grid(box.nx, box.ny, box.nz, t[0], t[1], t[2], box.dx, box.dy, box.dz, box.dt,
-                box.theta, box.eta, box.cfix, pressure_compat, gmres_max_iter, gmres_tol)
+                box.theta, box.eta, box.cfix, pressure_compat, gmres_max_iter, gmres_tol, smoothing_count,
+                smoothing_parameter)
 
 
 def _as_particles(sp: dict) -> Particles:
@@ -216,7 +221,8 @@ def build_reference() -> str:
     return REF_BIN
 
 
-def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = False, density: bool = False):
+def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = False, density: bool = False,
+                  smoothing_count: int = 0, smoothing_parameter: float = 0.5):
     """Runs the PIC++ reference (compiled from its own sources) on the state
     and returns (species positions/momenta by input order, E, B, extras)."""
     from picpp_gb300.initstate import positions
@@ -225,8 +231,9 @@ def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = Fals
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            f.write(struct.pack("<8i", solver, box.nx, box.ny, box.nz, len(species), steps, int(dump), int(density)))
-            f.write(struct.pack("<4d", box.dx, box.dt, box.theta, box.eta))
+            f.write(struct.pack("<9i", solver, box.nx, box.ny, box.nz, len(species), steps, int(dump), int(density),
+                                smoothing_count))
+            f.write(struct.pack("<5d", box.dx, box.dt, box.theta, box.eta, smoothing_parameter))
             for sp in species:
                 x, y, z = positions(box, sp)
                 f.write(struct.pack("<3dq", sp["q"], sp["m"], sp["w"], len(sp["cell"])))

@@ -49,11 +49,13 @@ int main(int argc, char** argv) {
     if (argc != 3) die("usage: harness in.bin out.bin");
     FILE* f = fopen(argv[1], "rb");
     if (!f) die("cannot open input");
-    int32_t hdr[8];
-    for (int a = 0; a < 8; ++a) hdr[a] = rd<int32_t>(f);
+    int32_t hdr[9];
+    for (int a = 0; a < 9; ++a) hdr[a] = rd<int32_t>(f);
     const int solver = hdr[0], nx = hdr[1], ny = hdr[2], nz = hdr[3], ns = hdr[4], steps = hdr[5], dump = hdr[6];
     const int density = hdr[7];   // 1: append updateDensityParameters' grids after the run
+    const int smoothing = hdr[8];  // smoothingCount
     double dx = rd<double>(f), dt = rd<double>(f), theta = rd<double>(f), eta = rd<double>(f);
+    const double smoothing_parameter = rd<double>(f);
     Box bx{nx, ny, nz};
     const long N = (long)nx * ny * nz;
 
@@ -83,7 +85,8 @@ int main(int argc, char** argv) {
     S->boundaryConditionTypeX = PERIODIC;
     S->boundaryConditionTypeY = PERIODIC;
     S->boundaryConditionTypeZ = PERIODIC;
-    S->smoothingCount = 0;
+    S->smoothingCount = smoothing;
+    S->smoothingParameter = smoothing_parameter;
     S->theta = theta;
     S->eta = eta;
     S->deltaT = dt;
@@ -163,6 +166,8 @@ int main(int argc, char** argv) {
             S->tristanEvaluateBhalfStep();
             S->exchangeBunemanBfield(S->bunemanBx, S->bunemanBy, S->bunemanBz);
             S->tristanUpdateFlux();
+            for (int n = 0; n < S->smoothingCount; ++n)   // simulation.cpp:186-188
+                S->smoothBunemanEfieldGeneral(S->bunemanJx, S->bunemanJy, S->bunemanJz);
             S->tristanEvaluateE();
             S->exchangeBunemanEfield(S->bunemanEx, S->bunemanEy, S->bunemanEz);
             // simulation.cpp:266-279, 394
@@ -181,6 +186,11 @@ int main(int argc, char** argv) {
             // simulation.cpp:205-259
             S->evaluateParticlesRotationTensor();
             S->updateElectroMagneticParameters();
+            for (int n = 0; n < S->smoothingCount; ++n) {   // simulation.cpp:213-217
+                S->smoothChargeDensityHat();
+                S->smoothFlux();
+                S->smoothMatrixNodeParameter(S->dielectricTensor);
+            }
             S->evaluateElectricField();
             S->exchangeEfield();
             S->evaluateMagneticField();

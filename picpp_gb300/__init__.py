@@ -33,6 +33,7 @@ EXPORTS = [
     "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile", "pic_energy_noalloc",
     "pic_fill_species", "pic_nn_param_count", "pic_nn_init", "pic_nn_set_params", "pic_nn_get_params",
     "pic_nn_train", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
+    "pic_save_checkpoint", "pic_load_checkpoint",
 ]
 PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover"]
 
@@ -49,7 +50,7 @@ class Config(C.Structure):
                 ("theta", C.c_double), ("eta", C.c_double), ("cfix", C.c_double),
                 ("solver", C.c_int), ("particle_real", C.c_int), ("field_real", C.c_int),
                 ("pressure_compat", C.c_int), ("sort_every", C.c_int), ("tile", C.c_int * 3),
-                ("max_species", C.c_int)]
+                ("max_species", C.c_int), ("smoothing_count", C.c_int), ("smoothing_parameter", C.c_double)]
 
 
 class SolveOpts(C.Structure):
@@ -125,6 +126,8 @@ def load_library(path: str | None = None):
     ptrs = C.POINTER(C.c_void_p)
     L.pic_energy_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, C.c_int,
                                      C.POINTER(C.c_long), _dp, _dp, ptrs, ptrs, ptrs, vp, _dp]
+    L.pic_save_checkpoint.argtypes = [vp, C.c_char_p]
+    L.pic_load_checkpoint.argtypes = [vp, C.c_char_p]
     L.pic_update_density_parameters.argtypes = [vp]
     L.pic_download_density.argtypes = [vp, C.c_int, _dp, _dp, _dp, _dp]
     L.pic_nn_param_count.argtypes = []
@@ -173,7 +176,7 @@ class GpuSimulation:
     ``download_*``; each method mirrors the member function of that name."""
 
     def __init__(self, box, solver=BUNEMAN, particle_real=F32, field_real=None, pressure_compat=1,
-                 sort_every=1, tile=(8, 8, 8), max_species=8):
+                 sort_every=1, tile=(8, 8, 8), max_species=8, smoothing_count=0, smoothing_parameter=0.5):
         self.L = load_library()
         self.box = box
         cfg = Config()
@@ -185,6 +188,8 @@ class GpuSimulation:
         cfg.field_real = particle_real if field_real is None else field_real
         cfg.pressure_compat = pressure_compat
         cfg.sort_every = sort_every
+        cfg.smoothing_count = smoothing_count
+        cfg.smoothing_parameter = smoothing_parameter
         cfg.tile[0], cfg.tile[1], cfg.tile[2] = tile
         cfg.max_species = max_species
         self.cfg = cfg
@@ -347,6 +352,13 @@ class GpuSimulation:
         self.last_solve = info.as_dict()
         self._ck(st)
         return x, self.last_solve
+
+    # -------------------------------------------------------------- checkpoint
+    def save_checkpoint(self, path):
+        self._ck(self.L.pic_save_checkpoint(self.ctx, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        self._ck(self.L.pic_load_checkpoint(self.ctx, os.fsencode(path)))
 
     # -------------------------------------------------------------- diagnostics
     def updateDensityParameters(self):

@@ -1,6 +1,8 @@
 // api.cu -- the C ABI (include/picpp_gb300.h): one context per simulation,
 // owning every device buffer, one CUDA stream, status codes instead of exit().
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -67,6 +69,8 @@ struct pic_ctx {
     bool moments_ready = false, efield_ready = false;
     bool mu_valid = false;   // ctx->mu holds an operator (moments or an uploaded mu)
     Net* net = nullptr;      // learned preconditioner, created by pic_nn_init / pic_nn_set_params
+    double* smooth_tmp = nullptr;   // scratch of the smoothing passes (max(9N, rho-hat ext))
+    float* fields32 = nullptr;      // FP32 copies of E^n, B^n (6N) for the FP32 deposit
     // updateDensityParameters grids: per species conc, energy, velocity (5N), charge density (N)
     double* dens = nullptr;
     double* dens_rho = nullptr;
@@ -203,6 +207,45 @@ bool all_sorted(const pic_ctx* ctx) {
     return true;
 }
 
+pic_status ensure_smooth_tmp(pic_ctx* ctx) {
+    if (ctx->smooth_tmp) return PIC_OK;
+    const size_t n = std::max<size_t>(9 * (size_t)ctx->g.N, (size_t)ctx->rho_ext_len);
+    CK(dalloc(&ctx->smooth_tmp, sizeof(double) * n));
+    return PIC_OK;
+}
+
+// smoothingCount passes over the explicit current (simulation.cpp:186-188).
+pic_status smooth_current(pic_ctx* ctx) {
+    if (ctx->cfg.smoothing_count <= 0) return PIC_OK;
+    pic_status st = ensure_smooth_tmp(ctx);
+    if (st != PIC_OK) return st;
+    const size_t L = 3 * (size_t)ctx->g.N;
+    for (int q = 0; q < ctx->cfg.smoothing_count; ++q) {
+        launch_smooth(ctx->s, ctx->g, ctx->J, ctx->smooth_tmp, 3, ctx->cfg.smoothing_parameter);
+        CK(cudaMemcpyAsync(ctx->J, ctx->smooth_tmp, sizeof(double) * L, cudaMemcpyDeviceToDevice, ctx->s));
+    }
+    return PIC_OK;
+}
+
+// smoothingCount passes over rho-hat, J-hat and mu (simulation.cpp:213-217).
+pic_status smooth_moments(pic_ctx* ctx) {
+    if (ctx->cfg.smoothing_count <= 0) return PIC_OK;
+    pic_status st = ensure_smooth_tmp(ctx);
+    if (st != PIC_OK) return st;
+    const GridP& g = ctx->g;
+    const double sp = ctx->cfg.smoothing_parameter;
+    cudaStream_t s = ctx->s;
+    for (int q = 0; q < ctx->cfg.smoothing_count; ++q) {
+        launch_smooth_rho_ext(s, g, ctx->rho_ext, ctx->smooth_tmp, ctx->ex, ctx->ey, ctx->ez, sp);
+        CK(cudaMemcpyAsync(ctx->rho_ext, ctx->smooth_tmp, sizeof(double) * ctx->rho_ext_len, cudaMemcpyDeviceToDevice, s));
+        launch_smooth(s, g, ctx->Jh, ctx->smooth_tmp, 3, sp);
+        CK(cudaMemcpyAsync(ctx->Jh, ctx->smooth_tmp, sizeof(double) * 3 * g.N, cudaMemcpyDeviceToDevice, s));
+        launch_smooth(s, g, ctx->mu, ctx->smooth_tmp, 9, sp);
+        CK(cudaMemcpyAsync(ctx->mu, ctx->smooth_tmp, sizeof(double) * 9 * g.N, cudaMemcpyDeviceToDevice, s));
+    }
+    return PIC_OK;
+}
+
 // -------------------------------------------------------------- explicit
 template <typename T>
 pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
@@ -254,7 +297,9 @@ pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
             for (auto& sp : ctx->sp) PK<T>::zigzag(s, g, view<T>(sp), sp.q, sp.m, sp.w, ctx->J);
         }
         {
-            Phase ph(ctx, PIC_PHASE_FIELDS, 1);
+            Phase ph(ctx, PIC_PHASE_FIELDS, 2 * ctx->cfg.smoothing_count + 1);
+            pic_status st = smooth_current(ctx);
+            if (st != PIC_OK) return st;
             PK<T>::yee_e(s, g, ctx->E, ctx->B, ctx->J);
         }
         CKL(ctx, "buneman step");
@@ -288,7 +333,16 @@ pic_status implicit_moments(pic_ctx* ctx) {
             S.q[q] = ctx->sp[q].q; S.m[q] = ctx->sp[q].m; S.w[q] = ctx->sp[q].w;
             S.off[q] = ctx->sp[q].off;
         }
-        PK<T>::implicit_deposit_tiled(s, g, ctx->tg, bk, S, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu, ctx->rho, ctx->Pi);
+        const T* Ef = (const T*)ctx->Ei;
+        const T* Bf = (const T*)ctx->Bi;
+        if (sizeof(T) == sizeof(float)) {   // FP32 copies of E^n and B^n for the FP32 gathers
+            if (!ctx->fields32) CK(dalloc(&ctx->fields32, sizeof(float) * 6 * (size_t)N));
+            PK<float>::to_real(s, ctx->Ei, ctx->fields32, 3 * N);
+            PK<float>::to_real(s, ctx->Bi, ctx->fields32 + 3 * N, 3 * N);
+            Ef = (const T*)ctx->fields32;
+            Bf = (const T*)(ctx->fields32 + 3 * N);
+        }
+        PK<T>::implicit_deposit_tiled(s, g, ctx->tg, bk, S, Ef, Bf, ctx->Jh, ctx->mu, ctx->rho, ctx->Pi);
     } else {
         for (auto& sp : ctx->sp)
             PK<T>::implicit_deposit(s, g, view<T>(sp), sp.q, sp.m, sp.w, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu,
@@ -304,6 +358,8 @@ pic_status implicit_moments(pic_ctx* ctx) {
         launch_j_minus_divpi(s, g, ctx->Pi, ctx->Jh, ctx->Jg);
         CK(cudaMemcpyAsync(ctx->Jh, ctx->Jg, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
         launch_rho_ext_periodic(s, g, ctx->Jh, ctx->rho, ctx->rho_ext, ctx->ex, ctx->ey, ctx->ez);
+        pic_status st = smooth_moments(ctx);
+        if (st != PIC_OK) return st;
     }
     launch_maxwell_rhs(s, g, ctx->Ei, ctx->Bi, ctx->Jh, ctx->rho_ext, ctx->ex, ctx->ey, ctx->rhs);
     CKL(ctx, "implicit moments");
@@ -315,9 +371,23 @@ pic_status implicit_moments(pic_ctx* ctx) {
 template <typename T>
 pic_status implicit_move(pic_ctx* ctx) {
     Phase ph(ctx, PIC_PHASE_MOVER, (int)ctx->sp.size());
-    for (auto& sp : ctx->sp) PK<T>::implicit_push(ctx->s, ctx->g, view<T>(sp), sp.q, sp.m, ctx->Ei, ctx->Bi, ctx->Et);
+    bool tiled = false;
+    if (all_sorted(ctx)) {
+        ImpSpecies<T> S{};
+        S.ns = (int)ctx->sp.size();
+        for (int q = 0; q < S.ns; ++q) {
+            S.p[q] = view<T>(ctx->sp[q]);
+            S.q[q] = ctx->sp[q].q; S.m[q] = ctx->sp[q].m; S.w[q] = ctx->sp[q].w;
+            S.off[q] = ctx->sp[q].off;
+        }
+        tiled = PK<T>::implicit_push_tiled(ctx->s, ctx->g, ctx->tg, S, ctx->Ei, ctx->Bi, ctx->Et);
+    }
+    if (!tiled)
+        for (auto& sp : ctx->sp)
+            PK<T>::implicit_push(ctx->s, ctx->g, view<T>(sp), sp.q, sp.m, ctx->Ei, ctx->Bi, ctx->Et);
     CKL(ctx, "implicit mover");
-    for (auto& sp : ctx->sp) sp.sorted = false;
+    // the tile order stays valid: the tiled deposit and mover check every
+    // particle's cell and take their halo or global path for drifted ones
     return PIC_OK;
 }
 
@@ -352,6 +422,11 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     if (c.particle_real != PIC_REAL_F32 && c.particle_real != PIC_REAL_F64) return PIC_ERR_ARG;
     if (c.solver == PIC_SOLVER_BUNEMAN && c.field_real != c.particle_real) return PIC_ERR_ARG;
     if (c.solver == PIC_SOLVER_IMPLICIT && !(c.theta > 0)) return PIC_ERR_ARG;
+    if (c.smoothing_count < 0 || (c.smoothing_count > 0 && !(c.smoothing_parameter >= 0 && c.smoothing_parameter <= 1)))
+        return PIC_ERR_ARG;
+    // the reference smooths J-hat and rho-hat including its own ghost values,
+    // which only the periodic pressure placement represents as periodic images
+    if (c.smoothing_count > 0 && c.solver == PIC_SOLVER_IMPLICIT && c.pressure_compat) return PIC_ERR_ARG;
     long long N = (long long)c.nx * c.ny * c.nz;
     if (N >= (1LL << 31)) return PIC_ERR_ARG;
     int tile[3];
@@ -463,6 +538,8 @@ pic_status pic_destroy(pic_ctx* ctx) {
     delete ctx->net;
     cudaFree(ctx->dens);
     cudaFree(ctx->dens_rho);
+    cudaFree(ctx->smooth_tmp);
+    cudaFree(ctx->fields32);
     if (ctx->s) cudaStreamDestroy(ctx->s);
     delete ctx;
     return PIC_OK;
@@ -691,6 +768,8 @@ pic_status pic_tristan_update_flux(pic_ctx* ctx) {
         if (ctx->preal) PK<double>::zigzag(ctx->s, ctx->g, view<double>(sp), sp.q, sp.m, sp.w, ctx->J);
         else PK<float>::zigzag(ctx->s, ctx->g, view<float>(sp), sp.q, sp.m, sp.w, ctx->J);
     }
+    pic_status st = smooth_current(ctx);
+    if (st != PIC_OK) return st;
     return sync(ctx, "update flux");
 }
 
@@ -910,6 +989,154 @@ pic_status pic_profile(pic_ctx* ctx, int enable, double* phase_ms, long* launche
     }
     ctx->prof_on = enable != 0;
     return sync(ctx, "profile");
+}
+
+// ---------------------------------------------------------------- checkpoint
+namespace {
+
+constexpr char kCkptMagic[8] = {'P', 'I', 'C', 'G', 'B', '3', '0', '0'};
+constexpr int32_t kCkptVersion = 2;
+
+struct CkptHeader {
+    char magic[8];
+    int32_t version, solver, particle_real, field_real, nx, ny, nz, nspecies, has_net, sorted, pad;
+    int64_t step;
+    double dx, dy, dz, dt, theta, eta, cfix;
+};
+
+// Device bytes to the file through a host buffer.
+pic_status dev_write(pic_ctx* ctx, FILE* f, const void* d, size_t bytes, std::vector<char>& buf) {
+    if (bytes == 0) return PIC_OK;
+    buf.resize(bytes);
+    CK(cudaMemcpyAsync(buf.data(), d, bytes, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    if (fwrite(buf.data(), 1, bytes, f) != bytes) return fail(ctx, PIC_ERR_ARG, "checkpoint write failed");
+    return PIC_OK;
+}
+
+pic_status dev_read(pic_ctx* ctx, FILE* f, void* d, size_t bytes, std::vector<char>& buf) {
+    if (bytes == 0) return PIC_OK;
+    buf.resize(bytes);
+    if (fread(buf.data(), 1, bytes, f) != bytes) return fail(ctx, PIC_ERR_ARG, "checkpoint truncated");
+    CK(cudaMemcpyAsync(d, buf.data(), bytes, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return PIC_OK;
+}
+
+struct FileCloser {
+    FILE* f;
+    ~FileCloser() { if (f) fclose(f); }
+};
+
+}  // namespace
+
+pic_status pic_save_checkpoint(pic_ctx* ctx, const char* path) {
+    if (!ctx || !path) return PIC_ERR_ARG;
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(ctx, PIC_ERR_ARG, std::string("cannot open ") + path);
+    FileCloser fc{f};
+    CkptHeader h{};
+    memcpy(h.magic, kCkptMagic, 8);
+    h.version = kCkptVersion;
+    h.solver = ctx->cfg.solver; h.particle_real = ctx->cfg.particle_real; h.field_real = ctx->cfg.field_real;
+    h.nx = ctx->g.nx; h.ny = ctx->g.ny; h.nz = ctx->g.nz;
+    h.nspecies = (int32_t)ctx->sp.size();
+    h.has_net = ctx->net && ctx->net->ready() ? 1 : 0;
+    h.sorted = all_sorted(ctx) ? 1 : 0;
+    h.step = ctx->step;
+    h.dx = ctx->g.dx; h.dy = ctx->g.dy; h.dz = ctx->g.dz; h.dt = ctx->g.dt;
+    h.theta = ctx->g.theta; h.eta = ctx->g.eta; h.cfix = ctx->g.cfix;
+    if (fwrite(&h, sizeof(h), 1, f) != 1) return fail(ctx, PIC_ERR_ARG, "checkpoint write failed");
+    std::vector<char> buf;
+    pic_status st;
+    for (auto& sp : ctx->sp) {
+        const double qmw[3] = {sp.q, sp.m, sp.w};
+        const int64_t n = sp.n;
+        if (fwrite(qmw, sizeof(qmw), 1, f) != 1 || fwrite(&n, sizeof(n), 1, f) != 1)
+            return fail(ctx, PIC_ERR_ARG, "checkpoint write failed");
+        if ((st = dev_write(ctx, f, sp.cell, sizeof(int) * n, buf)) != PIC_OK) return st;
+        if ((st = dev_write(ctx, f, sp.id, sizeof(int) * n, buf)) != PIC_OK) return st;
+        for (int a = 0; a < 6; ++a)
+            if ((st = dev_write(ctx, f, sp.a[a], ctx->rsz * n, buf)) != PIC_OK) return st;
+        // tile offsets of the last sort (particles may have drifted since)
+        if (h.sorted && (st = dev_write(ctx, f, sp.off, sizeof(int) * ((size_t)ctx->nkeys + 1), buf)) != PIC_OK)
+            return st;
+    }
+    const size_t L = 3 * (size_t)ctx->g.N;
+    if (is_buneman(ctx)) {
+        const size_t fb = ctx->preal ? sizeof(double) : sizeof(float);
+        if ((st = dev_write(ctx, f, ctx->E, fb * L, buf)) != PIC_OK) return st;
+        if ((st = dev_write(ctx, f, ctx->B, fb * L, buf)) != PIC_OK) return st;
+        if ((st = dev_write(ctx, f, ctx->J, sizeof(double) * L, buf)) != PIC_OK) return st;
+    } else {
+        if ((st = dev_write(ctx, f, ctx->Ei, sizeof(double) * L, buf)) != PIC_OK) return st;
+        if ((st = dev_write(ctx, f, ctx->Bi, sizeof(double) * L, buf)) != PIC_OK) return st;
+        if ((st = dev_write(ctx, f, ctx->Jh, sizeof(double) * L, buf)) != PIC_OK) return st;
+    }
+    if (h.has_net) {
+        std::vector<float> p((size_t)Net::param_count());
+        if ((st = ctx->net->get_params(ctx->s, p.data(), &ctx->err)) != PIC_OK) return st;
+        if (fwrite(p.data(), sizeof(float), p.size(), f) != p.size()) return fail(ctx, PIC_ERR_ARG, "checkpoint write failed");
+    }
+    return PIC_OK;
+}
+
+pic_status pic_load_checkpoint(pic_ctx* ctx, const char* path) {
+    if (!ctx || !path) return PIC_ERR_ARG;
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(ctx, PIC_ERR_ARG, std::string("cannot open ") + path);
+    FileCloser fc{f};
+    CkptHeader h{};
+    if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != kCkptVersion)
+        return fail(ctx, PIC_ERR_ARG, "not a picpp_gb300 checkpoint");
+    if (h.solver != ctx->cfg.solver || h.particle_real != ctx->cfg.particle_real ||
+        h.field_real != ctx->cfg.field_real || h.nx != ctx->g.nx || h.ny != ctx->g.ny || h.nz != ctx->g.nz ||
+        h.dx != ctx->g.dx || h.dy != ctx->g.dy || h.dz != ctx->g.dz || h.dt != ctx->g.dt ||
+        h.theta != ctx->g.theta || h.eta != ctx->g.eta || h.cfix != ctx->g.cfix)
+        return fail(ctx, PIC_ERR_ARG, "checkpoint configuration differs from the context's");
+    if (h.nspecies > ctx->cfg.max_species) return fail(ctx, PIC_ERR_ARG, "too many species in the checkpoint");
+    std::vector<char> buf;
+    pic_status st;
+    for (int q = 0; q < h.nspecies; ++q) {
+        double qmw[3];
+        int64_t n = 0;
+        if (fread(qmw, sizeof(qmw), 1, f) != 1 || fread(&n, sizeof(n), 1, f) != 1 || n < 0)
+            return fail(ctx, PIC_ERR_ARG, "checkpoint truncated");
+        if (q >= (int)ctx->sp.size()) {
+            if ((st = pic_add_species(ctx, qmw[0], qmw[1], qmw[2], (long)n, nullptr)) != PIC_OK) return st;
+        }
+        Species& sp = ctx->sp[q];
+        if (n > sp.cap) return fail(ctx, PIC_ERR_NOMEM, "checkpoint species exceeds the capacity");
+        sp.q = qmw[0]; sp.m = qmw[1]; sp.w = qmw[2];
+        if ((st = dev_read(ctx, f, sp.cell, sizeof(int) * n, buf)) != PIC_OK) return st;
+        if ((st = dev_read(ctx, f, sp.id, sizeof(int) * n, buf)) != PIC_OK) return st;
+        for (int a = 0; a < 6; ++a)
+            if ((st = dev_read(ctx, f, sp.a[a], ctx->rsz * n, buf)) != PIC_OK) return st;
+        if (h.sorted && (st = dev_read(ctx, f, sp.off, sizeof(int) * ((size_t)ctx->nkeys + 1), buf)) != PIC_OK)
+            return st;
+        sp.n = n;
+        sp.sorted = h.sorted != 0;
+    }
+    const size_t L = 3 * (size_t)ctx->g.N;
+    if (is_buneman(ctx)) {
+        const size_t fb = ctx->preal ? sizeof(double) : sizeof(float);
+        if ((st = dev_read(ctx, f, ctx->E, fb * L, buf)) != PIC_OK) return st;
+        if ((st = dev_read(ctx, f, ctx->B, fb * L, buf)) != PIC_OK) return st;
+        if ((st = dev_read(ctx, f, ctx->J, sizeof(double) * L, buf)) != PIC_OK) return st;
+    } else {
+        if ((st = dev_read(ctx, f, ctx->Ei, sizeof(double) * L, buf)) != PIC_OK) return st;
+        if ((st = dev_read(ctx, f, ctx->Bi, sizeof(double) * L, buf)) != PIC_OK) return st;
+        if ((st = dev_read(ctx, f, ctx->Jh, sizeof(double) * L, buf)) != PIC_OK) return st;
+    }
+    if (h.has_net) {
+        std::vector<float> p((size_t)Net::param_count());
+        if (fread(p.data(), sizeof(float), p.size(), f) != p.size()) return fail(ctx, PIC_ERR_ARG, "checkpoint truncated");
+        if (!ctx->net) ctx->net = new Net();
+        if ((st = ctx->net->set_params(ctx->s, p.data(), &ctx->err)) != PIC_OK) return st;
+    }
+    ctx->step = h.step;
+    ctx->moments_ready = ctx->efield_ready = ctx->mu_valid = false;
+    return sync(ctx, "load checkpoint");
 }
 
 // ---------------------------------------------------------------- density diagnostics

@@ -88,6 +88,79 @@ void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, co
     k_maxwell_apply_t<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, mu, y, out);
 }
 
+// One pass of the periodic 3x3x3 smoothing (createSmoothingMatrix and the
+// smooth*Parameter loops, smoothing.cpp:105-137, 251-412, 535-739): weights
+// s/2, 1-s, s/2 on every active axis, ncomp planar components, src -> dst.
+__global__ void k_smooth27(GridP g, const double* __restrict__ src, double* __restrict__ dst, int ncomp, double sp) {
+    const long long N = g.N;
+    const double wside = sp / 2, wmid = 1.0 - sp;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < N * ncomp;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long c = e / N, id = e - c * N;
+        int i, j, k;
+        decode(g, (int)id, i, j, k);
+        const double* a = src + c * N;
+        double s = 0.0;
+        for (int dk = -1; dk <= 1; ++dk) {
+            if (!g.z3 && dk) continue;
+            const double wk = g.z3 ? (dk ? wside : wmid) : 1.0;
+            for (int dj = -1; dj <= 1; ++dj) {
+                if (!g.y3 && dj) continue;
+                const double wj = g.y3 ? (dj ? wside : wmid) : 1.0;
+                for (int di = -1; di <= 1; ++di) {
+                    if (g.nx == 1 && di) continue;
+                    const double wi = g.nx > 1 ? (di ? wside : wmid) : 1.0;
+                    s += a[linw(g, i + di, j + dj, k + dk)] * (wi * wj * wk);
+                }
+            }
+        }
+        dst[e] = s;
+    }
+}
+
+// The same pass on rho-hat stored with one low ghost layer (extent n + 1 on
+// active axes, ext index e holds cell e - 1, so ext 0 is the periodic image
+// of cell n - 1): every ext entry gets the smoothed value of its cell.
+__global__ void k_smooth_rho_ext(GridP g, const double* __restrict__ src, double* __restrict__ dst, int ex, int ey,
+                                 int ez, double sp) {
+    const long long tot = (long long)ex * ey * ez;
+    const double wside = sp / 2, wmid = 1.0 - sp;
+    auto at = [&](int i, int j, int k) -> double {   // cell (i, j, k), periodic, from the ext array
+        const int ri = g.nx > 1 ? wrap_any(i, g.nx) + 1 : 0;
+        const int rj = g.y3 ? wrap_any(j, g.ny) + 1 : 0;
+        const int rk = g.z3 ? wrap_any(k, g.nz) + 1 : 0;
+        return src[((long long)rk * ey + rj) * ex + ri];
+    };
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+        const int ri = (int)(e % ex), rj = (int)((e / ex) % ey), rk = (int)(e / ((long long)ex * ey));
+        const int i = g.nx > 1 ? ri - 1 : 0, j = g.y3 ? rj - 1 : 0, k = g.z3 ? rk - 1 : 0;
+        double s = 0.0;
+        for (int dk = -1; dk <= 1; ++dk) {
+            if (!g.z3 && dk) continue;
+            const double wk = g.z3 ? (dk ? wside : wmid) : 1.0;
+            for (int dj = -1; dj <= 1; ++dj) {
+                if (!g.y3 && dj) continue;
+                const double wj = g.y3 ? (dj ? wside : wmid) : 1.0;
+                for (int di = -1; di <= 1; ++di) {
+                    if (g.nx == 1 && di) continue;
+                    const double wi = g.nx > 1 ? (di ? wside : wmid) : 1.0;
+                    s += at(i + di, j + dj, k + dk) * (wi * wj * wk);
+                }
+            }
+        }
+        dst[e] = s;
+    }
+}
+
+void launch_smooth(cudaStream_t s, const GridP& g, const double* src, double* dst, int ncomp, double sp) {
+    k_smooth27<<<grid_for(g.N * ncomp, 256), 256, 0, s>>>(g, src, dst, ncomp, sp);
+}
+
+void launch_smooth_rho_ext(cudaStream_t s, const GridP& g, const double* src, double* dst, int ex, int ey, int ez,
+                           double sp) {
+    k_smooth_rho_ext<<<grid_for((long long)ex * ey * ez, 256), 256, 0, s>>>(g, src, dst, ex, ey, ez, sp);
+}
+
 // Bulk velocity = momentum density / energy density (0 where the energy
 // density is 0), rho += q conc (momentum_collecting.cpp:960-1005).
 __global__ void k_density_finish(long long N, double q, const double* __restrict__ conc,

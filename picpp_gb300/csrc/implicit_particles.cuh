@@ -6,9 +6,9 @@
 
 namespace pic {
 
-template <typename T>
+template <typename T, typename FT = double>
 __device__ __forceinline__ void gather_node(const GridP& g, int i, int j, int k, T ox, T oy, T oz,
-                                            const double* __restrict__ F, T out[3]) {
+                                            const FT* __restrict__ F, T out[3]) {
     int X[2], Y[2], Z[2];
     T wx[2], wy[2], wz[2];
     node_w(ox, i, g.nx, X, wx); node_w(oy, j, g.ny, Y, wy); node_w(oz, k, g.nz, Z, wz);
@@ -27,9 +27,9 @@ __device__ __forceinline__ void gather_node(const GridP& g, int i, int j, int k,
             }
 }
 
-template <typename T>
+template <typename T, typename FT = double>
 __device__ __forceinline__ void gather_cell(const GridP& g, int i, int j, int k, T ox, T oy, T oz,
-                                            const double* __restrict__ F, T out[3]) {
+                                            const FT* __restrict__ F, T out[3]) {
     int X[2], Y[2], Z[2];
     T wx[2], wy[2], wz[2];
     cell_w(ox, i, g.nx, X, wx); cell_w(oy, j, g.ny, Y, wy); cell_w(oz, k, g.nz, Z, wz);

@@ -25,6 +25,7 @@ namespace pic {
 constexpr int kImpThreads = 256;
 constexpr int kXposeMin = 4;   // fewest lanes of one cell that take the transpose-reduction
 
+
 // Symmetric pressure components kept in shared memory, q = 0..5:
 // (a, b) = (0,0) (0,1) (0,2) (1,1) (1,2) (2,2).
 __host__ __device__ constexpr int sym_a(int q) { return q < 3 ? 0 : (q < 5 ? 1 : 2); }
@@ -104,10 +105,12 @@ __device__ __noinline__ void imp_deposit_global(const GridP& g, int i, int j, in
             }
 }
 
+// E and B come in the particle precision (FP32 copies for the FP32 path:
+// no FP64 conversion per gather).
 template <typename T, typename A>
 __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP g, TileGeom t, ImpBlock bk,
-                                                                       ImpSpecies<T> S, const double* __restrict__ E,
-                                                                       const double* __restrict__ B,
+                                                                       ImpSpecies<T> S, const T* __restrict__ E,
+                                                                       const T* __restrict__ B,
                                                                        double* __restrict__ J, double* __restrict__ mu,
                                                                        double* __restrict__ rho,
                                                                        double* __restrict__ Pi) {
@@ -157,8 +160,8 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
                         T gam, v[3];
                         gamma_vel<T>(mom, T(ms), gam, v);
                         T e[3], bf[3];
-                        gather_node<T>(g, i, j, k, ox, oy, oz, E, e);
-                        gather_cell<T>(g, i, j, k, ox, oy, oz, B, bf);
+                        gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
+                        gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, bf);
                         T al[9];
                         alpha_tensor<T>(beta, v, gam, e, bf, al);
                         const T vg[3] = {v[0] * gam, v[1] * gam, v[2] * gam};
@@ -232,6 +235,7 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
                                               sum);
                                 }
                             }
+
                         } else if (me) {
 #pragma unroll
                             for (int c = 0; c < 8; ++c) {
@@ -283,6 +287,200 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
             }
         }
         __syncthreads();
+    }
+}
+
+}  // namespace pic
+
+namespace pic {
+
+constexpr int kMoverHalo = 2;   // cells of field halo staged around a mover tile
+
+// Field blocks of the tiled mover: nodes (E^n, E^theta) over tile + 2H + 1,
+// cells (B^n) over tile + 2H + 2 on active axes.
+struct MoverBlock {
+    int nbx, nby, nbz, NB;
+    int cbx, cby, cbz, CB;
+};
+
+// Trilinear gather from a staged block: base = block index of the lower
+// corner, (sx, sy, sz) strides (0 on a single-cell axis), weights of the
+// upper corners.
+template <typename T>
+__device__ __forceinline__ T tri_block(const T* __restrict__ F, int base, int sx, int sy, int sz, T wx, T wy, T wz) {
+    const T ux = T(1) - wx, uy = T(1) - wy, uz = T(1) - wz;
+    return uz * (uy * (ux * F[base] + wx * F[base + sx]) + wy * (ux * F[base + sy] + wx * F[base + sy + sx])) +
+           wz * (uy * (ux * F[base + sz] + wx * F[base + sz + sx]) +
+                 wy * (ux * F[base + sz + sy] + wx * F[base + sz + sy + sx]));
+}
+
+// moveParticle (PIC++/mover.cpp:194-491), periodic box, one CTA per tile of
+// tile-ordered particles: E^n and E^{n+theta} (nodes) and B^n (cells) of
+// the tile and a two-cell halo are staged in shared memory in the particle
+// precision, so the predictor and the up to three Picard gathers read
+// shared memory; a particle whose stencil leaves the block gathers from the
+// FP64 grids.  Same arithmetic as k_implicit_push.
+template <typename T>
+__global__ void __launch_bounds__(256) k_implicit_push_tile(GridP g, TileGeom t, MoverBlock mb, ImpSpecies<T> S,
+                                                            const double* __restrict__ E, const double* __restrict__ B,
+                                                            const double* __restrict__ Et) {
+    extern __shared__ __align__(16) unsigned char mv_smem[];
+    T* sE = reinterpret_cast<T*>(mv_smem);   // [3][NB]
+    T* sEt = sE + 3 * mb.NB;                 // [3][NB]
+    T* sB = sEt + 3 * mb.NB;                 // [3][CB]
+    const int ntiles = t.ntx * t.nty * t.ntz;
+    const int T3 = t.tx * t.ty * t.tz;
+    const bool ax = g.nx > 1, ay = g.y3, az = g.z3;
+    const int hx = ax ? kMoverHalo : 0, hy = ay ? kMoverHalo : 0, hz = az ? kMoverHalo : 0;
+    const int nsx = ax ? 1 : 0, nsy = ay ? mb.nbx : 0, nsz = az ? mb.nbx * mb.nby : 0;
+    const int csx = ax ? 1 : 0, csy = ay ? mb.cbx : 0, csz = az ? mb.cbx * mb.cby : 0;
+    const T dt = T(g.dt), eta = T(g.eta), edt = T(g.eta * g.dt);
+    const T id[3] = {T(1.0 / g.dx), T(1.0 / g.dy), T(1.0 / g.dz)};
+    const int nn[3] = {g.nx, g.ny, g.nz};
+    const T dxT = T(g.dx);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
+        const int x0 = ti * t.tx, y0 = tj * t.ty, z0 = tk * t.tz;
+        __syncthreads();   // previous tile's particles are done with the blocks
+        for (int e = threadIdx.x; e < mb.NB; e += blockDim.x) {
+            const int lx = e % mb.nbx, ly = (e / mb.nbx) % mb.nby, lz = e / (mb.nbx * mb.nby);
+            const long long gid = linw(g, x0 - hx + lx, y0 - hy + ly, z0 - hz + lz);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sE[c * mb.NB + e] = T(E[c * g.N + gid]);
+                sEt[c * mb.NB + e] = T(Et[c * g.N + gid]);
+            }
+        }
+        for (int e = threadIdx.x; e < mb.CB; e += blockDim.x) {
+            const int lx = e % mb.cbx, ly = (e / mb.cbx) % mb.cby, lz = e / (mb.cbx * mb.cby);
+            const long long gid = linw(g, x0 - hx - (ax ? 1 : 0) + lx, y0 - hy - (ay ? 1 : 0) + ly,
+                                       z0 - hz - (az ? 1 : 0) + lz);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sB[c * mb.CB + e] = T(B[c * g.N + gid]);
+        }
+        __syncthreads();
+        for (int s = 0; s < S.ns; ++s) {
+            const PartView<T> p = S.p[s];
+            const double qs = S.q[s], ms = S.m[s];
+            const T beta = T(0.5 * qs * g.dt / ms);
+            const T qdt = T(qs * g.dt);
+            const T mm = T(ms);
+            const int b0 = S.off[s][tile * T3], b1 = S.off[s][(tile + 1) * T3];
+            for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x) {
+                int ci[3];
+                decode(g, p.cell[n], ci[0], ci[1], ci[2]);
+                // gathers at (cell c, offset u): shared block when the whole
+                // stencil is staged, else the FP64 grids
+                auto gat = [&](const int c[3], const T u[3], const T* __restrict__ blkN, const double* __restrict__ glbN,
+                               bool node, T out[3]) {
+                    int l[3];
+                    const bool inb = local_axis(c[0], x0, t.tx, hx, g.nx, l[0]) &&
+                                     local_axis(c[1], y0, t.ty, hy, g.ny, l[1]) &&
+                                     local_axis(c[2], z0, t.tz, hz, g.nz, l[2]);
+                    if (!inb) {
+                        if (node) gather_node<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], glbN, out);
+                        else gather_cell<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], glbN, out);
+                        return;
+                    }
+                    T w[3];
+                    int base;
+                    if (node) {
+                        T wn[2];
+                        int dummy[2];
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            node_w<T>(u[a], c[a], nn[a], dummy, wn);
+                            w[a] = wn[1];
+                        }
+                        base = (l[2] + hz) * nsz + (l[1] + hy) * nsy + (l[0] + hx) * nsx;
+#pragma unroll
+                        for (int q = 0; q < 3; ++q)
+                            out[q] = tri_block<T>(blkN + q * mb.NB, base, nsx, nsy, nsz, w[0], w[1], w[2]);
+                    } else {
+                        T wc[2];
+                        int idx[2];
+                        int lo[3];
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            cell_w<T>(u[a], c[a], nn[a], idx, wc);
+                            w[a] = wc[1];
+                            // lower cell of the pair: c - 1 below the centre, c above
+                            lo[a] = (nn[a] > 1 && u[a] < T(0.5)) ? l[a] - 1 : l[a];
+                        }
+                        const int ex = ax ? 1 : 0, ey = ay ? 1 : 0, ez = az ? 1 : 0;
+                        base = (lo[2] + hz + ez) * csz + (lo[1] + hy + ey) * csy + (lo[0] + hx + ex) * csx;
+#pragma unroll
+                        for (int q = 0; q < 3; ++q)
+                            out[q] = tri_block<T>(blkN + q * mb.CB, base, csx, csy, csz, w[0], w[1], w[2]);
+                    }
+                };
+                T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
+                T mom0[3] = {p.px[n], p.py[n], p.pz[n]};
+                T gam, v[3];
+                gamma_vel<T>(mom0, mm, gam, v);
+                T e[3], b[3], al[9];
+                gat(ci, u0, sE, E, true, e);
+                gat(ci, u0, sB, B, false, b);
+                alpha_tensor<T>(beta, v, gam, e, b, al);
+                gat(ci, u0, sEt, Et, true, e);
+                T vxb[3] = {v[1] * b[2] - v[2] * b[1], -v[0] * b[2] + v[2] * b[0], v[0] * b[1] - v[1] * b[0]};
+                T pnew[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + vxb[d]) * qdt;
+                T vnew[3];
+                evaluate_velocity<T>(pnew, mm, vnew);
+                T mv[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
+                T vh[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                    vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
+                const T momNorm = dev_sqrt(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
+                T err = dev_sqrt((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
+                                 (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
+                T cerr = dxT;
+                T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
+                T prevDisp[3];
+                int it = 0;
+                while (err > T(1e-14) * momNorm && cerr > T(1e-8) * dxT && it < 3) {
+                    ++it;
+                    const T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) prevDisp[d] = newDisp[d];
+                    T re[3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) re[a] = al[3 * a] * e[0] + al[3 * a + 1] * e[1] + al[3 * a + 2] * e[2];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
+                    int tc[3];
+                    T tu[3];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        tc[d] = ci[d]; tu[d] = u0[d];
+                        advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
+                    }
+                    gat(tc, tu, sEt, Et, true, e);
+                    gat(tc, tu, sB, B, false, b);
+                    const T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
+                    err = dev_sqrt((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) +
+                                   (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
+                                   (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
+                    cerr = dev_sqrt((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
+                                    (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
+                                    (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
+                }
+                p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+                p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+                p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+            }
+        }
     }
 }
 

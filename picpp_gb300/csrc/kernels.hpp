@@ -51,8 +51,12 @@ struct PK {
     static ImpBlock implicit_block(const GridP& g, const TileGeom& t, int h);
     static size_t implicit_tile_smem(const ImpBlock& bk);
     static void implicit_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const ImpBlock& bk,
-                                       const ImpSpecies<T>& S, const double* E, const double* B, double* J,
+                                       const ImpSpecies<T>& S, const T* E, const T* B, double* J,
                                        double* mu, double* rho, double* Pi);
+    // tiled mover (implicit_tile.cuh): fields staged per tile; needs
+    // tile-major sorted particles; false if the blocks do not fit
+    static bool implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const ImpSpecies<T>& S,
+                                    const double* E, const double* B, const double* Et);
     static void implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const double* E,
                               const double* B, const double* Et);
     static void gather_payload(cudaStream_t s, const int* perm, long long n, PartView<T> src, PartView<T> dst);
@@ -99,6 +103,9 @@ void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, co
                             double* out);
 void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,
                          double* En, double* Bn, int doE, int doB);
+void launch_smooth(cudaStream_t s, const GridP& g, const double* src, double* dst, int ncomp, double sp);
+void launch_smooth_rho_ext(cudaStream_t s, const GridP& g, const double* src, double* dst, int ex, int ey, int ez,
+                           double sp);
 void launch_density_finish(cudaStream_t s, long long N, double q, const double* conc, const double* energy,
                            double* mom_to_vel, double* rho);
 // Krylov

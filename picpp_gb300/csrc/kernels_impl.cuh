@@ -208,7 +208,7 @@ size_t PK<T>::implicit_tile_smem(const ImpBlock& bk) {
 
 template <typename T>
 void PK<T>::implicit_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const ImpBlock& bk,
-                                   const ImpSpecies<T>& S, const double* E, const double* B, double* J, double* mu,
+                                   const ImpSpecies<T>& S, const T* E, const T* B, double* J, double* mu,
                                    double* rho, double* Pi) {
     static bool attr_set = false;
     if (!attr_set) {
@@ -220,6 +220,33 @@ void PK<T>::implicit_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeo
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int grid = ntiles < kNumSM * (per_sm > 0 ? per_sm : 1) ? ntiles : kNumSM * (per_sm > 0 ? per_sm : 1);
     k_implicit_deposit_tile<T, T><<<grid, kImpThreads, smem, s>>>(g, t, bk, S, E, B, J, mu, rho, Pi);
+}
+
+template <typename T>
+bool PK<T>::implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const ImpSpecies<T>& S,
+                                const double* E, const double* B, const double* Et) {
+    MoverBlock mb{};
+    const int H = kMoverHalo;
+    mb.nbx = g.nx > 1 ? t.tx + 2 * H + 1 : 1;
+    mb.nby = g.y3 ? t.ty + 2 * H + 1 : 1;
+    mb.nbz = g.z3 ? t.tz + 2 * H + 1 : 1;
+    mb.cbx = g.nx > 1 ? t.tx + 2 * H + 2 : 1;
+    mb.cby = g.y3 ? t.ty + 2 * H + 2 : 1;
+    mb.cbz = g.z3 ? t.tz + 2 * H + 2 : 1;
+    mb.NB = mb.nbx * mb.nby * mb.nbz;
+    mb.CB = mb.cbx * mb.cby * mb.cbz;
+    const size_t smem = (6 * (size_t)mb.NB + 3 * (size_t)mb.CB) * sizeof(T);
+    if (smem > 227 * 1024) return false;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_implicit_push_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    const int per_sm = (int)((228 * 1024) / (smem + 1024));
+    const int ntiles = t.ntx * t.nty * t.ntz;
+    const int cap = kNumSM * (per_sm > 0 ? per_sm : 1);
+    k_implicit_push_tile<T><<<ntiles < cap ? ntiles : cap, 256, smem, s>>>(g, t, mb, S, E, B, Et);
+    return true;
 }
 
 template <typename T>

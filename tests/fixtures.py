@@ -32,6 +32,12 @@ def load(name):
                 E=z["E"].copy(), B=z["B"].copy(), extra=extra)
 
 
+def smoothing_of(f):
+    """(smoothingCount, smoothingParameter) a golden case was run with."""
+    sm = f["extra"].get("smoothing")
+    return (int(sm[0]), float(sm[1])) if sm is not None else (0, 0.5)
+
+
 def copy_species(species):
     return [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()} for s in species]
 

@@ -47,9 +47,12 @@ def _save(name, solver, st, steps, out_sp, E, B, extra):
     print("wrote", name)
 
 
-def buneman(name, nx, ny, nz, ppc, steps, seed):
+def buneman(name, nx, ny, nz, ppc, steps, seed, smoothing=(0, 0.5)):
     st = _noise(I.buneman_plasma(nx, ny, nz, ppc=ppc, seed=seed), 0.05, seed + 100)
-    out_sp, E, B, extra = O.run_reference(0, st.box, st.species, st.E, st.B, steps)
+    out_sp, E, B, extra = O.run_reference(0, st.box, st.species, st.E, st.B, steps, smoothing_count=smoothing[0],
+                                          smoothing_parameter=smoothing[1])
+    if smoothing[0]:
+        extra["smoothing"] = np.array(smoothing, dtype=np.float64)
     _save(name, 0, st, steps, out_sp, E, B, extra)
 
 
@@ -82,6 +85,8 @@ def main():
     implicit("implicit_6x5x7_1step", 6, 5, 7, 2, 1, 21)
     implicit("implicit_8x8x8_3steps", 8, 8, 8, 2, 3, 22)
     implicit("implicit_gamma10_6x6x6_2steps", 6, 6, 6, 2, 2, 23, beam_gamma=10.0, dt=0.5)
+    buneman("buneman_smooth_8x6x5_2steps", 8, 6, 5, 3, 2, 14, smoothing=(2, 0.4))
+    buneman("buneman_smooth_2d_12x8x1_2steps", 12, 8, 1, 3, 2, 15, smoothing=(1, 0.5))
     density("density_8x6x5", 8, 6, 5, 3, 31)
     density("density_2d_8x8x1", 8, 8, 1, 4, 32)
 

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from fixtures import copy_species, golden_names, load, periodic_dist, rel_err
+from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of
 from picpp_gb300 import initstate as I
 
 pytestmark = pytest.mark.gpu
@@ -166,7 +166,9 @@ def test_buneman_golden_vectors(pg, name):
     """The GPU FP64 path against outputs of the reference itself."""
     f = load(name)
     st = f["state"]
-    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=1, tile=(0, 0, 0))
+    sc, spar = smoothing_of(f)
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=1, tile=(0, 0, 0), smoothing_count=sc,
+                           smoothing_parameter=spar)
     sim.upload_state(st)
     sim.buneman_step(f["steps"])
     E, B, J = sim.download_fields()
@@ -483,3 +485,114 @@ def test_density_parameters_after_explicit_steps_match_oracle(pg):
         assert rel_err(e, en[s]) < 1e-11
         assert rel_err(v, vel[s]) < 1e-11
     assert rel_err(r, rho) < 1e-11
+
+
+@pytest.mark.parametrize("solver,real,every", [(0, 1, 1), (0, 0, 1), (0, 1, 3), (1, 1, 2), (1, 0, 2)])
+def test_checkpoint_resumes_the_run(pg, tmp_path, solver, real, every):
+    """Save after some steps and load into a fresh context: the loaded state
+    is the saved one bit for bit (particles in their device order, fields).
+    Both contexts then continue; the deposits sum in shared-memory and FP64
+    atomics whose order varies from run to run, so the continued runs agree
+    to rounding."""
+    if solver == 0:
+        st = noisy(I.buneman_plasma(8, 8, 8, ppc=3, seed=41))
+        kw = dict(sort_every=every, tile=(4, 4, 4))
+        step = lambda s, n: s.buneman_step(n)  # noqa: E731
+    else:
+        st = implicit_state(ppc=2)
+        kw = dict(sort_every=every, tile=(4, 3, 5), pressure_compat=0)
+
+        def step(s, n):
+            for _ in range(n):
+                s.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    a = pg.GpuSimulation(st.box, solver, particle_real=real, **kw)
+    a.upload_state(st)
+    step(a, 2)
+    path = str(tmp_path / "state.ckpt")
+    a.save_checkpoint(path)
+    b = pg.GpuSimulation(st.box, solver, particle_real=real, **kw)
+    b.load_checkpoint(path)
+    for x, y in zip(a.download_fields(), b.download_fields()):
+        assert np.array_equal(x, y)
+    for s in range(2):
+        pa, pb = a.download_particles(s), b.download_particles(s)
+        for k in pa:
+            assert np.array_equal(pa[k], pb[k]), k
+    step(a, 3)
+    step(b, 3)
+    tol = 1e-12 if real else 1e-5
+    for x, y in zip(a.download_fields()[:2], b.download_fields()[:2]):
+        assert rel_err(x, y) < tol
+    for s in range(2):
+        pa, pb = by_id(a.download_particles(s)), by_id(b.download_particles(s))
+        for k in ("px", "py", "pz"):
+            assert rel_err(pa[k], pb[k]) < tol, k
+
+
+def test_checkpoint_rejects_another_configuration(pg, tmp_path):
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=2, seed=42))
+    a = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1)
+    a.upload_state(st)
+    path = str(tmp_path / "s.ckpt")
+    a.save_checkpoint(path)
+    other = I.Box(8, 8, 4, st.box.dx, st.box.dy, st.box.dz, st.box.dt)
+    b = pg.GpuSimulation(other, pg.BUNEMAN, particle_real=1, tile=(0, 0, 0))
+    with pytest.raises(pg.PicError):
+        b.load_checkpoint(path)
+    with pytest.raises(pg.PicError):
+        b.load_checkpoint(str(tmp_path / "missing.ckpt"))
+
+
+@pytest.mark.parametrize("real", [1, 0])
+def test_smoothing_phase_calls_and_fused_step_match_oracle(pg, real):
+    """Current smoothing after the deposit (simulation.cpp:186-188), through
+    the phase calls (per-particle kernels) and the fused tiled step."""
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=3, seed=43))
+    g = O.make_grid(st.box, smoothing_count=2, smoothing_parameter=0.3)
+    sp = copy_species(st.species)
+    Eo, Bo = st.E.copy(), st.B.copy()
+    for _ in range(2):
+        Jo = O.buneman_step(g, sp, Eo, Bo)
+    tol = TOL64 if real else 1e-4
+    for fused in (False, True):
+        sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real, sort_every=1 if fused else 0, tile=(4, 4, 4),
+                               smoothing_count=2, smoothing_parameter=0.3)
+        sim.upload_state(st)
+        if fused:
+            sim.buneman_step(2)
+        else:
+            for _ in range(2):
+                sim.tristanEvaluateBhalfStep()
+                sim.moveParticles()
+                sim.tristanEvaluateBhalfStep()
+                sim.tristanUpdateFlux()
+                sim.tristanEvaluateE()
+        E, B, J = sim.download_fields()
+        assert rel_err(E, Eo) < tol
+        assert rel_err(J, Jo.reshape(J.shape)) < tol
+
+
+@pytest.mark.parametrize("real", [1, 0])
+def test_implicit_smoothing_matches_oracle(pg, real):
+    st = implicit_state(ppc=3)
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1, tile=(4, 3, 5),
+                           smoothing_count=1, smoothing_parameter=0.5)
+    sim.upload_state(st)
+    for _ in range(2):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    E, B, _ = sim.download_fields()
+    g = O.make_grid(st.box, pressure_compat=0, smoothing_count=1, smoothing_parameter=0.5)
+    sp = copy_species(st.species)
+    Eo, Bo = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(2):
+        O.implicit_step(g, sp, Eo, Bo)
+    tol = 1e-9 if real else 1e-4
+    assert rel_err(E.reshape(-1), Eo) < tol
+    assert rel_err(B.reshape(-1), Bo) < tol
+
+
+def test_implicit_smoothing_needs_the_periodic_pressure_placement(pg):
+    st = implicit_state(ppc=1)
+    pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, pressure_compat=0, smoothing_count=1, tile=(0, 0, 0))
+    with pytest.raises(pg.PicError):
+        pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, pressure_compat=1, smoothing_count=1, tile=(0, 0, 0))

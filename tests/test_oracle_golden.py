@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from fixtures import copy_species, golden_names, load, periodic_dist, rel_err
+from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of
 from picpp_gb300 import initstate as I
 
 # The oracle keeps cell + offset where the reference keeps absolute FP64
@@ -16,7 +16,8 @@ TOL = 1e-11
 def test_buneman_matches_reference(name):
     f = load(name)
     st = f["state"]
-    g = O.make_grid(st.box)
+    sc, spar = smoothing_of(f)
+    g = O.make_grid(st.box, smoothing_count=sc, smoothing_parameter=spar)
     sp = copy_species(st.species)
     E, B = st.E.copy(), st.B.copy()
     for _ in range(f["steps"]):

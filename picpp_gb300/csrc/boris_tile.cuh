@@ -89,8 +89,11 @@ __device__ __forceinline__ bool run_sum(int key, TP a[12]) {
     if (H != 0xffffffffu) {
         const unsigned after = H & ~((2u << lane) - 1u);
         const int seg_end = after ? (__ffs(after) - 2) : 31;
+        // only as many doubling rounds as the longest run needs
+        const unsigned run = __reduce_max_sync(0xffffffffu, head ? (unsigned)(seg_end - lane + 1) : 1u);
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
+            if ((unsigned)d >= run) break;
             const bool take = lane + d <= seg_end;
 #pragma unroll
             for (int q = 0; q < 12; ++q) {

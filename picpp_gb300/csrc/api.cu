@@ -70,6 +70,7 @@ struct pic_ctx {
     bool mu_valid = false;   // ctx->mu holds an operator (moments or an uploaded mu)
     Net* net = nullptr;      // learned preconditioner, created by pic_nn_init / pic_nn_set_params
     double* smooth_tmp = nullptr;   // scratch of the smoothing passes (max(9N, rho-hat ext))
+    bool fresh_sort = false;        // particles sorted and not moved since
     float* fields32 = nullptr;      // FP32 copies of E^n, B^n (6N) for the FP32 deposit
     // updateDensityParameters grids: per species conc, energy, velocity (5N), charge density (N)
     double* dens = nullptr;
@@ -198,6 +199,7 @@ pic_status sort_all(pic_ctx* ctx) {
         pic_status st = ctx->preal ? sort_species<double>(ctx, sp) : sort_species<float>(ctx, sp);
         if (st != PIC_OK) return st;
     }
+    ctx->fresh_sort = true;
     return PIC_OK;
 }
 
@@ -323,8 +325,14 @@ pic_status implicit_moments(pic_ctx* ctx) {
     // tiled shared-memory deposit when the particles are in tile order and
     // the pressure tensor goes to the particle's cells; halo of one cell when
     // the block fits in shared memory
-    ImpBlock bk = PK<T>::implicit_block(g, ctx->tg, 1);
-    if (PK<T>::implicit_tile_smem(bk) > 227 * 1024) bk = PK<T>::implicit_block(g, ctx->tg, 0);
+    // right after a sort every particle is in its tile: no halo, and E, B
+    // staged next to the accumulators; otherwise a one-cell halo for drift
+    ImpBlock bk = PK<T>::implicit_block(g, ctx->tg, 0);
+    bk.stage = 1;
+    if (!ctx->fresh_sort || PK<T>::implicit_tile_smem(bk) > 227 * 1024) {
+        bk = PK<T>::implicit_block(g, ctx->tg, 1);
+        if (PK<T>::implicit_tile_smem(bk) > 227 * 1024) bk = PK<T>::implicit_block(g, ctx->tg, 0);
+    }
     if (!compat && all_sorted(ctx) && PK<T>::implicit_tile_smem(bk) <= 227 * 1024) {
         ImpSpecies<T> S{};
         S.ns = (int)ctx->sp.size();
@@ -386,6 +394,7 @@ pic_status implicit_move(pic_ctx* ctx) {
         for (auto& sp : ctx->sp)
             PK<T>::implicit_push(ctx->s, ctx->g, view<T>(sp), sp.q, sp.m, ctx->Ei, ctx->Bi, ctx->Et);
     CKL(ctx, "implicit mover");
+    ctx->fresh_sort = false;
     // the tile order stays valid: the tiled deposit and mover check every
     // particle's cell and take their halo or global path for drifted ones
     return PIC_OK;
@@ -1136,6 +1145,7 @@ pic_status pic_load_checkpoint(pic_ctx* ctx, const char* path) {
     }
     ctx->step = h.step;
     ctx->moments_ready = ctx->efield_ready = ctx->mu_valid = false;
+    ctx->fresh_sort = false;
     return sync(ctx, "load checkpoint");
 }
 

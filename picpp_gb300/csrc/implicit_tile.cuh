@@ -70,6 +70,17 @@ __device__ __forceinline__ bool local_axis(int c, int x0, int t, int h, int n, i
     return false;
 }
 
+// Trilinear gather from a staged block: base = block index of the lower
+// corner, (sx, sy, sz) strides (0 on a single-cell axis), weights of the
+// upper corners.
+template <typename T>
+__device__ __forceinline__ T tri_block(const T* __restrict__ F, int base, int sx, int sy, int sz, T wx, T wy, T wz) {
+    const T ux = T(1) - wx, uy = T(1) - wy, uz = T(1) - wz;
+    return uz * (uy * (ux * F[base] + wx * F[base + sx]) + wy * (ux * F[base + sy] + wx * F[base + sy + sx])) +
+           wz * (uy * (ux * F[base + sz] + wx * F[base + sz + sx]) +
+                 wy * (ux * F[base + sz + sy] + wx * F[base + sz + sy + sx]));
+}
+
 // All 8 node and 8 cell contributions of one particle to the FP64 grids
 // (particles outside the tile's block; rare).
 template <typename T>
@@ -117,6 +128,8 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
     extern __shared__ __align__(16) unsigned char imp_smem[];
     A* sN = reinterpret_cast<A*>(imp_smem);   // [12][NB]
     A* sC = sN + 12 * bk.NB;                  // [7][CB]
+    T* sE = reinterpret_cast<T*>(sC + 7 * bk.CB);   // [3][NB] when staged
+    T* sB = sE + 3 * bk.NB;                          // [3][CB] when staged
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int T3 = t.tx * t.ty * t.tz;
     const int ntiles = t.ntx * t.nty * t.ntz;
@@ -134,6 +147,20 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
         const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
         const int x0 = ti * t.tx, y0 = tj * t.ty, z0 = tk * t.tz;
         for (int e = threadIdx.x; e < tot; e += blockDim.x) sN[e] = A(0);
+        if (bk.stage) {   // with h = 0 the blocks cover exactly the stencils of the tile's own cells
+            for (int e = threadIdx.x; e < bk.NB; e += blockDim.x) {
+                const int lx = e % bk.nbx, ly = (e / bk.nbx) % bk.nby, lz = e / (bk.nbx * bk.nby);
+                const long long id = linw(g, x0 + lx, y0 + ly, z0 + lz);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) sE[c * bk.NB + e] = E[c * g.N + id];
+            }
+            for (int e = threadIdx.x; e < bk.CB; e += blockDim.x) {
+                const int lx = e % bk.cbx, ly = (e / bk.cbx) % bk.cby, lz = e / (bk.cbx * bk.cby);
+                const long long id = linw(g, x0 - (ax ? 1 : 0) + lx, y0 - (ay ? 1 : 0) + ly, z0 - (az ? 1 : 0) + lz);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) sB[c * bk.CB + e] = B[c * g.N + id];
+            }
+        }
         __syncthreads();
         for (int s = 0; s < S.ns; ++s) {
             const PartView<T> p = S.p[s];
@@ -159,9 +186,33 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
                         T mom[3] = {p.px[n], p.py[n], p.pz[n]};
                         T gam, v[3];
                         gamma_vel<T>(mom, T(ms), gam, v);
+                        T nwx[2], nwy[2], nwz[2], cwx[3], cwy[3], cwz[3];
+                        axis_weights<T>(ox, ax, nwx, cwx);
+                        axis_weights<T>(oy, ay, nwy, cwy);
+                        axis_weights<T>(oz, az, nwz, cwz);
+                        int li = 0, lj = 0, lk = 0;
+                        inb = local_axis(i, x0, t.tx, hx, g.nx, li) && local_axis(j, y0, t.ty, hy, g.ny, lj) &&
+                              local_axis(k, z0, t.tz, hz, g.nz, lk);
+                        if (inb) {
+                            nb = (lk + hz) * nsz + (lj + hy) * nsy + (li + hx);
+                            cb = (lk + hz) * csz + (lj + hy) * csy + (li + hx);
+                        }
                         T e[3], bf[3];
-                        gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
-                        gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, bf);
+                        if (inb && bk.stage) {
+                            // node pair (c, c+1); cell pair (c-1, c) below the centre, (c, c+1) above
+                            const int cbase = cb + (ox < T(0.5) ? 0 : oxc) + (oy < T(0.5) ? 0 : oyc) + (oz < T(0.5) ? 0 : ozc);
+                            const T ux = ox < T(0.5) ? cwx[1] : cwx[2];
+                            const T uy = oy < T(0.5) ? cwy[1] : cwy[2];
+                            const T uz = oz < T(0.5) ? cwz[1] : cwz[2];
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) {
+                                e[c] = tri_block<T>(sE + c * bk.NB, nb, oxn, oyn, ozn, nwx[1], nwy[1], nwz[1]);
+                                bf[c] = tri_block<T>(sB + c * bk.CB, cbase, oxc, oyc, ozc, ux, uy, uz);
+                            }
+                        } else {
+                            gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
+                            gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, bf);
+                        }
                         T al[9];
                         alpha_tensor<T>(beta, v, gam, e, bf, al);
                         const T vg[3] = {v[0] * gam, v[1] * gam, v[2] * gam};
@@ -176,21 +227,11 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
                         QC[0] = A(cq);
 #pragma unroll
                         for (int q = 0; q < 6; ++q) QC[1 + q] = A(cq) * (rv[sym_a(q)] * rv[sym_b(q)]);
-                        T nwx[2], nwy[2], nwz[2], cwx[3], cwy[3], cwz[3];
-                        axis_weights<T>(ox, ax, nwx, cwx);
-                        axis_weights<T>(oy, ay, nwy, cwy);
-                        axis_weights<T>(oz, az, nwz, cwz);
 #pragma unroll
                         for (int c = 0; c < 8; ++c) wn[c] = A(nwx[c & 1] * nwy[(c >> 1) & 1] * nwz[c >> 2]);
 #pragma unroll
                         for (int q = 0; q < 27; ++q) wc[q] = A(cwx[q % 3] * cwy[(q / 3) % 3] * cwz[q / 9]);
-                        int li = 0, lj = 0, lk = 0;
-                        inb = local_axis(i, x0, t.tx, hx, g.nx, li) && local_axis(j, y0, t.ty, hy, g.ny, lj) &&
-                              local_axis(k, z0, t.tz, hz, g.nz, lk);
-                        if (inb) {
-                            nb = (lk + hz) * nsz + (lj + hy) * nsy + (li + hx);
-                            cb = (lk + hz) * csz + (lj + hy) * csy + (li + hx);
-                        } else {
+                        if (!inb) {
                             double qn[12], qc[7];
 #pragma unroll
                             for (int d = 0; d < 12; ++d) qn[d] = double(QN[d]);
@@ -302,17 +343,6 @@ struct MoverBlock {
     int nbx, nby, nbz, NB;
     int cbx, cby, cbz, CB;
 };
-
-// Trilinear gather from a staged block: base = block index of the lower
-// corner, (sx, sy, sz) strides (0 on a single-cell axis), weights of the
-// upper corners.
-template <typename T>
-__device__ __forceinline__ T tri_block(const T* __restrict__ F, int base, int sx, int sy, int sz, T wx, T wy, T wz) {
-    const T ux = T(1) - wx, uy = T(1) - wy, uz = T(1) - wz;
-    return uz * (uy * (ux * F[base] + wx * F[base + sx]) + wy * (ux * F[base + sy] + wx * F[base + sy + sx])) +
-           wz * (uy * (ux * F[base + sz] + wx * F[base + sz + sx]) +
-                 wy * (ux * F[base + sz + sy] + wx * F[base + sz + sy + sx]));
-}
 
 // moveParticle (PIC++/mover.cpp:194-491), periodic box, one CTA per tile of
 // tile-ordered particles: E^n and E^{n+theta} (nodes) and B^n (cells) of

@@ -203,7 +203,7 @@ ImpBlock PK<T>::implicit_block(const GridP& g, const TileGeom& t, int h) {
 
 template <typename T>
 size_t PK<T>::implicit_tile_smem(const ImpBlock& bk) {
-    return (12 * (size_t)bk.NB + 7 * (size_t)bk.CB) * sizeof(T);
+    return (12 * (size_t)bk.NB + 7 * (size_t)bk.CB + (bk.stage ? 3 * ((size_t)bk.NB + bk.CB) : 0)) * sizeof(T);
 }
 
 template <typename T>

@@ -53,6 +53,7 @@ struct ImpBlock {
     int h;
     int nbx, nby, nbz, NB;
     int cbx, cby, cbz, CB;
+    int stage;   // 1: E (node block) and B (cell block) staged in shared memory too (h = 0 only)
 };
 
 // Coefficients of the matrix-free Maxwell operator (implicit_grid.cuh).

@@ -12,10 +12,15 @@
 //      of a particle is two segments, each with 12 terms at fixed positions
 //      relative to one cell: the segment from the old position to the relay
 //      point (in the old cell) and the one from the relay point to the new
-//      position (in the new cell).  Lanes of a warp holding the same cell
-//      (particles are sorted by cell) sum each segment's 12 values with a
-//      segmented shuffle reduction, and the first lane of each run adds them
-//      to a shared-memory current block (tile plus two cells of halo);
+//      position (in the new cell).  Lanes holding the same cell (particles
+//      are sorted by cell) sum each segment's 12 values with a segmented
+//      shuffle reduction, and the first lane of each run adds the totals to a
+//      shared-memory current block (tile plus two cells of halo).  FP32
+//      particles: the block is exact 64-bit fixed point in two 32-bit words
+//      per entry, added with native 32-bit integer shared atomics (FP32 shared
+//      atomics are compare-and-swap loops that collapse under address
+//      conflicts); the block sums are exact and order-independent.  FP64
+//      particles: FP64 shared atomics;
 //   3. writes the block, unreduced, to a per-tile partial buffer.
 // k_assemble_j then sums the partials of every cell in a fixed order into
 // the FP64 current grid: no global floating-point atomics on the fast path.
@@ -29,7 +34,7 @@ namespace pic {
 
 constexpr int kTileThreads = 256;
 #ifndef PIC_TILE_MIN_BLOCKS
-#define PIC_TILE_MIN_BLOCKS 3   // CTAs per SM the register budget is sized for
+#define PIC_TILE_MIN_BLOCKS 2   // CTAs per SM the register budget is sized for
 #endif
 
 template <typename TP>
@@ -126,12 +131,43 @@ __device__ __forceinline__ void add_slots(TP* __restrict__ sJ, long long JC, int
     if (ey) atomicAdd(&jz[c + 1 + X0], a[11]);
 }
 
+// Fixed-point current block of the FP32 path: a run total a becomes the
+// integer x = rint(a * sc) (sc a power of two with |x| < 2^40 per term; the
+// block holds each entry as a 64-bit two's-complement sum in a low
+// (unsigned) and a high (signed) 32-bit word, the low word's carry added to
+// the high one.  Shared 32-bit integer atomics are native; the sums are exact
+// and independent of the order of the adds.
+__device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restrict__ hi, long long e, long long x) {
+    const unsigned xl = (unsigned)(x & 0xffffffffll);
+    const int xh = (int)(x >> 32);
+    const unsigned old = atomicAdd(&lo[e], xl);
+    const int carry = (old + xl < old) ? 1 : 0;
+    if (xh + carry != 0) atomicAdd(&hi[e], xh + carry);
+}
+
+// add_slots in fixed point.
+__device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __restrict__ hi, long long JC, int c,
+                                             int X0, int XY, int ey, int ez, const float a[12], float sc) {
+    const long long off[12] = {c, c + X0, c + XY, c + X0 + XY,
+                               JC + c, JC + c + 1, JC + c + XY, JC + c + 1 + XY,
+                               2 * JC + c, 2 * JC + c + 1, 2 * JC + c + X0, 2 * JC + c + 1 + X0};
+    const bool use[12] = {true, ey != 0, ez != 0, ey && ez, true, true, ez != 0, ez != 0, true, true, ey != 0, ey != 0};
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+        if (!use[q]) continue;
+        const long long x = __float2ll_rn(a[q] * sc);
+        if (x != 0) fx_add(lo, hi, off[q], x);
+    }
+}
+
 // CT: compile-time tile extent of a cubic 3-D tile (8), or 0 for shapes read
 // from TileShape at run time.
 template <typename TP, typename TF, int CT>
 __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
                                                                        const TF* __restrict__ E, const TF* __restrict__ B,
-                                                                       TP* __restrict__ Jpart, double* __restrict__ Jfix) {
+                                                                       TP* __restrict__ Jpart, double* __restrict__ Jfix,
+                                                                       float fx_scale) {
+    constexpr bool kFixed = sizeof(TP) == sizeof(float);   // FP32 particles: fixed-point block
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int fx = CT ? CT + 4 : s.fx, fy = CT ? CT + 4 : s.fy, fz = CT ? CT + 4 : s.fz;
     const int jx = fx, jy = fy, jz = fz;                 // both blocks: tile + 2 halo on active axes
@@ -140,7 +176,9 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
     const int F = fx * fy * fz;
     const long long JC = (long long)jx * jy * jz;
     TF* sF = reinterpret_cast<TF*>(smem_raw);   // 6 * F
-    TP* sJ = reinterpret_cast<TP*>(smem_raw + ((6 * F * sizeof(TF) + 15) & ~size_t(15)));   // 3 * JC
+    TP* sJ = reinterpret_cast<TP*>(smem_raw + ((6 * F * sizeof(TF) + 15) & ~size_t(15)));   // 3 * JC (FP64)
+    unsigned* sLo = reinterpret_cast<unsigned*>(sJ);                                        // 3 * JC (FP32)
+    int* sHi = reinterpret_cast<int*>(sLo + 3 * JC);                                        // 3 * JC (FP32)
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int T3 = tx * ty * tz;
     const long long N = g.N;
@@ -164,7 +202,11 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                 sF[(3 + comp) * F + e] = B[comp * N + gi];
             }
         }
-        for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) sJ[e] = TP(0);
+        if (kFixed) {
+            for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) { sLo[e] = 0u; sHi[e] = 0; }
+        } else {
+            for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) sJ[e] = TP(0);
+        }
         __syncthreads();
 
         for (int sp = 0; sp < S.ns; ++sp) {
@@ -276,15 +318,30 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
 #pragma unroll
                     for (int q2 = 0; q2 < 12; ++q2) aB[q2] = TP(0);
                 }
-                if (run_sum<TP>(keyB, aB) && keyB >= 0) add_slots<TP>(sJ, JC, keyB, jx, jx * jy, ey, ez, aB);
                 TP aA[12];
                 segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);   // zeros off the reduction
-                if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);
+                if constexpr (kFixed) {
+                    if (run_sum<TP>(keyB, aB) && keyB >= 0)
+                        add_slots_fx(sLo, sHi, JC, keyB, jx, jx * jy, ey, ez, (const float*)aB, fx_scale);
+                    if (run_sum<TP>(keyA, aA) && keyA >= 0)
+                        add_slots_fx(sLo, sHi, JC, keyA, jx, jx * jy, ey, ez, (const float*)aA, fx_scale);
+                } else {
+                    if (run_sum<TP>(keyB, aB) && keyB >= 0) add_slots<TP>(sJ, JC, keyB, jx, jx * jy, ey, ez, aB);
+                    if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);
+                }
             }
         }
         __syncthreads();
         TP* dst = Jpart + (long long)tile * 3 * JC;
-        for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) dst[e] = sJ[e];
+        if (kFixed) {
+            const double inv = 1.0 / (double)fx_scale;
+            for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) {
+                const long long v = (long long)sHi[e] * 4294967296ll + (long long)sLo[e];
+                dst[e] = TP((double)v * inv);
+            }
+        } else {
+            for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) dst[e] = sJ[e];
+        }
         __syncthreads();
     }
 }

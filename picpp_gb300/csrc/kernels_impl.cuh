@@ -1,6 +1,8 @@
 // kernels_impl.cuh -- launchers of the particle and Yee kernels for one
 // particle precision T; instantiated by kernels_f32.cu and kernels_f64.cu.
 #pragma once
+#include <algorithm>
+#include <cmath>
 #include "boris.cuh"
 #include "boris_tile.cuh"
 #include "diag.cuh"
@@ -151,7 +153,8 @@ void PK<T>::zigzag(cudaStream_t s, const GridP& g, PartView<T> p, double q, doub
 template <typename T>
 size_t PK<T>::tile_smem_bytes(const TileShape& sh) {
     size_t F = (size_t)sh.fx * sh.fy * sh.fz;
-    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + 3 * (size_t)sh.jcells * sizeof(T);
+    // FP32: the current block is 64-bit fixed point in two 32-bit words
+    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + 3 * (size_t)sh.jcells * 8;
 }
 
 template <typename T>
@@ -166,10 +169,20 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
     }
     const bool cube8 = t.tx == 8 && t.ty == 8 && t.tz == 8 && g.y3 && g.z3 && sh.fx == 12 && sh.fy == 12 &&
                        sh.fz == 12 && sh.jx == 12 && sh.jy == 12 && sh.jz == 12;
+    // fixed-point scale of the FP32 current block: the power of two with
+    // max_species |q w / V| * scale <= 2^35 (every zigzag term is bounded by
+    // q w / V because |v| < c = 1; a run total of up to 32 terms stays below
+    // 2^40 and 2^23 such totals per entry below 2^63)
+    double fmax = 0;
+    for (int q = 0; q < S.ns; ++q)
+        fmax = std::max(fmax, std::fabs((double)S.q[q] * (double)S.w[q] / (g.dx * g.dy * g.dz)));
+    const float fx_scale = fmax > 0 ? (float)std::ldexp(1.0, 35 - (int)std::ceil(std::log2(fmax))) : 1.0f;
     if (cube8)
-        k_push_deposit_tile<T, T, 8><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix);
+        k_push_deposit_tile<T, T, 8><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix,
+                                                                     fx_scale);
     else
-        k_push_deposit_tile<T, T, 0><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix);
+        k_push_deposit_tile<T, T, 0><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix,
+                                                                     fx_scale);
 }
 
 template <typename T>

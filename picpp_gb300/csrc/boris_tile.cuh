@@ -132,17 +132,29 @@ __device__ __forceinline__ void add_slots(TP* __restrict__ sJ, long long JC, int
 }
 
 // Fixed-point current block of the FP32 path: a run total a becomes the
-// integer x = rint(a * sc) (sc a power of two with |x| < 2^40 per term; the
-// block holds each entry as a 64-bit two's-complement sum in a low
-// (unsigned) and a high (signed) 32-bit word, the low word's carry added to
-// the high one.  Shared 32-bit integer atomics are native; the sums are exact
-// and independent of the order of the adds.
-__device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restrict__ hi, long long e, long long x) {
-    const unsigned xl = (unsigned)(x & 0xffffffffll);
-    const int xh = (int)(x >> 32);
+// integer x = rint(a * sc) (sc a power of two with |x| < 2^40), and the block
+// holds each entry as a 64-bit two's-complement sum in a low (unsigned) and a
+// high (signed) 32-bit word, the low word's carry added to the high one.
+// Shared 32-bit integer atomics are native; the sums are exact and
+// independent of the order of the adds.  The split uses 32-bit conversions
+// and integer operations only (64-bit integer conversions run on the FP64
+// pipe, which is slow on this GPU): |x| = h 2^31 + l with h < 2^9, l < 2^31.
+__device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restrict__ hi, long long e, float xf) {
+    const float m = fabsf(xf);
+    const float hf = floorf(m * 4.656612873077393e-10f);            // m / 2^31, exact power-of-two scaling
+    const unsigned h = (unsigned)hf;
+    const unsigned l = __float2uint_rn(m - hf * 2147483648.0f);      // exact remainder, rounded to an integer
+    unsigned xl = ((h & 1u) << 31) | l;                              // |x| in base 2^32
+    unsigned xh = h >> 1;
+    if (xl == 0u && xh == 0u) return;
+    if (xf < 0.f) {                                                  // two's complement of the 64-bit value
+        xl = ~xl + 1u;
+        xh = ~xh + (xl == 0u ? 1u : 0u);
+    }
     const unsigned old = atomicAdd(&lo[e], xl);
-    const int carry = (old + xl < old) ? 1 : 0;
-    if (xh + carry != 0) atomicAdd(&hi[e], xh + carry);
+    const unsigned carry = (old + xl < old) ? 1u : 0u;
+    const int add_hi = (int)(xh + carry);
+    if (add_hi != 0) atomicAdd(&hi[e], add_hi);
 }
 
 // add_slots in fixed point.
@@ -153,11 +165,8 @@ __device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __r
                                2 * JC + c, 2 * JC + c + 1, 2 * JC + c + X0, 2 * JC + c + 1 + X0};
     const bool use[12] = {true, ey != 0, ez != 0, ey && ez, true, true, ez != 0, ez != 0, true, true, ey != 0, ey != 0};
 #pragma unroll
-    for (int q = 0; q < 12; ++q) {
-        if (!use[q]) continue;
-        const long long x = __float2ll_rn(a[q] * sc);
-        if (x != 0) fx_add(lo, hi, off[q], x);
-    }
+    for (int q = 0; q < 12; ++q)
+        if (use[q]) fx_add(lo, hi, off[q], a[q] * sc);
 }
 
 // CT: compile-time tile extent of a cubic 3-D tile (8), or 0 for shapes read

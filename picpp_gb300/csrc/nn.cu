@@ -47,7 +47,7 @@ int gs(long long n) { return grid_for(n, 256, 16); }
 template <int CI, int CO>
 void conv_t(cudaStream_t s, const bf16* x, const bf16* W, const float* b, bf16* y16, float* y32, Dims d, int relu) {
     static bool attr = false;
-    const size_t sm = nn::conv_smem_bytes(CI);
+    const size_t sm = nn::conv_smem_bytes(CI, CO);
     if (!attr) {
         cudaFuncSetAttribute(nn::k_conv3<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;

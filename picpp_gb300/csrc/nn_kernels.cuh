@@ -25,13 +25,22 @@ constexpr int kHD = kBD + 2, kHH = kBH + 2, kHW = kBW + 2;
 constexpr int kHalo = kHD * kHH * kHW;
 constexpr int kConvThreads = 256;
 
-__host__ __device__ constexpr size_t conv_smem_bytes(int cin) { return (size_t)kHalo * (cin + 8) * 2; }
+// Shared memory of one conv CTA: the input brick with halo and one plane
+// (9 taps) of weights, both with row stride CIN + 8 BF16.
+__host__ __device__ constexpr size_t conv_smem_bytes(int cin, int cout) {
+    return ((size_t)kHalo + 9 * (size_t)cout) * (cin + 8) * 2;
+}
 
 __device__ __forceinline__ void ldsm_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
     const unsigned a = (unsigned)__cvta_generic_to_shared(p);
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
                  : "r"(a));
+}
+
+__device__ __forceinline__ void ldsm_x2(unsigned& r0, unsigned& r1, const void* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(a));
 }
 
 __device__ __forceinline__ void mma_bf16_16816(float c[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
@@ -46,23 +55,24 @@ __device__ __forceinline__ void mma_bf16_16816(float c[4], unsigned a0, unsigned
 // y[v][co] = bias[co] + sum_tap sum_ci x[v + off(tap)][ci] * Wk[tap][co][ci]
 // (zero outside the box), then optional ReLU; written as BF16 (y16) and/or
 // FP32 (y32).  GEMM per CTA: M = 128 voxels (8 warps x m16), N = COUT, K =
-// 27 taps x CIN; the input brick plus a one-voxel halo is staged in shared
-// memory (row stride CIN + 8 BF16: conflict-free ldmatrix), the weights are
-// read through the read-only cache.
+// 27 taps x CIN.  The input brick plus a one-voxel halo and, plane by plane
+// (kd = 0, 1, 2), the nine taps' weights are staged in shared memory with
+// row stride CIN + 8 BF16 (conflict-free ldmatrix for A and B fragments).
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(kConvThreads) k_conv3(const bf16* __restrict__ x, const bf16* __restrict__ Wk,
                                                         const float* __restrict__ bias, bf16* __restrict__ y16,
                                                         float* __restrict__ y32, Dims dm, int relu) {
-    static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
     constexpr int SST = CIN + 8;
     constexpr int NT = COUT / 8;
+    constexpr int C8 = CIN / 8;
     extern __shared__ __align__(16) unsigned char conv_smem[];
-    bf16* sx = reinterpret_cast<bf16*>(conv_smem);
+    bf16* sx = reinterpret_cast<bf16*>(conv_smem);   // [kHalo][SST]
+    bf16* sw = sx + kHalo * SST;                     // [9][COUT][SST]
     const int nbd = (dm.D + kBD - 1) / kBD;
     const int w0 = blockIdx.x * kBW, h0 = blockIdx.y * kBH;
     const int n = blockIdx.z / nbd, d0 = (blockIdx.z % nbd) * kBD;
     // stage the halo brick, 8 channels (16 bytes) per access
-    constexpr int C8 = CIN / 8;
     for (int e = threadIdx.x; e < kHalo * C8; e += kConvThreads) {
         const int hv = e / C8, c8 = e - hv * C8;
         const int hw = hv % kHW, hh = (hv / kHW) % kHH, hd = hv / (kHW * kHH);
@@ -72,7 +82,6 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3(const bf16* __restrict__
             val = *reinterpret_cast<const uint4*>(x + ((((long long)n * dm.D + d) * dm.H + h) * dm.W + w) * CIN + c8 * 8);
         *reinterpret_cast<uint4*>(sx + hv * SST + c8 * 8) = val;
     }
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
     // ldmatrix row of this lane: voxel r = lane % 16 of the warp's 16
@@ -80,24 +89,39 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3(const bf16* __restrict__
     const int v = warp * 16 + r;
     const int vd = v / (kBH * kBW), vh = (v / kBW) % kBH, vw = v % kBW;
     const int koff = (lane >> 4) * 8;
+    // B fragments: lanes 0-7 rows co of k half 0, lanes 8-15 k half 1,
+    // lanes 16-31 the same for the next n-tile
+    const int brow = (lane & 7) + ((lane >> 4) << 3);
+    const int bk = ((lane >> 3) & 1) * 8;
     float acc[NT][4];
 #pragma unroll
     for (int i = 0; i < NT; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
 #pragma unroll 1
-    for (int tap = 0; tap < 27; ++tap) {
-        const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
-        const bf16* arow = sx + (((vd + kd) * kHH + (vh + kh)) * kHW + (vw + kw)) * SST + koff;
-        const bf16* wt = Wk + (size_t)tap * COUT * CIN;
+    for (int kd = 0; kd < 3; ++kd) {
+        __syncthreads();   // previous plane's weights consumed (and, for kd = 0, the halo staged)
+        const bf16* wsrc = Wk + (size_t)kd * 9 * COUT * CIN;
+        for (int e = threadIdx.x; e < 9 * COUT * C8; e += kConvThreads) {
+            const int row = e / C8, c8 = e - row * C8;   // row = tap_in_plane * COUT + co
+            *reinterpret_cast<uint4*>(sw + row * SST + c8 * 8) =
+                *reinterpret_cast<const uint4*>(wsrc + (size_t)row * CIN + c8 * 8);
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int tp = 0; tp < 9; ++tp) {
+            const int kh = tp / 3, kw = tp % 3;
+            const bf16* arow = sx + (((vd + kd) * kHH + (vh + kh)) * kHW + (vw + kw)) * SST + koff;
+            const bf16* wt = sw + (size_t)tp * COUT * SST;
 #pragma unroll
-        for (int k0 = 0; k0 < CIN; k0 += 16) {
-            unsigned a0, a1, a2, a3;
-            ldsm_x4(a0, a1, a2, a3, arow + k0);
+            for (int k0 = 0; k0 < CIN; k0 += 16) {
+                unsigned a0, a1, a2, a3;
+                ldsm_x4(a0, a1, a2, a3, arow + k0);
 #pragma unroll
-            for (int nt = 0; nt < NT; ++nt) {
-                const bf16* wp = wt + (nt * 8 + g) * CIN + k0 + 2 * t;
-                const unsigned b0 = __ldg(reinterpret_cast<const unsigned*>(wp));
-                const unsigned b1 = __ldg(reinterpret_cast<const unsigned*>(wp + 8));
-                mma_bf16_16816(acc[nt], a0, a1, a2, a3, b0, b1);
+                for (int nt = 0; nt < NT; nt += 2) {
+                    unsigned b0, b1, b2, b3;
+                    ldsm_x4(b0, b1, b2, b3, wt + (nt * 8 + brow) * SST + k0 + bk);
+                    mma_bf16_16816(acc[nt], a0, a1, a2, a3, b0, b1);
+                    mma_bf16_16816(acc[nt + 1], a0, a1, a2, a3, b2, b3);
+                }
             }
         }
     }

@@ -344,8 +344,14 @@ def run_gb300(a):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
+    # DRAM bytes of one launch from an ncu capture of the same kernel on the
+    # 64^3 case (profiles/push_deposit_tile_64cubed_ncu.md: 457.3 MB), scaled
+    # by the units a launch processes (particles and cells grow alike)
+    units = npart / (64 ** 3 * 2 * a.ppc) if a.ppc else 0.0
+    traffic = 457.3e6 * units if (nx * ny * nz) * 2 * a.ppc == npart else None
     roof = {"kernel": "k_push_deposit_tile<float,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "ncu dram bytes of the 64^3 launch scaled by the particles per launch",
             "peak_source": "measured" if peaks else "fallback",
             "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": push_ms,
             "phase_ms_per_step": {k: v / a.steps for k, v in phases.items() if v > 0}}

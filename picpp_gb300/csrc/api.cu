@@ -477,6 +477,12 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     ts.fx = t.tx + 2 * ts.hx; ts.fy = t.ty + 2 * ts.hy; ts.fz = t.tz + 2 * ts.hz;
     ts.jx = t.tx + 2 * ts.gx; ts.jy = t.ty + 2 * ts.gy; ts.jz = t.tz + 2 * ts.gz;
     ts.jcells = (long long)ts.jx * ts.jy * ts.jz;
+    // the fused explicit kernel holds the tile's fields and current in shared memory
+    if (c.solver == PIC_SOLVER_BUNEMAN &&
+        (ctx->preal ? PK<double>::tile_smem_bytes(ts) : PK<float>::tile_smem_bytes(ts)) > 200 * 1024) {
+        delete ctx;
+        return PIC_ERR_ARG;
+    }
     GhostAxes& ga = ctx->ga;
     ga.cex = c.nx > 1 ? c.nx + 4 : 1; ga.cey = c.ny > 1 ? c.ny + 4 : 1; ga.cez = c.nz > 1 ? c.nz + 4 : 1;
     ga.gx = c.nx > 1 ? 2 : 0; ga.gy = c.ny > 1 ? 2 : 0; ga.gz = c.nz > 1 ? 2 : 0;

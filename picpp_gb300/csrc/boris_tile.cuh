@@ -32,7 +32,10 @@
 
 namespace pic {
 
-constexpr int kTileThreads = 256;
+#ifndef PIC_TILE_THREADS
+#define PIC_TILE_THREADS 512   // threads per CTA of the fused explicit kernel (64 registers at 2 CTAs/SM)
+#endif
+constexpr int kTileThreads = PIC_TILE_THREADS;
 #ifndef PIC_TILE_MIN_BLOCKS
 #define PIC_TILE_MIN_BLOCKS 2   // CTAs per SM the register budget is sized for
 #endif

@@ -22,7 +22,14 @@
 
 namespace pic {
 
-constexpr int kImpThreads = 256;
+#ifndef PIC_IMP_THREADS
+#define PIC_IMP_THREADS 512   // threads per CTA of the tiled implicit deposit (2 CTAs/SM, 64 registers)
+#endif
+#ifndef PIC_MOVER_THREADS
+#define PIC_MOVER_THREADS 256   // threads per CTA of the tiled implicit mover (2 CTAs/SM)
+#endif
+constexpr int kImpThreads = PIC_IMP_THREADS;
+constexpr int kMoverThreads = PIC_MOVER_THREADS;
 constexpr int kXposeMin = 4;   // fewest lanes of one cell that take the transpose-reduction
 
 
@@ -351,7 +358,7 @@ struct MoverBlock {
 // shared memory; a particle whose stencil leaves the block gathers from the
 // FP64 grids.  Same arithmetic as k_implicit_push.
 template <typename T>
-__global__ void __launch_bounds__(256) k_implicit_push_tile(GridP g, TileGeom t, MoverBlock mb, ImpSpecies<T> S,
+__global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g, TileGeom t, MoverBlock mb, ImpSpecies<T> S,
                                                             const double* __restrict__ E, const double* __restrict__ B,
                                                             const double* __restrict__ Et) {
     extern __shared__ __align__(16) unsigned char mv_smem[];

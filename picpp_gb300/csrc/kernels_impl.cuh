@@ -258,7 +258,7 @@ bool PK<T>::implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& 
     const int per_sm = (int)((228 * 1024) / (smem + 1024));
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int cap = kNumSM * (per_sm > 0 ? per_sm : 1);
-    k_implicit_push_tile<T><<<ntiles < cap ? ntiles : cap, 256, smem, s>>>(g, t, mb, S, E, B, Et);
+    k_implicit_push_tile<T><<<ntiles < cap ? ntiles : cap, kMoverThreads, smem, s>>>(g, t, mb, S, E, B, Et);
     return true;
 }
 

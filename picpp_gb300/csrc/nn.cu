@@ -6,6 +6,7 @@
 
 #include "kernels.hpp"
 #include "nn.hpp"
+#include "conv_tc.cuh"
 #include "nn_kernels.cuh"
 #include "solver.hpp"
 
@@ -45,23 +46,24 @@ enum { E0A, E0B, E1A, E1B, E2A, E2B, D1A, D1B, D0A, D0B, HEAD };
 int gs(long long n) { return grid_for(n, 256, 16); }
 
 template <int CI, int CO>
-void conv_t(cudaStream_t s, const bf16* x, const bf16* W, const float* b, bf16* y16, float* y32, Dims d, int relu) {
+void conv_t(cudaStream_t s, const bf16* x, const bf16* W, const float* b, bf16* y16, float* y32, Dims d, int relu,
+            int* err) {
     static bool attr = false;
-    const size_t sm = nn::conv_smem_bytes(CI, CO);
+    const size_t sm = nn::tc_conv_smem_bytes(CI, CO);
     if (!attr) {
-        cudaFuncSetAttribute(nn::k_conv3<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(nn::k_conv3_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
-    dim3 grid((d.W + nn::kBW - 1) / nn::kBW, (d.H + nn::kBH - 1) / nn::kBH, d.N * ((d.D + nn::kBD - 1) / nn::kBD));
-    nn::k_conv3<CI, CO><<<grid, nn::kConvThreads, sm, s>>>(x, W, b, y16, y32, d, relu);
+    dim3 grid((d.W + nn::kTcW - 1) / nn::kTcW, (d.H + nn::kTcH - 1) / nn::kTcH, d.N * d.D);
+    nn::k_conv3_tc<CI, CO><<<grid, nn::kTcThreads, sm, s>>>(x, W, b, y16, y32, d.N, d.D, d.H, d.W, relu, err);
 }
 
 // Every (cin, cout) pair of the forward layers and of their input-gradient
 // (transposed) convolutions.
 void conv(cudaStream_t s, int ci, int co, const bf16* x, const bf16* W, const float* b, bf16* y16, float* y32, Dims d,
-          int relu) {
+          int relu, int* err) {
 #define PIC_CONV(A, B) \
-    if (ci == A && co == B) return conv_t<A, B>(s, x, W, b, y16, y32, d, relu)
+    if (ci == A && co == B) return conv_t<A, B>(s, x, W, b, y16, y32, d, relu, err)
     PIC_CONV(16, 16); PIC_CONV(16, 32); PIC_CONV(32, 16); PIC_CONV(32, 32); PIC_CONV(32, 64); PIC_CONV(64, 32);
     PIC_CONV(64, 64); PIC_CONV(96, 32); PIC_CONV(32, 96); PIC_CONV(48, 16); PIC_CONV(16, 48);
 #undef PIC_CONV
@@ -230,6 +232,7 @@ Net::Net() = default;
 Net::~Net() {
     for (auto* b : bufs_) delete b;
     cudaFree(p_); cudaFree(g_); cudaFree(m_); cudaFree(v_); cudaFree(wk_); cudaFree(wt_); cudaFree(loss_);
+    cudaFree(tc_err_);
 }
 
 const std::vector<NetLayer>& Net::layers() {
@@ -299,6 +302,8 @@ pic_status Net::init(cudaStream_t s, unsigned long long seed, std::string* err) 
         NCK(cudaMalloc(&wk_, sizeof(bf16) * n));
         NCK(cudaMalloc(&wt_, sizeof(bf16) * n));
         NCK(cudaMalloc(&loss_, sizeof(double)));
+        NCK(cudaMalloc(&tc_err_, sizeof(int)));
+        NCK(cudaMemsetAsync(tc_err_, 0, sizeof(int), s));
     }
     NCK(cudaMemsetAsync(p_, 0, sizeof(float) * n, s));
     NCK(cudaMemsetAsync(m_, 0, sizeof(float) * n, s));
@@ -343,12 +348,24 @@ pic_status Net::get_params(cudaStream_t s, float* host, std::string* err) {
     return PIC_OK;
 }
 
+pic_status Net::check_tc(cudaStream_t s, std::string* err) {
+    int flag = 0;
+    NCK(cudaMemcpyAsync(&flag, tc_err_, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NCK(cudaStreamSynchronize(s));
+    if (flag) {
+        cudaMemsetAsync(tc_err_, 0, sizeof(int), s);
+        if (err) *err = "tensor-core convolution: an MMA completion wait ran out";
+        return PIC_ERR_CUDA;
+    }
+    return PIC_OK;
+}
+
 void Net::forward(cudaStream_t s, NetBuffers& b) {
     const auto& L = layers();
     const bf16* wk = (const bf16*)wk_;
     auto cv = [&](int li, const bf16* x, bf16* y16, float* y32, Dims d) {
         const NetLayer& l = L[li];
-        conv(s, l.cin, l.cout, x, wk + l.woff, p_ + l.boff, y16, y32, d, l.relu);
+        conv(s, l.cin, l.cout, x, wk + l.woff, p_ + l.boff, y16, y32, d, l.relu, tc_err_);
     };
     cv(E0A, b.x0, b.e0a, nullptr, b.dm0);
     cv(E0B, b.e0a, b.e0, nullptr, b.dm0);
@@ -378,7 +395,7 @@ void Net::backward(cudaStream_t s, NetBuffers& b) {
         const long long n = d.vox() * l.cout;
         nn::k_relu_bwd<<<gs(n), 256, 0, s>>>(gy, l.relu ? y : nullptr, b.g16, n);
         wgrad(s, l.cin, l.cout, x, b.g16, d, g_ + l.woff, g_ + l.boff);
-        if (gx) conv(s, l.cout, l.cin, b.g16, wt + l.woff, nullptr, nullptr, gx, d, 0);
+        if (gx) conv(s, l.cout, l.cin, b.g16, wt + l.woff, nullptr, nullptr, gx, d, 0, tc_err_);
     };
     back(HEAD, b.A0, nullptr, b.d0, b.B0, b.dm0);
     back(D0B, b.B0, b.d0, b.d0a, b.A0, b.dm0);
@@ -417,7 +434,7 @@ pic_status Net::forward_host(cudaStream_t s, int n, int d, int h, int w, const f
     cudaFree(tmp);
     NCK(e);
     NCK(cudaGetLastError());
-    return PIC_OK;
+    return check_tc(s, err);
 }
 
 pic_status Net::loss_grad_host(cudaStream_t s, int n, int d, int h, int w, const float* x0, const float* target,
@@ -440,7 +457,7 @@ pic_status Net::loss_grad_host(cudaStream_t s, int n, int d, int h, int w, const
     NCK(cudaMemcpyAsync(grad, g_, sizeof(float) * param_count(), cudaMemcpyDeviceToHost, s));
     NCK(cudaStreamSynchronize(s));
     NCK(cudaGetLastError());
-    return PIC_OK;
+    return check_tc(s, err);
 }
 
 pic_status Net::apply(cudaStream_t s, const GridP& g, const double* mu, const double* v, double* z, double* scal,
@@ -452,7 +469,8 @@ pic_status Net::apply(cudaStream_t s, const GridP& g, const double* mu, const do
     launch_dot(s, v, v, L, partials, red_blocks(L), scal, 1);
     double nv = 0;
     NCK(cudaMemcpyAsync(&nv, scal, sizeof(double), cudaMemcpyDeviceToHost, s));
-    NCK(cudaStreamSynchronize(s));
+    st = check_tc(s, err);   // also waits for the norm
+    if (st != PIC_OK) return st;
     if (!(nv > 0) || !std::isfinite(nv)) {
         NCK(cudaMemsetAsync(z, 0, sizeof(double) * L, s));
         return PIC_OK;
@@ -565,7 +583,7 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
         if (err) *err = "training diverged";
         return PIC_ERR_NUMERIC;
     }
-    return PIC_OK;
+    return check_tc(s, err);
 }
 
 }  // namespace pic

@@ -35,6 +35,8 @@ public:
     pic_status set_params(cudaStream_t s, const float* host, std::string* err);
     pic_status get_params(cudaStream_t s, float* host, std::string* err);
     bool ready() const { return ready_; }
+    // waits for the stream; an error if a convolution reported a timed-out wait
+    pic_status check_tc(cudaStream_t s, std::string* err);
 
     // x0: [n][d][h][w][16] BF16 on the device is packed by the callers below.
     // Forward on host FP32 input (channels 16), output [..][16] FP32 to host.
@@ -61,6 +63,7 @@ private:
     void* wk_ = nullptr;   // BF16 forward weights, per layer at woff
     void* wt_ = nullptr;   // BF16 flipped/transposed weights
     double* loss_ = nullptr;
+    int* tc_err_ = nullptr;   // set by a convolution whose MMA completion wait ran out
     int adam_t_ = 0;
     bool ready_ = false;
     std::vector<NetBuffers*> bufs_;

@@ -1,7 +1,6 @@
-// nn_kernels.cuh -- kernels of the learned preconditioner's network: 3x3x3
-// convolutions as implicit GEMMs on the BF16 tensor cores (FP32
-// accumulation), pooling / upsampling / skip concatenation, their
-// backward passes, weight gradients, the loss and Adam.
+// nn_kernels.cuh -- kernels of the learned preconditioner's network besides
+// the tensor-core convolution (conv_tc.cuh): pooling / upsampling / skip
+// concatenation, their backward passes, weight gradients, the loss and Adam.
 //
 // Activations are NDHWC BF16 with channel counts that are multiples of 16;
 // a voxel's channels are one contiguous 16-byte-aligned run.
@@ -18,131 +17,6 @@ struct Dims {
     int N, D, H, W;
     __host__ __device__ long long vox() const { return (long long)N * D * H * W; }
 };
-
-// Output brick of one conv CTA: 2 x 8 x 8 voxels, 16 per warp.
-constexpr int kBD = 2, kBH = 8, kBW = 8;
-constexpr int kHD = kBD + 2, kHH = kBH + 2, kHW = kBW + 2;
-constexpr int kHalo = kHD * kHH * kHW;
-constexpr int kConvThreads = 256;
-
-// Shared memory of one conv CTA: the input brick with halo and one plane
-// (9 taps) of weights, both with row stride CIN + 8 BF16.
-__host__ __device__ constexpr size_t conv_smem_bytes(int cin, int cout) {
-    return ((size_t)kHalo + 9 * (size_t)cout) * (cin + 8) * 2;
-}
-
-__device__ __forceinline__ void ldsm_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(a));
-}
-
-__device__ __forceinline__ void ldsm_x2(unsigned& r0, unsigned& r1, const void* p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(a));
-}
-
-__device__ __forceinline__ void mma_bf16_16816(float c[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
-                                               unsigned b0, unsigned b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// y[v][co] = bias[co] + sum_tap sum_ci x[v + off(tap)][ci] * Wk[tap][co][ci]
-// (zero outside the box), then optional ReLU; written as BF16 (y16) and/or
-// FP32 (y32).  GEMM per CTA: M = 128 voxels (8 warps x m16), N = COUT, K =
-// 27 taps x CIN.  The input brick plus a one-voxel halo and, plane by plane
-// (kd = 0, 1, 2), the nine taps' weights are staged in shared memory with
-// row stride CIN + 8 BF16 (conflict-free ldmatrix for A and B fragments).
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(kConvThreads) k_conv3(const bf16* __restrict__ x, const bf16* __restrict__ Wk,
-                                                        const float* __restrict__ bias, bf16* __restrict__ y16,
-                                                        float* __restrict__ y32, Dims dm, int relu) {
-    static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
-    constexpr int SST = CIN + 8;
-    constexpr int NT = COUT / 8;
-    constexpr int C8 = CIN / 8;
-    extern __shared__ __align__(16) unsigned char conv_smem[];
-    bf16* sx = reinterpret_cast<bf16*>(conv_smem);   // [kHalo][SST]
-    bf16* sw = sx + kHalo * SST;                     // [9][COUT][SST]
-    const int nbd = (dm.D + kBD - 1) / kBD;
-    const int w0 = blockIdx.x * kBW, h0 = blockIdx.y * kBH;
-    const int n = blockIdx.z / nbd, d0 = (blockIdx.z % nbd) * kBD;
-    // stage the halo brick, 8 channels (16 bytes) per access
-    for (int e = threadIdx.x; e < kHalo * C8; e += kConvThreads) {
-        const int hv = e / C8, c8 = e - hv * C8;
-        const int hw = hv % kHW, hh = (hv / kHW) % kHH, hd = hv / (kHW * kHH);
-        const int d = d0 - 1 + hd, h = h0 - 1 + hh, w = w0 - 1 + hw;
-        uint4 val = make_uint4(0, 0, 0, 0);
-        if (d >= 0 && d < dm.D && h >= 0 && h < dm.H && w >= 0 && w < dm.W)
-            val = *reinterpret_cast<const uint4*>(x + ((((long long)n * dm.D + d) * dm.H + h) * dm.W + w) * CIN + c8 * 8);
-        *reinterpret_cast<uint4*>(sx + hv * SST + c8 * 8) = val;
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    // ldmatrix row of this lane: voxel r = lane % 16 of the warp's 16
-    const int r = lane & 15;
-    const int v = warp * 16 + r;
-    const int vd = v / (kBH * kBW), vh = (v / kBW) % kBH, vw = v % kBW;
-    const int koff = (lane >> 4) * 8;
-    // B fragments: lanes 0-7 rows co of k half 0, lanes 8-15 k half 1,
-    // lanes 16-31 the same for the next n-tile
-    const int brow = (lane & 7) + ((lane >> 4) << 3);
-    const int bk = ((lane >> 3) & 1) * 8;
-    float acc[NT][4];
-#pragma unroll
-    for (int i = 0; i < NT; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
-#pragma unroll 1
-    for (int kd = 0; kd < 3; ++kd) {
-        __syncthreads();   // previous plane's weights consumed (and, for kd = 0, the halo staged)
-        const bf16* wsrc = Wk + (size_t)kd * 9 * COUT * CIN;
-        for (int e = threadIdx.x; e < 9 * COUT * C8; e += kConvThreads) {
-            const int row = e / C8, c8 = e - row * C8;   // row = tap_in_plane * COUT + co
-            *reinterpret_cast<uint4*>(sw + row * SST + c8 * 8) =
-                *reinterpret_cast<const uint4*>(wsrc + (size_t)row * CIN + c8 * 8);
-        }
-        __syncthreads();
-#pragma unroll 1
-        for (int tp = 0; tp < 9; ++tp) {
-            const int kh = tp / 3, kw = tp % 3;
-            const bf16* arow = sx + (((vd + kd) * kHH + (vh + kh)) * kHW + (vw + kw)) * SST + koff;
-            const bf16* wt = sw + (size_t)tp * COUT * SST;
-#pragma unroll
-            for (int k0 = 0; k0 < CIN; k0 += 16) {
-                unsigned a0, a1, a2, a3;
-                ldsm_x4(a0, a1, a2, a3, arow + k0);
-#pragma unroll
-                for (int nt = 0; nt < NT; nt += 2) {
-                    unsigned b0, b1, b2, b3;
-                    ldsm_x4(b0, b1, b2, b3, wt + (nt * 8 + brow) * SST + k0 + bk);
-                    mma_bf16_16816(acc[nt], a0, a1, a2, a3, b0, b1);
-                    mma_bf16_16816(acc[nt + 1], a0, a1, a2, a3, b2, b3);
-                }
-            }
-        }
-    }
-    // epilogue: rows g and g + 8 of the warp's 16 voxels
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        const int vv = warp * 16 + g + half * 8;
-        const int d = d0 + vv / (kBH * kBW), h = h0 + (vv / kBW) % kBH, w = w0 + vv % kBW;
-        if (d >= dm.D || h >= dm.H || w >= dm.W) continue;
-        const long long o = ((((long long)n * dm.D + d) * dm.H + h) * dm.W + w) * COUT;
-#pragma unroll
-        for (int nt = 0; nt < NT; ++nt) {
-            const int co = nt * 8 + 2 * t;
-            float y0 = acc[nt][2 * half], y1 = acc[nt][2 * half + 1];
-            if (bias) { y0 += bias[co]; y1 += bias[co + 1]; }
-            if (relu) { y0 = fmaxf(y0, 0.f); y1 = fmaxf(y1, 0.f); }
-            if (y16) *reinterpret_cast<__nv_bfloat162*>(y16 + o + co) = __floats2bfloat162_rn(y0, y1);
-            if (y32) *reinterpret_cast<float2*>(y32 + o + co) = make_float2(y0, y1);
-        }
-    }
-}
 
 // dW[tap][co][ci] += sum_v x[v + off(tap)][ci] * gy[v][co], and (blocks of
 // tap 0) db[co] += sum_v gy[v][co]; FP32 partial sums over a chunk of 128

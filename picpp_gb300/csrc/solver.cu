@@ -194,6 +194,7 @@ pic_status ensure_z(SolveCtx& c, int m, long long L) {
 pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, double* x, const pic_solve_opts& o,
                            pic_solve_info* info, Net* pc = nullptr) {
     const GridP& g = *c.g;
+    Net* const net = pc;   // pc becomes nullptr on a fallback
     const long long L = 3 * g.N;
     const int P = red_blocks(L);
     const int m = std::max(1, o.restart > 0 ? o.restart : 30);
@@ -315,6 +316,7 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             if (degenerate) { pc = nullptr; fallback = true; }
         }
     }
+    if (net && (st = net->check_tc(c.s, c.err)) != PIC_OK) return st;
     if (info) {
         info->iterations = total;
         info->restarts = restarts;

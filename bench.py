@@ -100,7 +100,7 @@ def implicit_section(a):
     out["step_ms"] = ms
     out["particle_steps_per_s"] = npart / (ms * 1e-3)
     out["phase_ms"] = {k: v for k, v in phases.items() if v > 0}
-    out["plain"] = {"solver": "GMRES(30), CGS2, FP64", "iterations": info["iterations"],
+    out["plain"] = {"solver": "GMRES(30), classical Gram-Schmidt with selective second pass, FP64", "iterations": info["iterations"],
                     "restarts": info["restarts"], "rel_residual": info["rel_residual"],
                     "seconds": info["seconds"]}
     if a.nn_steps > 0:

@@ -899,7 +899,9 @@ pic_status pic_maxwell_apply(pic_ctx* ctx, const double* mu, const double* x, do
     CK(cudaMemcpyAsync(ctx->mu, mu, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->Et, x, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
     OpCoef oc = make_opcoef(ctx->g);
-    launch_maxwell_apply(s, ctx->g, oc, ctx->mu, ctx->Et, ctx->En);
+    pic_status st = ensure_smooth_tmp(ctx);
+    if (st != PIC_OK) return st;
+    launch_maxwell_apply(s, ctx->g, oc, ctx->mu, ctx->Et, ctx->En, ctx->smooth_tmp);
     CK(cudaMemcpyAsync(y, ctx->En, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
     ctx->mu_valid = true;
     ctx->moments_ready = false;

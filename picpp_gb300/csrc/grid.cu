@@ -79,8 +79,9 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
 }
 
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
-                          double* y) {
-    k_maxwell_apply<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, mu, x, y);
+                          double* y, double* wmu) {
+    k_mu_times<<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
+    k_maxwell_stencil<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
 }
 
 void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* y,

@@ -232,68 +232,70 @@ __device__ __forceinline__ void mu_times(const double* __restrict__ mu, long lon
         w[a] = mu[(3 * a) * N + id] * x0 + mu[(3 * a + 1) * N + id] * x1 + mu[(3 * a + 2) * N + id] * x2;
 }
 
-__global__ void __launch_bounds__(256) k_maxwell_apply(GridP g, OpCoef oc, const double* __restrict__ mu,
-                                                       const double* __restrict__ x, double* __restrict__ y) {
+// The operator in two passes, A x = P x + Q (mu x): this GPU's FP64 rate
+// (about 1/64 of FP32) makes the apply arithmetic-bound, so mu x is formed
+// once per node (9 operations) instead of at every stencil point that reads
+// it (centre, 6 neighbours, 12 corners: about 190 operations per node).
+// Pass 1: w_a = sum_b mu_ab x_b.
+__global__ void __launch_bounds__(256) k_mu_times(long long N, const double* __restrict__ mu,
+                                                  const double* __restrict__ x, double* __restrict__ w) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        double wc[3];
+        mu_times(mu, N, c, x, wc);
+        w[c] = wc[0]; w[N + c] = wc[1]; w[2 * N + c] = wc[2];
+    }
+}
+
+// Pass 2: per row a (createInternalEquationX/Y/Z, fields.cpp:1396-1509,
+// 1961-2073, 2521-2633): diag x_a - c1 w_a; along axis a K/da^2 (w_a - x_a)
+// at both neighbours, along the other axes -K/d^2 x_a; in the (a, d) planes
+// K/(4 da dd) (w_d(++) - w_d(+-) - w_d(-+) + w_d(--)).  Periodic box.
+__global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, const double* __restrict__ x,
+                                                         const double* __restrict__ w, double* __restrict__ y) {
     const long long N = g.N;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const long long st[3] = {1, (long long)g.nx, (long long)g.nx * g.ny};
+    double diag = 1.0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+        if (oc.has[ax]) diag += 2.0 * oc.kd2[ax];
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
         int p[3];
         decode(g, (int)c, p[0], p[1], p[2]);
-        const int n[3] = {g.nx, g.ny, g.nz};
-        double xc[3] = {x[c], x[N + c], x[2 * N + c]};
-        double wc[3];
-        mu_times(mu, N, c, x, wc);
-        double acc[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            double diag = 1.0;
-            for (int ax = 0; ax < 3; ++ax)
-                if (oc.has[ax]) diag += 2.0 * oc.kd2[ax];
-            double c1 = oc.has[a] ? 1.0 + 2.0 * oc.kd2[a] : 1.0;
-            acc[a] = diag * xc[a] - c1 * wc[a];
-        }
-        // neighbours along each axis: +-a term for row a, Laplacian for the others
+        long long up[3], dn[3];   // linear offsets of the periodic +1 / -1 neighbours
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
-            if (!oc.has[ax]) continue;
-            for (int s = -1; s <= 1; s += 2) {
-                int q[3] = {p[0], p[1], p[2]};
-                q[ax] = wrap_any(q[ax] + s, n[ax]);
-                long long cn = lin(g, q[0], q[1], q[2]);
-                double wn[3];
-                mu_times(mu, N, cn, x, wn);
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    double xa = x[a * N + cn];
-                    if (a == ax) acc[a] += oc.kd2[ax] * (wn[a] - xa);
-                    else acc[a] -= oc.kd2[ax] * xa;
-                }
-            }
+            up[ax] = p[ax] + 1 == n[ax] ? -(long long)(n[ax] - 1) * st[ax] : st[ax];
+            dn[ax] = p[ax] == 0 ? (long long)(n[ax] - 1) * st[ax] : -st[ax];
         }
-        // mixed derivatives in the (a, d) planes: row a reads w_d at the corners
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 3; ++a) {
+            const double* xa = x + a * N + c;
+            const double* wa = w + a * N + c;
+            const double c1 = oc.has[a] ? 1.0 + 2.0 * oc.kd2[a] : 1.0;
+            double acc = fma(-c1, wa[0], diag * xa[0]);
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                if (!oc.has[ax]) continue;
+                const double xs = xa[up[ax]] + xa[dn[ax]];
+                if (ax == a) acc = fma(oc.kd2[ax], (wa[up[ax]] + wa[dn[ax]]) - xs, acc);
+                else acc = fma(-oc.kd2[ax], xs, acc);
+            }
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (d == a || !oc.has[a] || !oc.has[d]) continue;
-                double sum = 0.0;
-                for (int sa = -1; sa <= 1; sa += 2)
-                    for (int sd = -1; sd <= 1; sd += 2) {
-                        int q[3] = {p[0], p[1], p[2]};
-                        q[a] = wrap_any(q[a] + sa, n[a]);
-                        q[d] = wrap_any(q[d] + sd, n[d]);
-                        long long cn = lin(g, q[0], q[1], q[2]);
-                        double xn0 = x[cn], xn1 = x[N + cn], xn2 = x[2 * N + cn];
-                        double wd = mu[(3 * d) * N + cn] * xn0 + mu[(3 * d + 1) * N + cn] * xn1 + mu[(3 * d + 2) * N + cn] * xn2;
-                        sum += (sa * sd > 0) ? wd : -wd;
-                    }
-                acc[a] += oc.kx4[a][d] * sum;
+                const double* wd = w + d * N + c;
+                const double sum = (wd[up[a] + up[d]] - wd[up[a] + dn[d]]) - (wd[dn[a] + up[d]] - wd[dn[a] + dn[d]]);
+                acc = fma(oc.kx4[a][d], sum, acc);
             }
-        y[c] = acc[0]; y[N + c] = acc[1]; y[2 * N + c] = acc[2];
+            y[a * N + c] = acc;
+        }
     }
 }
 
-// Transpose of k_maxwell_apply.  The operator splits as A x = P x + Q (mu x)
+// Transpose of the operator (k_mu_times + k_maxwell_stencil).  The operator splits as A x = P x + Q (mu x)
 // with P and Q constant-coefficient periodic stencils that are symmetric
 // (P: the diagonal and the -K/d^2 neighbour couplings; Q: -c1 on the node,
 // +K/da^2 along axis a in row a, the K/(4 da dd) corner couplings, whose

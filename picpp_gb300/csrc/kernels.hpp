@@ -97,8 +97,9 @@ void launch_rho_ext_periodic(cudaStream_t s, const GridP& g, const double* J, co
                              int ex, int ey, int ez);
 void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const double* B, const double* J,
                         const double* rho_ext, int ex, int ey, double* rhs);
+// y = A(mu) x; wmu: scratch of 3N doubles (mu x)
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
-                          double* y);
+                          double* y, double* wmu);
 void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* y,
                             double* out);
 void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,

@@ -73,9 +73,12 @@ __global__ void k_multi_axpy_minus(double* __restrict__ w, const double* __restr
 // v = w / h[0] (v = 0 when h[0] == 0, specialmath.cpp:336-349).
 __global__ void k_scale_inv_dev(double* __restrict__ v, const double* __restrict__ w, const double* __restrict__ h,
                                 long long n) {
+    // one reciprocal per thread: an FP64 division per element would make
+    // this copy arithmetic-bound on this GPU's FP64 pipe
     const double d = *h;
+    const double inv = d > 0 ? 1.0 / d : 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        v[i] = d > 0 ? w[i] / d : 0.0;
+        v[i] = w[i] * inv;
 }
 
 // v = w * s (host scalar)

@@ -369,16 +369,16 @@ void Net::forward(cudaStream_t s, NetBuffers& b) {
     };
     cv(E0A, b.x0, b.e0a, nullptr, b.dm0);
     cv(E0B, b.e0a, b.e0, nullptr, b.dm0);
-    nn::k_pool<<<gs(b.dm1.vox() * 16), 256, 0, s>>>(b.e0, b.p1, b.dm0, 16);
+    nn::k_pool<<<gs(b.dm1.vox() * 2), 256, 0, s>>>(b.e0, b.p1, b.dm0, 16);
     cv(E1A, b.p1, b.e1a, nullptr, b.dm1);
     cv(E1B, b.e1a, b.e1, nullptr, b.dm1);
-    nn::k_pool<<<gs(b.dm2.vox() * 32), 256, 0, s>>>(b.e1, b.p2, b.dm1, 32);
+    nn::k_pool<<<gs(b.dm2.vox() * 4), 256, 0, s>>>(b.e1, b.p2, b.dm1, 32);
     cv(E2A, b.p2, b.e2a, nullptr, b.dm2);
     cv(E2B, b.e2a, b.e2, nullptr, b.dm2);
-    nn::k_up_concat<<<gs(b.dm1.vox() * 96), 256, 0, s>>>(b.e2, b.e1, b.c1, b.dm1, 64, 32);
+    nn::k_up_concat<<<gs(b.dm1.vox() * 12), 256, 0, s>>>(b.e2, b.e1, b.c1, b.dm1, 64, 32);
     cv(D1A, b.c1, b.d1a, nullptr, b.dm1);
     cv(D1B, b.d1a, b.d1, nullptr, b.dm1);
-    nn::k_up_concat<<<gs(b.dm0.vox() * 48), 256, 0, s>>>(b.d1, b.e0, b.c0, b.dm0, 32, 16);
+    nn::k_up_concat<<<gs(b.dm0.vox() * 6), 256, 0, s>>>(b.d1, b.e0, b.c0, b.dm0, 32, 16);
     cv(D0A, b.c0, b.d0a, nullptr, b.dm0);
     cv(D0B, b.d0a, b.d0, nullptr, b.dm0);
     cv(HEAD, b.d0, nullptr, b.out, b.dm0);
@@ -495,7 +495,7 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
     pic_status st = buffers(s, nb, g.nz, g.ny, g.nx, true, &b, err);
     if (st != PIC_OK) return st;
     const long long L = 3 * g.N;
-    double *r = nullptr, *r2 = nullptr, *z = nullptr, *e = nullptr, *scal = nullptr;
+    double *r = nullptr, *r2 = nullptr, *z = nullptr, *e = nullptr, *wm = nullptr, *scal = nullptr;
     std::vector<void*> tmp;
     auto al = [&](double** p, size_t n) -> bool {
         if (cudaMalloc((void**)p, sizeof(double) * n) != cudaSuccess) return false;
@@ -503,7 +503,7 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
         return true;
     };
     auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
-    if (!al(&r, (size_t)L * nb) || !al(&r2, L) || !al(&z, L) || !al(&e, L) || !al(&scal, 4)) {
+    if (!al(&r, (size_t)L * nb) || !al(&r2, L) || !al(&z, L) || !al(&e, L) || !al(&wm, L) || !al(&scal, 4)) {
         cleanup();
         if (err) *err = "out of device memory for training";
         return PIC_ERR_NOMEM;
@@ -543,7 +543,7 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
         cudaMemsetAsync(loss_, 0, sizeof(double), s);
         for (int q = 0; q < nb; ++q) {
             k_unpack_box<<<gs(V), 256, 0, s>>>(b->out + (size_t)q * V * 16, 1.0, z, V);
-            launch_maxwell_apply(s, g, oc, mu, z, e);
+            launch_maxwell_apply(s, g, oc, mu, z, e, wm);
             k_sub_loss<<<gs(L), 256, 0, s>>>(e, r + (size_t)q * L, L, 1.0 / ((double)L * nb), loss_);
             launch_maxwell_apply_t(s, g, oc, mu, e, z);
             k_pack_grad<<<gs(V), 256, 0, s>>>(z, 2.0 / ((double)L * nb), b->A0 + (size_t)q * V * 16, V);

@@ -76,37 +76,50 @@ __global__ void __launch_bounds__(256) k_wgrad(const bf16* __restrict__ x, const
 
 // 2x2x2 average pooling (NDHWC, C channels), dims of the input.
 __global__ void k_pool(const bf16* __restrict__ x, bf16* __restrict__ y, Dims di, int C) {
-    const int D2 = di.D / 2, H2 = di.H / 2, W2 = di.W / 2;
-    const long long tot = (long long)di.N * D2 * H2 * W2 * C;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(e % C);
-        long long v = e / C;
-        const int w = (int)(v % W2), h = (int)((v / W2) % H2), d = (int)((v / ((long long)W2 * H2)) % D2);
-        const long long n = v / ((long long)W2 * H2 * D2);
-        float s = 0.f;
+    // one thread per (coarse voxel, 8-channel chunk): 16-byte loads and stores, 32-bit index math
+    const int D2 = di.D / 2, H2 = di.H / 2, W2 = di.W / 2, C8 = C / 8;
+    const int tot = di.N * D2 * H2 * W2 * C8;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
+        const int c8 = e % C8, v = e / C8;
+        const int w = v % W2, h = (v / W2) % H2, d = (v / (W2 * H2)) % D2, n = v / (W2 * H2 * D2);
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int dd = 2 * d + (q >> 2), hh = 2 * h + ((q >> 1) & 1), ww = 2 * w + (q & 1);
-            s += __bfloat162float(x[(((n * di.D + dd) * di.H + hh) * di.W + ww) * C + c]);
+            const uint4 u = *reinterpret_cast<const uint4*>(
+                x + ((((long long)n * di.D + dd) * di.H + hh) * di.W + ww) * C + c8 * 8);
+            const __nv_bfloat162* p2 = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float2 f = __bfloat1622float2(p2[i]);
+                s[2 * i] += f.x;
+                s[2 * i + 1] += f.y;
+            }
         }
-        y[e] = __float2bfloat16(s * 0.125f);
+        __align__(16) __nv_bfloat162 o[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) o[i] = __floats2bfloat162_rn(s[2 * i] * 0.125f, s[2 * i + 1] * 0.125f);
+        *reinterpret_cast<uint4*>(y + (long long)v * C + c8 * 8) = *reinterpret_cast<const uint4*>(o);
     }
 }
 
 // y[v] = concat(lo[v / 2] (C1 channels, nearest upsampling), skip[v] (C2)),
-// dims of the fine level.
+// dims of the fine level.  One thread per (voxel, 8-channel chunk).
 __global__ void k_up_concat(const bf16* __restrict__ lo, const bf16* __restrict__ skip, bf16* __restrict__ y, Dims df,
                             int C1, int C2) {
-    const int C = C1 + C2;
-    const long long tot = df.vox() * C;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(e % C);
-        const long long v = e / C;
-        if (c >= C1) { y[e] = skip[v * C2 + (c - C1)]; continue; }
-        const int w = (int)(v % df.W), h = (int)((v / df.W) % df.H), d = (int)((v / ((long long)df.W * df.H)) % df.D);
-        const long long n = v / ((long long)df.W * df.H * df.D);
-        const long long vl = ((n * (df.D / 2) + d / 2) * (df.H / 2) + h / 2) * (df.W / 2) + w / 2;
-        y[e] = lo[vl * C1 + c];
+    const int C8 = (C1 + C2) / 8, L8 = C1 / 8;
+    const int tot = (int)df.vox() * C8;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
+        const int c8 = e % C8, v = e / C8;
+        uint4 u;
+        if (c8 >= L8) {
+            u = *reinterpret_cast<const uint4*>(skip + (long long)v * C2 + (c8 - L8) * 8);
+        } else {
+            const int w = v % df.W, h = (v / df.W) % df.H, d = (v / (df.W * df.H)) % df.D, n = v / (df.W * df.H * df.D);
+            const long long vl = (((long long)n * (df.D / 2) + d / 2) * (df.H / 2) + h / 2) * (df.W / 2) + w / 2;
+            u = *reinterpret_cast<const uint4*>(lo + vl * C1 + c8 * 8);
+        }
+        *reinterpret_cast<uint4*>(y + (long long)e * 8) = u;
     }
 }
 

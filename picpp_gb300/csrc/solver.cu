@@ -26,7 +26,7 @@ OpCoef make_opcoef(const GridP& g) {
 }
 
 void krylov_free(Krylov& k) {
-    cudaFree(k.V); cudaFree(k.Z); cudaFree(k.w); cudaFree(k.r); cudaFree(k.hdev); cudaFree(k.ydev);
+    cudaFree(k.V); cudaFree(k.Z); cudaFree(k.w); cudaFree(k.mx); cudaFree(k.r); cudaFree(k.hdev); cudaFree(k.ydev);
     cudaFree(k.part); cudaFree(k.scal);
     k = Krylov{};
 }
@@ -54,6 +54,7 @@ pic_status ensure(SolveCtx& c, int cap, long long L) {
     krylov_free(k);
     CKS(cudaMalloc(&k.V, sizeof(double) * (size_t)cap * L));
     CKS(cudaMalloc(&k.w, sizeof(double) * (size_t)L));
+    CKS(cudaMalloc(&k.mx, sizeof(double) * (size_t)L));
     CKS(cudaMalloc(&k.r, sizeof(double) * (size_t)L));
     CKS(cudaMalloc(&k.hdev, sizeof(double) * 2 * (size_t)(cap + 2)));
     CKS(cudaMalloc(&k.ydev, sizeof(double) * (size_t)(cap + 2)));
@@ -117,7 +118,7 @@ pic_status gmres_reference(SolveCtx& c, const OpCoef& oc, const double* rhs, dou
     double relErr = 1.0;
     const long long lim = std::min<long long>(maxIter, dim + 3);
     while (relErr > tolRel && n < lim) {
-        launch_maxwell_apply(c.s, g, oc, c.mu, Vp(n - 2), Vp(n - 1));
+        launch_maxwell_apply(c.s, g, oc, c.mu, Vp(n - 2), Vp(n - 1), k.mx);
         for (int m = 0; m < n - 1; ++m) {
             launch_dot(c.s, Vp(m), Vp(n - 1), L, k.part, P,k.hdev + m, 0);
             launch_axpy_minus_dev(c.s, Vp(n - 1), Vp(m), k.hdev + m, L);
@@ -230,7 +231,7 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
         if (rel <= tol || total >= maxIter) break;
         if (pc && restarts > 0 && rel > 0.5 * prev_rel) { pc = nullptr; fallback = true; }
         prev_rel = rel;
-        launch_div(c.s, Vp(0), k.r, beta, L);
+        launch_scale(c.s, Vp(0), k.r, 1.0 / beta, L);   // one reciprocal, not an FP64 division per element
         std::fill(gv.begin(), gv.end(), 0.0);
         gv[0] = beta;
         int j = 0;
@@ -239,18 +240,35 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             double* w = Vp(j + 1);
             if (pc) {
                 if ((st = pc->apply(c.s, g, c.mu, Vp(j), Zp(j), k.scal + 8, c.partials, c.err)) != PIC_OK) return st;
-                launch_maxwell_apply(c.s, g, oc, c.mu, Zp(j), w);
+                launch_maxwell_apply(c.s, g, oc, c.mu, Zp(j), w, k.mx);
             } else {
-                launch_maxwell_apply(c.s, g, oc, c.mu, Vp(j), w);
+                launch_maxwell_apply(c.s, g, oc, c.mu, Vp(j), w, k.mx);
             }
-            launch_multi_dot(c.s, k.V, L, j + 1, w, L, k.part, P,k.hdev);
+            // classical Gram-Schmidt; the second pass only when the first
+            // left less than 1/sqrt(2) of |w| (Kahan's "twice is enough"
+            // test): every pass is (j + 1) FP64 dot products and updates of
+            // length L, arithmetic-bound on this GPU.  w is V[j + 1], so the
+            // first multi-dot over j + 2 vectors also returns |w|^2.
+            launch_multi_dot(c.s, k.V, L, j + 2, w, L, k.part, P, k.hdev);
             launch_multi_axpy_minus(c.s, w, k.V, L, j + 1, k.hdev, 1, L);
-            launch_multi_dot(c.s, k.V, L, j + 1, w, L, k.part, P,k.hdev + (m + 2));
-            launch_multi_axpy_minus(c.s, w, k.V, L, j + 1, k.hdev + (m + 2), 1, L);
-            launch_dot(c.s, w, w, L, k.part, P,k.hdev + (j + 1), 1);
-            launch_scale_inv_dev(c.s, w, w, k.hdev + (j + 1), L);
+            launch_dot(c.s, w, w, L, k.part, P, k.scal + 2, 1);
             CKS(cudaMemcpyAsync(h1.data(), k.hdev, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, c.s));
-            CKS(cudaMemcpyAsync(h2.data(), k.hdev + (m + 2), sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, c.s));
+            double after = 0;
+            CKS(cudaMemcpyAsync(&after, k.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, c.s));
+            CKS(cudaStreamSynchronize(c.s));
+            const double before = std::sqrt(std::max(h1[j + 1], 0.0));
+            if (!(after >= 0.7071067811865476 * before)) {
+                launch_multi_dot(c.s, k.V, L, j + 1, w, L, k.part, P, k.hdev + (m + 2));
+                launch_multi_axpy_minus(c.s, w, k.V, L, j + 1, k.hdev + (m + 2), 1, L);
+                launch_dot(c.s, w, w, L, k.part, P, k.hdev + (j + 1), 1);
+                CKS(cudaMemcpyAsync(h2.data(), k.hdev + (m + 2), sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, c.s));
+                CKS(cudaMemcpyAsync(&h1[j + 1], k.hdev + (j + 1), sizeof(double), cudaMemcpyDeviceToHost, c.s));
+            } else {
+                std::fill(h2.begin(), h2.begin() + (j + 1), 0.0);
+                h1[j + 1] = after;
+                CKS(cudaMemcpyAsync(k.hdev + (j + 1), k.scal + 2, sizeof(double), cudaMemcpyDeviceToDevice, c.s));
+            }
+            launch_scale_inv_dev(c.s, w, w, k.hdev + (j + 1), L);
             CKS(cudaStreamSynchronize(c.s));
             if (pc) {
                 // a non-finite direction, or one already in the Krylov space
@@ -301,7 +319,7 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             CKS(cudaMemcpyAsync(Vp(1), k.r, sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
         }
         launch_combine(c.s, x, pc ? k.Z : k.V, L, kk, k.ydev, 1.0, 1, L);
-        launch_maxwell_apply(c.s, g, oc, c.mu, x, k.w);
+        launch_maxwell_apply(c.s, g, oc, c.mu, x, k.w, k.mx);
         launch_residual(c.s, k.r, b, k.w, L);
         ++restarts;
         if (pc) {

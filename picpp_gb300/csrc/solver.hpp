@@ -13,6 +13,7 @@ struct Krylov {
     double* V = nullptr;      // basis, cap vectors of length L
     double* Z = nullptr;      // preconditioned directions (flexible GMRES)
     double* w = nullptr;      // scratch vector
+    double* mx = nullptr;     // mu x of the operator apply
     double* r = nullptr;      // residual
     double* hdev = nullptr;   // Hessenberg column (device), 2 * (cap + 1)
     double* ydev = nullptr;   // combination coefficients

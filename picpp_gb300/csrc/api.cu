@@ -417,6 +417,19 @@ pic_status ensure_stage(pic_ctx* ctx, long long len) {
 
 constexpr long long kStageChunk = 1LL << 25;   // doubles per host transfer chunk
 
+// Host arrays that kernels can address directly (pinned or registered memory
+// under unified addressing): the conversion kernels read and write them over
+// the host link, with no staging copy and no separate conversion pass.
+bool device_addressable(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged) && a.devicePointer == p;
+}
+
 }  // namespace
 
 // ========================================================================== C ABI
@@ -620,6 +633,10 @@ pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, 
             CK(cudaMemcpyAsync(sp.a[q], src[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
             continue;
         }
+        if (device_addressable(src[q])) {
+            PK<float>::to_real_checked(s, src[q], sp.a[q], n, q < 3 ? 0 : 1, ctx->flag);
+            continue;
+        }
         for (long long b = 0; b < n; b += chunk) {
             long long len = std::min<long long>(chunk, n - b);
             CK(cudaMemcpyAsync(ctx->stage, src[q] + b, sizeof(double) * len, cudaMemcpyHostToDevice, s));
@@ -686,15 +703,19 @@ pic_status pic_download_particles(pic_ctx* ctx, int sid, long* n_out, int* cell,
     const long long chunk = std::min<long long>(kStageChunk, ctx->stage_len);
     for (int q = 0; q < 6; ++q) {
         if (!dst[q]) continue;
+        if (ctx->preal) {
+            CK(cudaMemcpyAsync(dst[q], sp.a[q], sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+            continue;
+        }
+        if (device_addressable(dst[q])) {
+            PK<float>::from_real(s, sp.a[q], dst[q], n);
+            continue;
+        }
+        // staged: the stream orders each conversion after the previous copy out of the stage
         for (long long b = 0; b < n; b += chunk) {
             long long len = std::min<long long>(chunk, n - b);
-            if (ctx->preal) {
-                CK(cudaMemcpyAsync(dst[q] + b, (double*)sp.a[q] + b, sizeof(double) * len, cudaMemcpyDeviceToHost, s));
-            } else {
-                PK<float>::from_real(s, (float*)sp.a[q] + b, ctx->stage, len);
-                CK(cudaMemcpyAsync(dst[q] + b, ctx->stage, sizeof(double) * len, cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-            }
+            PK<float>::from_real(s, (float*)sp.a[q] + b, ctx->stage, len);
+            CK(cudaMemcpyAsync(dst[q] + b, ctx->stage, sizeof(double) * len, cudaMemcpyDeviceToHost, s));
         }
     }
     return sync(ctx, "download particles");
@@ -705,21 +726,23 @@ pic_status pic_upload_fields(pic_ctx* ctx, const double* E, const double* B) {
     const long long L = 3 * ctx->g.N;
     cudaStream_t s = ctx->s;
     const double* src[2] = {E, B};
+    // each field goes to the stage buffer (3N doubles) and is checked there
+    // on the device: a non-finite value rejects it before the state changes
     for (int f = 0; f < 2; ++f) {
         if (!src[f]) continue;
-        for (long long a = 0; a < L; ++a)
-            if (!std::isfinite(src[f][a])) return fail(ctx, PIC_ERR_NUMERIC, "non-finite field value");
+        CK(cudaMemcpyAsync(ctx->stage, src[f], sizeof(double) * L, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(ctx->flag, 0, sizeof(int), s));
+        launch_nonfinite(s, ctx->stage, L, ctx->flag);
+        int bad = 0;
+        CK(cudaMemcpyAsync(&bad, ctx->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (bad) return fail(ctx, PIC_ERR_NUMERIC, "non-finite field value");
         if (is_buneman(ctx)) {
             void* dst = f == 0 ? ctx->E : ctx->B;
-            if (ctx->preal) {
-                CK(cudaMemcpyAsync(dst, src[f], sizeof(double) * L, cudaMemcpyHostToDevice, s));
-            } else {
-                CK(cudaMemcpyAsync(ctx->stage, src[f], sizeof(double) * L, cudaMemcpyHostToDevice, s));
-                PK<float>::to_real(s, ctx->stage, dst, L);
-                CK(cudaStreamSynchronize(s));
-            }
+            if (ctx->preal) CK(cudaMemcpyAsync(dst, ctx->stage, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
+            else PK<float>::to_real(s, ctx->stage, dst, L);
         } else {
-            CK(cudaMemcpyAsync(f == 0 ? ctx->Ei : ctx->Bi, src[f], sizeof(double) * L, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(f == 0 ? ctx->Ei : ctx->Bi, ctx->stage, sizeof(double) * L, cudaMemcpyDeviceToDevice, s));
         }
     }
     ctx->moments_ready = false;
@@ -737,10 +760,11 @@ pic_status pic_download_fields(pic_ctx* ctx, double* E, double* B, double* J) {
             void* src = f == 0 ? ctx->E : ctx->B;
             if (ctx->preal) {
                 CK(cudaMemcpyAsync(dst[f], src, sizeof(double) * L, cudaMemcpyDeviceToHost, s));
+            } else if (device_addressable(dst[f])) {
+                PK<float>::from_real(s, src, dst[f], L);
             } else {
                 PK<float>::from_real(s, src, ctx->stage, L);
                 CK(cudaMemcpyAsync(dst[f], ctx->stage, sizeof(double) * L, cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
             }
         } else {
             CK(cudaMemcpyAsync(dst[f], f == 0 ? ctx->Ei : ctx->Bi, sizeof(double) * L, cudaMemcpyDeviceToHost, s));

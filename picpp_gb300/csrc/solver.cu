@@ -186,8 +186,8 @@ pic_status ensure_z(SolveCtx& c, int m, long long L) {
     return PIC_OK;
 }
 
-// Restarted GMRES(m): classical Gram-Schmidt with one re-orthogonalisation,
-// Givens rotations on the host, FP64 true residual at every restart.  With
+// Restarted GMRES(m): classical Gram-Schmidt with a second pass where the
+// first one cancels, Givens rotations on the host, FP64 true residual at every restart.  With
 // a network (pc != nullptr) it is flexible GMRES (Saad 1993) with the right
 // preconditioner z_j = pc(v_j), x += Z y; a cycle that does not halve the
 // true residual, or a non-finite preconditioned direction, switches the

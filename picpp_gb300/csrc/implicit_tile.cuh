@@ -29,6 +29,9 @@ namespace pic {
 #define PIC_MOVER_THREADS 256   // threads per CTA of the tiled implicit mover (2 CTAs/SM)
 #endif
 constexpr int kImpThreads = PIC_IMP_THREADS;
+// FP64 particles keep 256 threads (128 registers): their accumulators spill at 64
+template <typename T>
+__host__ __device__ constexpr int imp_threads() { return sizeof(T) == sizeof(float) ? kImpThreads : 256; }
 constexpr int kMoverThreads = PIC_MOVER_THREADS;
 constexpr int kXposeMin = 4;   // fewest lanes of one cell that take the transpose-reduction
 
@@ -123,10 +126,21 @@ __device__ __noinline__ void imp_deposit_global(const GridP& g, int i, int j, in
             }
 }
 
+// Global trilinear gathers of E (nodes) and B (cells), out of line for the
+// staged kernel, where a particle outside its tile cannot occur after a sort.
+template <typename T>
+__device__ __noinline__ void gather_eb_global(const GridP& g, int i, int j, int k, T ox, T oy, T oz,
+                                              const T* __restrict__ E, const T* __restrict__ B, T* e, T* b) {
+    gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
+    gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, b);
+}
+
 // E and B come in the particle precision (FP32 copies for the FP32 path:
-// no FP64 conversion per gather).
-template <typename T, typename A>
-__global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP g, TileGeom t, ImpBlock bk,
+// no FP64 conversion per gather).  kStaged: E and B staged in shared memory
+// next to the accumulators (right after a sort, h = 0); a separate
+// instantiation keeps the hot loop's code small.
+template <typename T, typename A, bool kStaged>
+__global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(GridP g, TileGeom t, ImpBlock bk,
                                                                        ImpSpecies<T> S, const T* __restrict__ E,
                                                                        const T* __restrict__ B,
                                                                        double* __restrict__ J, double* __restrict__ mu,
@@ -154,7 +168,7 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
         const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
         const int x0 = ti * t.tx, y0 = tj * t.ty, z0 = tk * t.tz;
         for (int e = threadIdx.x; e < tot; e += blockDim.x) sN[e] = A(0);
-        if (bk.stage) {   // with h = 0 the blocks cover exactly the stencils of the tile's own cells
+        if (kStaged) {   // with h = 0 the blocks cover exactly the stencils of the tile's own cells
             for (int e = threadIdx.x; e < bk.NB; e += blockDim.x) {
                 const int lx = e % bk.nbx, ly = (e / bk.nbx) % bk.nby, lz = e / (bk.nbx * bk.nby);
                 const long long id = linw(g, x0 + lx, y0 + ly, z0 + lz);
@@ -205,7 +219,7 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
                             cb = (lk + hz) * csz + (lj + hy) * csy + (li + hx);
                         }
                         T e[3], bf[3];
-                        if (inb && bk.stage) {
+                        if (kStaged && inb) {
                             // node pair (c, c+1); cell pair (c-1, c) below the centre, (c, c+1) above
                             const int cbase = cb + (ox < T(0.5) ? 0 : oxc) + (oy < T(0.5) ? 0 : oyc) + (oz < T(0.5) ? 0 : ozc);
                             const T ux = ox < T(0.5) ? cwx[1] : cwx[2];
@@ -216,6 +230,8 @@ __global__ void __launch_bounds__(kImpThreads, 2) k_implicit_deposit_tile(GridP 
                                 e[c] = tri_block<T>(sE + c * bk.NB, nb, oxn, oyn, ozn, nwx[1], nwy[1], nwz[1]);
                                 bf[c] = tri_block<T>(sB + c * bk.CB, cbase, oxc, oyc, ozc, ux, uy, uz);
                             }
+                        } else if (kStaged) {
+                            gather_eb_global<T>(g, i, j, k, ox, oy, oz, E, B, e, bf);
                         } else {
                             gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
                             gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, bf);

@@ -225,14 +225,17 @@ void PK<T>::implicit_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeo
                                    double* rho, double* Pi) {
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_implicit_deposit_tile<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_implicit_deposit_tile<T, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_implicit_deposit_tile<T, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr_set = true;
     }
     const size_t smem = implicit_tile_smem(bk);
     const int per_sm = (int)((227 * 1024) / (smem + 1024));
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int grid = ntiles < kNumSM * (per_sm > 0 ? per_sm : 1) ? ntiles : kNumSM * (per_sm > 0 ? per_sm : 1);
-    k_implicit_deposit_tile<T, T><<<grid, kImpThreads, smem, s>>>(g, t, bk, S, E, B, J, mu, rho, Pi);
+    constexpr int nt = imp_threads<T>();
+    if (bk.stage) k_implicit_deposit_tile<T, T, true><<<grid, nt, smem, s>>>(g, t, bk, S, E, B, J, mu, rho, Pi);
+    else k_implicit_deposit_tile<T, T, false><<<grid, nt, smem, s>>>(g, t, bk, S, E, B, J, mu, rho, Pi);
 }
 
 template <typename T>

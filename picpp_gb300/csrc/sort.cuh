@@ -110,10 +110,21 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(int* __restrict__ a, 
         if (base + q < n) a[base + q] += add;
 }
 
+// Source index a to tmp[cursor[key[a]]++], one atomic per distinct key per
+// warp (consecutive particles mostly share a key: the input is the previous
+// sort order); the order inside a key is restored by the segment sort.
 __global__ void k_scatter_atomic(const int* __restrict__ key, long long n, int* __restrict__ cursor, int* __restrict__ tmp) {
-    for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < n; a += (long long)gridDim.x * blockDim.x) {
-        int pos = atomicAdd(&cursor[key[a]], 1);
-        tmp[pos] = (int)a;
+    const int lane = threadIdx.x & 31;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
+        const long long a = base + lane;
+        const int kk = a < n ? key[a] : -1;
+        const unsigned m = __match_any_sync(0xffffffffu, kk);
+        const int leader = __ffs(m) - 1;
+        int pos = 0;
+        if (kk >= 0 && lane == leader) pos = atomicAdd(&cursor[kk], __popc(m));
+        pos = __shfl_sync(0xffffffffu, pos, leader);
+        if (kk >= 0) tmp[pos + __popc(m & ((1u << lane) - 1u))] = (int)a;
     }
 }
 

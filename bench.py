@@ -48,6 +48,8 @@ def _args():
     p.add_argument("--implicit-ppc", type=int, default=64)
     p.add_argument("--nn-steps", type=int, default=1500, help="training steps of the learned preconditioner")
     p.add_argument("--no-implicit", action="store_true")
+    p.add_argument("--only-implicit", action="store_true",
+                   help="run and print only the implicit section (profiling the implicit step, solver and network)")
     return p.parse_args()
 
 
@@ -345,10 +347,10 @@ def run_gb300(a):
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
     # DRAM bytes of one launch from an ncu capture of the same kernel on the
-    # 64^3 case (profiles/push_deposit_tile_64cubed_ncu.md: 457.3 MB), scaled
-    # by the units a launch processes (particles and cells grow alike)
+    # 64^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 504.1 MB),
+    # scaled by the units a launch processes (particles and cells grow alike)
     units = npart / (64 ** 3 * 2 * a.ppc) if a.ppc else 0.0
-    traffic = 457.3e6 * units if (nx * ny * nz) * 2 * a.ppc == npart else None
+    traffic = 504.1e6 * units if (nx * ny * nz) * 2 * a.ppc == npart else None
     roof = {"kernel": "k_push_deposit_tile<float,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "traffic_source": "ncu dram bytes of the 64^3 launch scaled by the particles per launch",
@@ -428,6 +430,10 @@ def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.only_implicit:
+        import picpp_gb300 as P
+        P.load_library()
+        print(json.dumps({"implicit_solve": implicit_section(a)}), flush=True)
     else:
         run_gb300(a)
 

@@ -200,13 +200,17 @@ pic_status pic_load_checkpoint(pic_ctx* ctx, const char* path);
 
 /* ---- learned preconditioner --------------------------------------------- */
 /* No counterpart in the reference (PIC++ solves with plain GMRES,
- * specialmath.cpp:367-671).  A 3-level encoder-decoder of 3x3x3
- * convolutions (16/32/64 channels, ReLU, 2x2x2 average pooling, nearest
- * upsampling with skip concatenation) maps (r / s, mu_xx, mu_yy, mu_zz) to
- * x / s, s = rms(r), approximating A(mu)^-1 r; used by PIC_FGMRES_LEARNED.
+ * specialmath.cpp:367-671).  A linear 3-level encoder-decoder of 3x3x3
+ * convolutions (16/32/64 channels, no activation, 2x2x2 average pooling,
+ * nearest upsampling with skip concatenation) maps (r / s, mu_xx, mu_yy,
+ * mu_zz) to a correction c / s, s = rms(r); z = g r + c approximates
+ * A(mu)^-1 r, g a trained gate (training starts it at 1 where the identity
+ * already reduces the residual, else at 0; g = 1 with a zero network is
+ * plain GMRES); used by PIC_FGMRES_LEARNED.
  * Activations BF16, FP32 accumulation.  Input tensors have 16 channels
  * (0-2 residual, 3-5 mu diagonal, 6-15 zero), outputs 16 (0-2 used).
- * Parameters: one FP32 vector, per layer W[27][cout][cin] then b[cout]. */
+ * Parameters: one FP32 vector, per layer W[27][cout][cin] then b[cout],
+ * the gate g last. */
 typedef struct {
     int steps;                    /* Adam steps                                   */
     int batch;                    /* random fields per step                       */

@@ -9,33 +9,39 @@ definition the GPU kernels follow.
 
 Architecture: a 3-level encoder-decoder of 3x3x3 convolutions (zero
 padding 1), 16/32/64 channels, 2x2x2 average pooling down, nearest
-upsampling with skip concatenation up, ReLU after every convolution but the
-head.  Activations are NDHWC; input channels 0-2 carry the scaled residual,
-3-5 the mu diagonal (xx, yy, zz), 6-15 are zero; output channels 0-2 are the
+upsampling with skip concatenation up, no activation (every layer linear:
+the preconditioner z = r + s net(r / s, mu) is then a fixed linear operator
+for a fixed mu).  The code below keeps a per-layer ReLU flag (all False).
+Activations are NDHWC; input channels 0-2 carry the scaled residual, 3-5
+the mu diagonal (xx, yy, zz), 6-15 are zero; output channels 0-2 are the
 scaled correction, 3-15 are zero padding.
 
 Parameters are one flat FP32 vector, per layer in LAYERS order: the weights
-W[27][cout][cin] (tap = (kd*3+kh)*3+kw) followed by the bias b[cout].
+W[27][cout][cin] (tap = (kd*3+kh)*3+kw) followed by the bias b[cout]; the
+last entry is the preconditioner's identity gate g (z = g r + s net(r / s,
+mu)), which acts outside the network (its gradient here is 0).
 """
 import numpy as np
 
 LAYERS = [  # name, cin, cout, relu
-    ("e0a", 16, 16, True), ("e0b", 16, 16, True),
-    ("e1a", 16, 32, True), ("e1b", 32, 32, True),
-    ("e2a", 32, 64, True), ("e2b", 64, 64, True),
-    ("d1a", 96, 32, True), ("d1b", 32, 32, True),
-    ("d0a", 48, 16, True), ("d0b", 16, 16, True),
+    ("e0a", 16, 16, False), ("e0b", 16, 16, False),
+    ("e1a", 16, 32, False), ("e1b", 32, 32, False),
+    ("e2a", 32, 64, False), ("e2b", 64, 64, False),
+    ("d1a", 96, 32, False), ("d1b", 32, 32, False),
+    ("d0a", 48, 16, False), ("d0b", 16, 16, False),
     ("head", 16, 16, False),
 ]
 IN_CH, OUT_CH = 6, 3
 
 
 def layer_offsets():
+    """Per layer (name, cin, cout, weight offset, bias offset) and the
+    parameter count (the layers plus the gate slot at the end)."""
     off, out = 0, []
     for name, ci, co, _ in LAYERS:
         out.append((name, ci, co, off, off + 27 * co * ci))
         off += 27 * co * ci + co
-    return out, off
+    return out, off + 1
 
 
 def n_params():

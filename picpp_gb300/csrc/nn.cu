@@ -28,9 +28,9 @@ namespace {
 
 std::vector<NetLayer> make_layers() {
     std::vector<NetLayer> L = {
-        {"e0a", 16, 16, 1}, {"e0b", 16, 16, 1}, {"e1a", 16, 32, 1}, {"e1b", 32, 32, 1},
-        {"e2a", 32, 64, 1}, {"e2b", 64, 64, 1}, {"d1a", 96, 32, 1}, {"d1b", 32, 32, 1},
-        {"d0a", 48, 16, 1}, {"d0b", 16, 16, 1}, {"head", 16, 16, 0},
+        {"e0a", 16, 16, 0}, {"e0b", 16, 16, 0}, {"e1a", 16, 32, 0}, {"e1b", 32, 32, 0},
+        {"e2a", 32, 64, 0}, {"e2b", 64, 64, 0}, {"d1a", 96, 32, 0}, {"d1b", 32, 32, 0},
+        {"d0a", 48, 16, 0}, {"d0b", 16, 16, 0}, {"head", 16, 16, 0},
     };
     long long off = 0;
     for (auto& l : L) {
@@ -108,14 +108,24 @@ __global__ void k_pack_box(const double* __restrict__ r, double inv_s, const dou
     }
 }
 
-// z[c][v] = s * out[v][c], c < 3.
-__global__ void k_unpack_box(const float* __restrict__ out, double s, double* __restrict__ z, long long N) {
+// z[c][v] = g r[c][v] + s * out[v][c], c < 3: the gated identity plus the
+// network's correction (g, a parameter, at *gate).
+__global__ void k_unpack_box(const float* __restrict__ out, double s, const double* __restrict__ r,
+                             const float* __restrict__ gate, double* __restrict__ z, long long N) {
+    const double gg = (double)*gate;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < N; v += (long long)gridDim.x * blockDim.x) {
         const float* o = out + v * 16;
-        z[v] = s * (double)o[0];
-        z[N + v] = s * (double)o[1];
-        z[2 * N + v] = s * (double)o[2];
+        z[v] = gg * r[v] + s * (double)o[0];
+        z[N + v] = gg * r[N + v] + s * (double)o[1];
+        z[2 * N + v] = gg * r[2 * N + v] + s * (double)o[2];
     }
+}
+
+// dL/dg = f * sum_q <A^T (A z_q - r_q), r_q> (the dot products in d[0..nb)).
+__global__ void k_gate_grad(const double* __restrict__ d, int nb, double f, float* __restrict__ gg) {
+    double t = 0;
+    for (int q = 0; q < nb; ++q) t += d[q];
+    *gg += (float)(f * t);
 }
 
 // a *= sqrt(n) / |a| (unit root-mean-square), |a| in norm[0].
@@ -242,7 +252,7 @@ const std::vector<NetLayer>& Net::layers() {
 
 long long Net::param_count() {
     const auto& L = layers();
-    return L.back().boff + L.back().cout;
+    return L.back().boff + L.back().cout + 1;   // + the identity gate g
 }
 
 pic_status Net::buffers(cudaStream_t, int n, int d, int h, int w, bool grads, NetBuffers** out, std::string* err) {
@@ -312,14 +322,14 @@ pic_status Net::init(cudaStream_t s, unsigned long long seed, std::string* err) 
     for (size_t li = 0; li < layers().size(); ++li) {
         const auto& l = layers()[li];
         const int cin_real = li == E0A ? 6 : l.cin, cout_real = li == HEAD ? 3 : l.cout;
-        // He-normal; the head starts at zero, so the untrained network
-        // outputs 0 (relative residual loss 1) and the first steps do not
-        // drive the ReLU layers into saturation
+        // He-normal weights; the head starts at zero, so the untrained
+        // preconditioner is the identity (z = r: plain GMRES)
         const float scale = li == HEAD ? 0.f : (float)std::sqrt(2.0 / (27.0 * cin_real));
         const long long nw = 27LL * l.cin * l.cout;
         k_he_init<<<gs(nw), 256, 0, s>>>(p_ + l.woff, nw, l.cin, l.cout, cin_real, cout_real, seed * 131 + li, scale);
     }
     adam_t_ = 0;
+    gate_pending_ = true;   // g = 0 until training chooses its start
     refresh_bf16(s);
     NCK(cudaGetLastError());
     ready_ = true;
@@ -333,6 +343,7 @@ pic_status Net::set_params(cudaStream_t s, const float* host, std::string* err) 
     }
     const long long n = param_count();
     NCK(cudaMemcpyAsync(p_, host, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    gate_pending_ = false;   // the gate is part of the parameters
     NCK(cudaMemsetAsync(m_, 0, sizeof(float) * n, s));
     NCK(cudaMemsetAsync(v_, 0, sizeof(float) * n, s));
     adam_t_ = 0;
@@ -478,7 +489,7 @@ pic_status Net::apply(cudaStream_t s, const GridP& g, const double* mu, const do
     const double sc = nv / std::sqrt((double)L);
     k_pack_box<<<gs(g.N), 256, 0, s>>>(v, 1.0 / sc, mu, b->x0, g.N);
     forward(s, *b);
-    k_unpack_box<<<gs(g.N), 256, 0, s>>>(b->out, sc, z, g.N);
+    k_unpack_box<<<gs(g.N), 256, 0, s>>>(b->out, sc, v, p_ + param_count() - 1, z, g.N);
     NCK(cudaGetLastError());
     return PIC_OK;
 }
@@ -503,7 +514,8 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
         return true;
     };
     auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
-    if (!al(&r, (size_t)L * nb) || !al(&r2, L) || !al(&z, L) || !al(&e, L) || !al(&wm, L) || !al(&scal, 4)) {
+    if (!al(&r, (size_t)L * nb) || !al(&r2, L) || !al(&z, L) || !al(&e, L) || !al(&wm, L) ||
+        !al(&scal, 4 + (size_t)nb)) {
         cleanup();
         if (err) *err = "out of device memory for training";
         return PIC_ERR_NOMEM;
@@ -537,19 +549,40 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
             k_rescale_by_norm<<<gs(L), 256, 0, s>>>(rq, L, scal);
             k_pack_box<<<gs(V), 256, 0, s>>>(rq, 1.0, mu, b->x0 + (size_t)q * V * 16, V);
         }
+        if (gate_pending_) {
+            // a fresh network starts from the identity (g = 1) where the
+            // identity preconditioner already reduces the residual of the
+            // first batch's field, |A r - r| < |r|, else from zero (g = 0)
+            cudaMemsetAsync(loss_, 0, sizeof(double), s);
+            launch_maxwell_apply(s, g, oc, mu, r, e, wm);
+            k_sub_loss<<<gs(L), 256, 0, s>>>(e, r, L, 1.0 / (double)L, loss_);
+            double l1 = 0;
+            cudaMemcpyAsync(&l1, loss_, sizeof(double), cudaMemcpyDeviceToHost, s);
+            cudaError_t ce = cudaStreamSynchronize(s);
+            if (ce != cudaSuccess) { cleanup(); NCK(ce); }
+            const float g0 = l1 < 1.0 ? 1.0f : 0.0f;
+            cudaMemcpyAsync(p_ + param_count() - 1, &g0, sizeof(float), cudaMemcpyHostToDevice, s);
+            cudaStreamSynchronize(s);
+            gate_pending_ = false;
+        }
         forward(s, *b);
-        // residual loss L = mean_q |A z_q - r_q|^2 / |r_q|^2 (|r_q|^2 = 3N);
-        // dL/dz_q = 2 A^T (A z_q - r_q) / (3N nb)
+        // residual loss L = mean_q |A z_q - r_q|^2 / |r_q|^2 (|r_q|^2 = 3N),
+        // z_q = g r_q + net(r_q); dL/dnet_q = 2 A^T (A z_q - r_q) / (3N nb),
+        // dL/dg = sum_q <dL/dz_q, r_q>
+        const float* gate = p_ + param_count() - 1;
         cudaMemsetAsync(loss_, 0, sizeof(double), s);
         for (int q = 0; q < nb; ++q) {
-            k_unpack_box<<<gs(V), 256, 0, s>>>(b->out + (size_t)q * V * 16, 1.0, z, V);
+            const double* rq = r + (size_t)q * L;
+            k_unpack_box<<<gs(V), 256, 0, s>>>(b->out + (size_t)q * V * 16, 1.0, rq, gate, z, V);
             launch_maxwell_apply(s, g, oc, mu, z, e, wm);
-            k_sub_loss<<<gs(L), 256, 0, s>>>(e, r + (size_t)q * L, L, 1.0 / ((double)L * nb), loss_);
+            k_sub_loss<<<gs(L), 256, 0, s>>>(e, rq, L, 1.0 / ((double)L * nb), loss_);
             launch_maxwell_apply_t(s, g, oc, mu, e, z);
             k_pack_grad<<<gs(V), 256, 0, s>>>(z, 2.0 / ((double)L * nb), b->A0 + (size_t)q * V * 16, V);
+            launch_dot(s, z, rq, L, partials, red_blocks(L), scal + 4 + q, 0);
         }
         cudaMemsetAsync(g_, 0, sizeof(float) * param_count(), s);
         backward(s, *b);
+        k_gate_grad<<<1, 1, 0, s>>>(scal + 4, nb, 2.0 / ((double)L * nb), g_ + param_count() - 1);
         ++adam_t_;
         const float c1 = (float)(o.lr / (1.0 - std::pow((double)b1, adam_t_)));
         const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, adam_t_)));

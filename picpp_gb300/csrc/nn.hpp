@@ -1,9 +1,13 @@
-// nn.hpp -- the learned right preconditioner: a 3-level 3x3x3-convolution
-// encoder-decoder (16/32/64 channels, 6 input channels: residual and mu
-// diagonal; 3 output channels: the correction), BF16 activations with FP32
-// accumulation, trained on the device with its own forward, backward and
-// Adam kernels.  The FP64 numpy restatement in the oracle defines the same
-// network and parameter layout.
+// nn.hpp -- the learned right preconditioner z = g r + s net(r / s, mu
+// diagonal), g a trained gate (the last parameter; training starts it at 1
+// where the identity already reduces the residual, else at 0): a 3-level
+// 3x3x3-convolution encoder-decoder (16/32/64
+// channels, 6 input channels: residual and mu diagonal; 3 output channels:
+// the correction), linear (no activation: with mu fixed during a solve the
+// preconditioner is a fixed linear operator, as flexible GMRES converges
+// best with), BF16 activations with FP32 accumulation, trained on the
+// device with its own forward, backward and Adam kernels.  The FP64 numpy
+// restatement in the oracle defines the same network and parameter layout.
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
@@ -16,7 +20,7 @@ namespace pic {
 
 struct NetLayer {
     const char* name;
-    int cin, cout, relu;
+    int cin, cout, relu;   // relu: 0 for every layer of this network
     long long woff, boff;   // offsets of W[27][cout][cin] and b[cout] in the parameter vector
 };
 
@@ -44,13 +48,14 @@ public:
     // Loss and parameter gradient for host input and target [..][3].
     pic_status loss_grad_host(cudaStream_t s, int n, int d, int h, int w, const float* x0, const float* target,
                               double* loss, float* grad, std::string* err);
-    // z = s * net(v / s, mu diagonal) on the box (FP64 planar vectors of 3N).
+    // z = g v + s * net(v / s, mu diagonal) on the box (FP64 planar vectors of 3N).
     pic_status apply(cudaStream_t s, const GridP& g, const double* mu, const double* v, double* z, double* scal,
                      double* partials, std::string* err);
     // Training on the box's operator A(mu): random fields r of unit rms
     // (white noise after 0 .. smooth_max binomial passes), loss
-    // |A z - r|^2 / |r|^2 with z = net(r, mu diagonal); its gradient
-    // 2 A^T (A z - r) / |r|^2 (k_maxwell_apply_t) seeds the backward pass.
+    // |A z - r|^2 / |r|^2 with z = g r + net(r, mu diagonal); its gradient
+    // 2 A^T (A z - r) / |r|^2 (k_maxwell_apply_t) seeds the backward pass
+    // and, dotted with r, gives the gate's.
     pic_status train(cudaStream_t s, const GridP& g, const double* mu, const pic_train_opts& o, pic_train_info* info,
                      double* partials, std::string* err);
 
@@ -65,6 +70,7 @@ private:
     double* loss_ = nullptr;
     int* tc_err_ = nullptr;   // set by a convolution whose MMA completion wait ran out
     int adam_t_ = 0;
+    bool gate_pending_ = false;   // fresh network: training picks the gate's start
     bool ready_ = false;
     std::vector<NetBuffers*> bufs_;
 };

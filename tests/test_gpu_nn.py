@@ -141,11 +141,30 @@ def test_operator_transpose_is_the_adjoint(pg, shape):
 
 
 def test_fgmres_falls_back_to_plain_gmres(pg):
+    """A network whose directions are not finite (NaN parameters) ends its
+    cycle; the solve finishes with plain GMRES to the same tolerance."""
     box, mu, rhs = hard_operator(8, seed=12)
     sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
-    sim.nn_set_params(np.zeros(pg.load_library().pic_nn_param_count(), dtype=np.float32))
+    sim.nn_set_params(np.full(pg.load_library().pic_nn_param_count(), np.nan, dtype=np.float32))
     x, info = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.FGMRES_LEARNED, restart=20, max_iter=3000, tol=1e-8))
     assert info["used_fallback"] == 1
+    r = O.maxwell_apply(O.make_grid(box), mu, x) - rhs
+    assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1.01e-8
+
+
+def test_gate_alone_is_the_identity_preconditioner(pg):
+    """Zero network, gate 1: z = r, so FGMRES takes the same iterations as
+    plain GMRES and reaches the same tolerance."""
+    box, mu, rhs = hard_operator(8, seed=14)
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    p = np.zeros(pg.load_library().pic_nn_param_count(), dtype=np.float32)
+    p[-1] = 1.0
+    sim.nn_set_params(p)
+    opts = dict(restart=20, max_iter=3000, tol=1e-8)
+    _, plain = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.GMRES_RESTARTED, **opts))
+    x, learned = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.FGMRES_LEARNED, **opts))
+    assert learned["used_fallback"] == 0
+    assert abs(learned["iterations"] - plain["iterations"]) <= 1, (learned, plain)
     r = O.maxwell_apply(O.make_grid(box), mu, x) - rhs
     assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1.01e-8
 

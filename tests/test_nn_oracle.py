@@ -18,7 +18,8 @@ def _case(seed=0, shape=(2, 4, 4, 8)):
 
 
 def test_parameter_count_and_flops():
-    assert NN.n_params() == sum(27 * ci * co + co for _, ci, co, _ in NN.LAYERS)
+    # the layers plus the preconditioner's identity gate
+    assert NN.n_params() == sum(27 * ci * co + co for _, ci, co, _ in NN.LAYERS) + 1
     assert 1.0e5 < NN.flops_per_voxel() < 1.5e5
 
 

@@ -92,6 +92,20 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, float v[8]) {
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 16-byte asynchronous copy global -> shared through L1 (neighbouring bricks
+// share their halos, every CTA the weights); src_bytes = 0 writes zeros
+// (the halo outside the box).  All of a thread's copies are in flight at
+// once instead of one load-store round trip per item.
+__device__ __forceinline__ void tc_cp16(void* dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_cp_wait_all() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 
@@ -132,15 +146,14 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __nv_bfloat16* __
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    // input brick: voxels (d0 - 1 .. d0 + 1, h0 - 1 .. h0 + 16, w0 - 1 .. w0 + 8), 16 bytes per access
+    // input brick: voxels (d0 - 1 .. d0 + 1, h0 - 1 .. h0 + 16, w0 - 1 .. w0 + 8), 16 bytes per copy
     for (int e = threadIdx.x; e < kTcBV * C8; e += kTcThreads) {
         const int bv = e / C8, c8 = e - bv * C8;
         const int bw = bv % kTcBW, bh = (bv / kTcBW) % kTcBH, bd = bv / (kTcBW * kTcBH);
         const int d = d0 - 1 + bd, h = h0 - 1 + bh, w = w0 - 1 + bw;
-        uint4 val = make_uint4(0, 0, 0, 0);
-        if (d >= 0 && d < dD && h >= 0 && h < dH && w >= 0 && w < dW)
-            val = *reinterpret_cast<const uint4*>(x + ((((long long)n * dD + d) * dH + h) * dW + w) * CIN + c8 * 8);
-        *reinterpret_cast<uint4*>(sA + ((size_t)c8 * kTcBV + bv) * 8) = val;
+        const bool in = d >= 0 && d < dD && h >= 0 && h < dH && w >= 0 && w < dW;
+        const __nv_bfloat16* src = in ? x + ((((long long)n * dD + d) * dH + h) * dW + w) * CIN + c8 * 8 : x;
+        tc_cp16(sA + ((size_t)c8 * kTcBV + bv) * 8, src, in ? 16 : 0);
     }
     tc_fence_before();
     __syncthreads();
@@ -156,10 +169,10 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __nv_bfloat16* __
         for (int e = threadIdx.x; e < kTapsPerStage * COUT * C8; e += kTcThreads) {
             const int row = e / C8, c8 = e - row * C8;   // row = tap' * COUT + co
             const int tp = row / COUT, co = row - tp * COUT;
-            *reinterpret_cast<uint4*>(sW + (((size_t)tp * C8 + c8) * COUT + co) * 8) =
-                *reinterpret_cast<const uint4*>(wsrc + (size_t)row * CIN + c8 * 8);
+            tc_cp16(sW + (((size_t)tp * C8 + c8) * COUT + co) * 8, wsrc + (size_t)row * CIN + c8 * 8, 16);
         }
-        // generic-proxy stores -> visible to the tensor cores
+        tc_cp_wait_all();   // this stage's weights (and, at stage 0, the brick) in shared memory
+        // generic-proxy writes -> visible to the tensor cores
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         tc_fence_before();
         __syncthreads();

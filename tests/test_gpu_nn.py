@@ -53,11 +53,14 @@ def sim_box(pg, n=8):
     return pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
 
 
-def test_forward_matches_oracle(pg):
+# boxes smaller than one 1 x 16 x 8 output brick and spanning several, with
+# ragged edges
+@pytest.mark.parametrize("shape", [(1, 8, 8, 16), (1, 4, 20, 24)])
+def test_forward_matches_oracle(pg, shape):
     sim = sim_box(pg)
     p = params(3)
     sim.nn_set_params(p)
-    x0 = net_input((1, 8, 8, 16), 4)
+    x0 = net_input(shape, 4)
     out = sim.nn_forward(x0)
     ref = NN.forward(p.astype(np.float64), bf16(x0).astype(np.float64))
     # BF16 activations between layers, FP32 accumulation
@@ -70,8 +73,9 @@ def test_gradients_match_oracle(pg):
     sim = sim_box(pg)
     p = params(5)
     sim.nn_set_params(p)
-    x0 = net_input((2, 16, 16, 16), 6)
-    t = np.random.default_rng(7).standard_normal((2, 16, 16, 16, 3)).astype(np.float32)
+    # level 0 (16 x 20 x 16): two output bricks in h, the second ragged
+    x0 = net_input((2, 16, 20, 16), 6)
+    t = np.random.default_rng(7).standard_normal((2, 16, 20, 16, 3)).astype(np.float32)
     L, g = sim.nn_loss_grad(x0, t)
     xb = bf16(x0).astype(np.float64)
     # the restatement rounding where the device rounds (weights, stored

@@ -33,7 +33,7 @@ constexpr unsigned kTcWaitLimit = 1u << 22;               // mbarrier polls befo
 // All 27 taps of weights staged at once when they fit next to the brick;
 // otherwise one kd plane (9 taps) at a time.
 __host__ __device__ constexpr bool tc_all_taps(int cin, int cout) {
-    return (27 * (size_t)cin * cout + (size_t)cin * kTcBV) * 2 <= 100 * 1024;
+    return (27 * (size_t)cin * cout + (size_t)cin * kTcBV) * 2 <= 64 * 1024;
 }
 __host__ __device__ constexpr size_t tc_conv_smem_bytes(int cin, int cout) {
     return ((size_t)cin * kTcBV + (tc_all_taps(cin, cout) ? 27 : 9) * (size_t)cin * cout) * 2;

@@ -108,7 +108,66 @@ def implicit_section(a):
     if a.nn_steps > 0:
         out["learned_vs_plain"] = learned_solve(a, sim, box, w, opts)
     sim.close()
+    if a.nn_steps > 0:
+        out["learned_vs_plain_stiff"] = stiff_solve(a, w)
     return out
+
+
+def _beams(box, ppc, w, seeds):
+    """A simulation of the implicit beam plasma on box (device fill), with
+    the uniform B0 along z; particles and fields as in implicit_section."""
+    import math
+    import numpy as np
+    import picpp_gb300 as P
+    sim = P.GpuSimulation(box, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=1)
+    N = box.ncells
+    sim.add_species(-1.0, 1.0, w, N * ppc)
+    sim.add_species(1.0, 25.0, w, N * ppc)
+    sim.fill_species(0, ppc, seeds[0], 0.01, 10.0, True)
+    sim.fill_species(1, ppc, seeds[1], 0.01 / 25.0, 10.0, True)
+    E = np.zeros((3, box.nz, box.ny, box.nx))
+    B = np.zeros((3, box.nz, box.ny, box.nx))
+    B[2] = math.sqrt(4 * math.pi * 0.01 * (1.0 / (4 * math.pi)) * 26.0 * 10.0)
+    sim.upload_fields(E, B)
+    return sim
+
+
+def stiff_solve(a, w):
+    """The same plasma and grid with dt = 2 (K / dx^2 = (c' theta dt / dx)^2
+    ~ 4.2 instead of 0.26): the system of the first implicit step solved to
+    an FP64 relative residual of 1e-8 with plain GMRES(30) and with
+    FGMRES(30) + the network trained on a 64x64x16 box of it (white-noise
+    fields).  A regime where the preconditioner has work to do; the
+    headline comparison is learned_vs_plain (dt = 0.5)."""
+    import picpp_gb300 as P
+    from picpp_gb300 import initstate as I
+    nx, ny, nz = a.implicit_grid
+    ppc = a.implicit_ppc
+    box = I.Box(nx, ny, nz, 0.5, 0.5, 0.5, 2.0, theta=0.5)
+    tb = I.Box(64, 64, 16, 0.5, 0.5, 0.5, 2.0, theta=0.5)
+    tsim = _beams(tb, ppc, w, (33, 34))
+    tsim.updateElectroMagneticParameters()
+    tsim.nn_init(1)
+    tr = tsim.nn_train(steps=a.nn_steps, batch=2, lr=1e-3, seed=3, smooth_max=0)
+    params = tsim.nn_get_params()
+    tsim.close()
+    sim = _beams(box, ppc, w, (23, 24))
+    sim.nn_set_params(params)
+    sim.updateElectroMagneticParameters()
+    _, mu, _, rhs = sim.download_moments()
+    plain_opts = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=3000, tol=1e-8)
+    learned_opts = P.solve_opts(P.FGMRES_LEARNED, restart=30, max_iter=3000, tol=1e-8)
+    sim.maxwell_solve(mu, rhs, plain_opts)   # warm-up of both paths
+    sim.maxwell_solve(mu, rhs, learned_opts)
+    _, ip = sim.maxwell_solve(mu, rhs, plain_opts)
+    _, il = sim.maxwell_solve(mu, rhs, learned_opts)
+    sim.close()
+    return {"system": f"first implicit step, {nx}x{ny}x{nz}, dt = 2 (K/dx^2 = 4.2)", "tol": 1e-8,
+            "plain": {k: ip[k] for k in ("iterations", "restarts", "rel_residual", "seconds")},
+            "learned": {k: il[k] for k in ("iterations", "restarts", "used_fallback", "rel_residual", "seconds")},
+            "speedup": ip["seconds"] / il["seconds"] if il["seconds"] > 0 else None,
+            "train": {"box": [64, 64, 16], "steps": tr["steps"], "seconds": tr["seconds"],
+                      "first_loss": tr["first_loss"], "last_loss": tr["last_loss"]}}
 
 
 NET_LAYERS = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1),

@@ -395,6 +395,75 @@ def test_bad_inputs_are_rejected(pg):
     assert e.value.status == 5
 
 
+def test_pinned_host_arrays_match_the_staged_path(pg):
+    """Pinned host arrays are read and written by the conversion kernels
+    directly; pageable ones go through the staging buffer.  Both give the
+    same device state and the same downloads, bit for bit, and both reject
+    invalid offsets."""
+    import ctypes as C
+    import torch
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=3, seed=41))
+    keys = ("ox", "oy", "oz", "px", "py", "pz")
+
+    def pinned_copy(a, dtype):
+        t = torch.empty(a.shape, dtype=dtype, pin_memory=True).numpy()
+        t[...] = a
+        return t
+
+    ref = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=0, sort_every=1)
+    ref.upload_state(st)
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=0, sort_every=1)
+    for s, sp in enumerate(st.species):
+        sim.add_species(sp["q"], sp["m"], sp["w"], len(sp["cell"]))
+        d = {k: pinned_copy(np.asarray(sp[k], np.float64), torch.float64) for k in keys}
+        d["cell"] = pinned_copy(np.asarray(sp["cell"], np.int32), torch.int32)
+        sim.upload_particles(s, d)
+    sim.upload_fields(pinned_copy(st.E, torch.float64), pinned_copy(st.B, torch.float64))
+    for s in (ref, sim):
+        s.buneman_step(2)
+    L = sim.L
+    dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    for sid, sp in enumerate(st.species):
+        n = len(sp["cell"])
+        out = {k: pinned_copy(np.zeros(n), torch.float64) for k in keys}
+        cell = pinned_copy(np.zeros(n, np.int32), torch.int32)
+        sim._ck(L.pic_download_particles(sim.ctx, sid, None, cell.ctypes.data_as(C.POINTER(C.c_int)),
+                                         *[dp(out[k]) for k in keys], None))
+        r = ref.download_particles(sid, with_ids=False)
+        assert np.array_equal(cell, r["cell"])
+        for k in keys:
+            assert np.array_equal(out[k], r[k]), k
+    E = pinned_copy(np.zeros_like(st.E), torch.float64)
+    B = pinned_copy(np.zeros_like(st.B), torch.float64)
+    J = pinned_copy(np.zeros_like(st.E), torch.float64)
+    sim._ck(L.pic_download_fields(sim.ctx, dp(E), dp(B), dp(J)))
+    Er, Br, Jr = ref.download_fields()
+    assert np.array_equal(E, Er) and np.array_equal(B, Br) and np.array_equal(J, Jr)
+    # invalid offsets are rejected on the direct path too
+    sp = st.species[0]
+    bad = {k: pinned_copy(np.asarray(sp[k], np.float64), torch.float64) for k in keys}
+    bad["ox"][0] = 1.0
+    bad["cell"] = pinned_copy(np.asarray(sp["cell"], np.int32), torch.int32)
+    with pytest.raises(pg.PicError) as e:
+        sim.upload_particles(0, bad)
+    assert e.value.status == 1
+
+
+def test_rejected_field_upload_keeps_the_fields(pg):
+    """A non-finite value is found on the device before the fields change."""
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=1, seed=42))
+    for real in (0, 1):
+        sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real)
+        sim.upload_state(st)
+        E0, B0, _ = sim.download_fields()
+        E = st.E.copy(); E[1, 2, 3, 4] = np.nan
+        with pytest.raises(pg.PicError) as e:
+            sim.upload_fields(E, st.B)
+        assert e.value.status == 5
+        E1, B1, _ = sim.download_fields()
+        assert np.array_equal(E0, E1) and np.array_equal(B0, B1)
+
+
 def test_empty_species_and_no_particles(pg):
     st = noisy(I.buneman_plasma(8, 8, 8, ppc=1, seed=36))
     sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, sort_every=1)

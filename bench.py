@@ -47,6 +47,7 @@ def _args():
     p.add_argument("--implicit-grid", type=int, nargs=3, default=[256, 256, 64])
     p.add_argument("--implicit-ppc", type=int, default=64)
     p.add_argument("--nn-steps", type=int, default=1500, help="training steps of the learned preconditioner")
+    p.add_argument("--nn-batch", type=int, default=4, help="random fields per training step (Adam, lr 1e-3)")
     p.add_argument("--no-implicit", action="store_true")
     p.add_argument("--only-implicit", action="store_true",
                    help="run and print only the implicit section (profiling the implicit step, solver and network)")
@@ -148,7 +149,7 @@ def stiff_solve(a, w):
     tsim = _beams(tb, ppc, w, (33, 34))
     tsim.updateElectroMagneticParameters()
     tsim.nn_init(1)
-    tr = tsim.nn_train(steps=a.nn_steps, batch=2, lr=1e-3, seed=3, smooth_max=0)
+    tr = tsim.nn_train(steps=a.nn_steps, batch=a.nn_batch, lr=1e-3, seed=3, smooth_max=0)
     params = tsim.nn_get_params()
     tsim.close()
     sim = _beams(box, ppc, w, (23, 24))
@@ -198,7 +199,7 @@ def learned_solve(a, sim, box, w, opts):
     tsim.implicit_step(opts)
     tsim.updateElectroMagneticParameters()
     tsim.nn_init(1)
-    tr = tsim.nn_train(steps=a.nn_steps, batch=2, lr=1e-3, seed=3, smooth_max=2)
+    tr = tsim.nn_train(steps=a.nn_steps, batch=a.nn_batch, lr=1e-3, seed=3, smooth_max=2)
     params = tsim.nn_get_params()
     tsim.close()
     sim.nn_set_params(params)

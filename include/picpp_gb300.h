@@ -219,7 +219,9 @@ typedef struct {
     int smooth_max;               /* fields get 0..smooth_max binomial passes     */
 } pic_train_opts;
 typedef struct {
-    double first_loss, last_loss; /* relative residual loss of the first / last step */
+    double first_loss, last_loss; /* relative residual loss of the first step / of the
+                                     returned parameters (the lowest loss seen at a check
+                                     every 50 steps, restored if the run degraded later) */
     double seconds;               /* device time                                  */
     int steps;
 } pic_train_info;

@@ -514,8 +514,14 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
         return true;
     };
     auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+    float *best_p = nullptr, *prev_p = nullptr;
+    auto alf = [&](float** p, size_t n) -> bool {
+        if (cudaMalloc((void**)p, sizeof(float) * n) != cudaSuccess) return false;
+        tmp.push_back(*p);
+        return true;
+    };
     if (!al(&r, (size_t)L * nb) || !al(&r2, L) || !al(&z, L) || !al(&e, L) || !al(&wm, L) ||
-        !al(&scal, 4 + (size_t)nb)) {
+        !al(&scal, 4 + (size_t)nb) || !alf(&best_p, param_count()) || !alf(&prev_p, param_count())) {
         cleanup();
         if (err) *err = "out of device memory for training";
         return PIC_ERR_NOMEM;
@@ -532,7 +538,12 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    double first = 0, last = 0;
+    double first = 0, last = 0, best = INFINITY;
+    // every kCheck steps (and at both ends) the batch loss is read; the
+    // parameters of the lowest checked loss are kept on the device and
+    // restored at the end if the run degraded from there (Adam at a constant
+    // rate can diverge late in long runs)
+    constexpr int kCheck = 50;
     const int steps = o.steps > 0 ? o.steps : 1;
     for (int it = 0; it < steps; ++it) {
         // nb random fields r (white noise after 0 .. smooth_max binomial
@@ -583,19 +594,32 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
         cudaMemsetAsync(g_, 0, sizeof(float) * param_count(), s);
         backward(s, *b);
         k_gate_grad<<<1, 1, 0, s>>>(scal + 4, nb, 2.0 / ((double)L * nb), g_ + param_count() - 1);
+        const bool check = it == 0 || it == steps - 1 || it % kCheck == kCheck - 1;
+        if (check) cudaMemcpyAsync(prev_p, p_, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
         ++adam_t_;
         const float c1 = (float)(o.lr / (1.0 - std::pow((double)b1, adam_t_)));
         const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, adam_t_)));
         nn::k_adam<<<gs(param_count()), 256, 0, s>>>(p_, g_, m_, v_, param_count(), b1, b2, eps, c1, c2);
         refresh_bf16(s);
-        if (it == 0 || it == steps - 1) {
+        if (check) {
             double lv = 0;
             cudaMemcpyAsync(&lv, loss_, sizeof(double), cudaMemcpyDeviceToHost, s);
             cudaError_t ce = cudaStreamSynchronize(s);
             if (ce != cudaSuccess) { cleanup(); NCK(ce); }
             if (it == 0) first = lv;
             last = lv;
+            if (std::isfinite(lv) && lv < best) {
+                best = lv;
+                // the loss was measured before this step's update: keep the
+                // parameters that produced it
+                cudaMemcpyAsync(best_p, prev_p, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
+            }
         }
+    }
+    if (!(last <= best) && std::isfinite(best)) {
+        cudaMemcpyAsync(p_, best_p, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
+        refresh_bf16(s);
+        last = best;
     }
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);

@@ -46,7 +46,7 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--implicit-grid", type=int, nargs=3, default=[256, 256, 64])
     p.add_argument("--implicit-ppc", type=int, default=64)
-    p.add_argument("--nn-steps", type=int, default=1500, help="training steps of the learned preconditioner")
+    p.add_argument("--nn-steps", type=int, default=4000, help="training steps of the learned preconditioner")
     p.add_argument("--nn-batch", type=int, default=4, help="random fields per training step (Adam, lr 1e-3)")
     p.add_argument("--no-implicit", action="store_true")
     p.add_argument("--only-implicit", action="store_true",

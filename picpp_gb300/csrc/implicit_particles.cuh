@@ -69,6 +69,16 @@ __device__ __forceinline__ void alpha_tensor(T beta, const T v[3], T gamma, cons
         }
 }
 
+// Picard stopping rule of moveParticle (mover.cpp:222-223, 292): momentum
+// change below 1e-14 |p| and position change below 1e-8 dx.  For the FP32
+// push the thresholds are at least 4 ulp: 1e-14 lies below FP32 resolution,
+// which would run every particle through all three iterations although the
+// last ones only change rounding.
+template <typename T> __device__ __forceinline__ T picard_mom_tol() { return T(1e-14); }
+template <> __device__ __forceinline__ float picard_mom_tol<float>() { return 4.8e-7f; }
+template <typename T> __device__ __forceinline__ T picard_pos_tol() { return T(1e-8); }
+template <> __device__ __forceinline__ float picard_pos_tol<float>() { return 4.8e-7f; }
+
 template <typename T>
 __device__ __forceinline__ void gamma_vel(const T mom[3], T m, T& gam, T v[3]) {
     T p2 = mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2];
@@ -216,7 +226,7 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
         T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
         T prevDisp[3];
         int it = 0;
-        while (err > T(1e-14) * momNorm && cerr > T(1e-8) * dxT && it < 3) {
+        while (err > picard_mom_tol<T>() * momNorm && cerr > picard_pos_tol<T>() * dxT && it < 3) {
             ++it;
             T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
 #pragma unroll

@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
                 T prevDisp[3];
                 int it = 0;
-                while (err > T(1e-14) * momNorm && cerr > T(1e-8) * dxT && it < 3) {
+                while (err > picard_mom_tol<T>() * momNorm && cerr > picard_pos_tol<T>() * dxT && it < 3) {
                     ++it;
                     const T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
 #pragma unroll

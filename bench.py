@@ -232,6 +232,25 @@ def _dist():
     return rank, world, local
 
 
+def max_over_ranks(x, world):
+    """The slowest rank's time: an all-reduce MAX over the process group
+    (CUDA tensor under NCCL, CPU tensor under gloo); x itself for one rank."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(particles_per_rank, world, ms_per_step):
+    """Whole-job particle-steps/s of world replicas, each with
+    particles_per_rank particles, from the slowest rank's ms per step."""
+    return particles_per_rank * world / (ms_per_step * 1e-3)
+
+
 # ---------------------------------------------------------------- CPU side
 def _oracle_worker(args):
     """One replica of the oracle on a bounded sample box (spawned process)."""
@@ -383,13 +402,9 @@ def run_gb300(a):
     e1.synchronize()
     barrier()
     ck = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
     ms_step = ms / a.steps
-    value = npart * world / (ms_step * 1e-3)
+    value = replica_value(npart, world, ms_step)
 
     # phase breakdown of the same workload, a separate profiled pass
     sim.profile(True)
@@ -459,8 +474,8 @@ def run_gb300(a):
     f1.record(stream)
     f1.synchronize()
     barrier()
-    e2e_ms = f0.elapsed_time(f1) / a.e2e_steps
-    e2e_val = npart * world / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(f0.elapsed_time(f1), world) / a.e2e_steps
+    e2e_val = replica_value(npart, world, e2e_ms)
 
     sim.close()
     imp = None

@@ -13,14 +13,37 @@
 
 namespace pic {
 
+// kGatherBatch destinations per thread per pass: their permutation entries
+// and then their 8 x kGatherBatch payload loads are all in flight together
+// (one pass is otherwise two dependent memory latencies for 32 bytes).
+constexpr int kGatherBatch = 4;
 template <typename T>
 __global__ void k_gather_payload(const int* __restrict__ perm, long long n, PartView<T> src, PartView<T> dst) {
-    for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n; d += (long long)gridDim.x * blockDim.x) {
-        int s = perm[d];
-        dst.cell[d] = src.cell[s];
-        dst.ox[d] = src.ox[s]; dst.oy[d] = src.oy[s]; dst.oz[d] = src.oz[s];
-        dst.px[d] = src.px[s]; dst.py[d] = src.py[s]; dst.pz[d] = src.pz[s];
-        dst.id[d] = src.id[s];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long d0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; d0 < n; d0 += stride * kGatherBatch) {
+        int s[kGatherBatch];
+#pragma unroll
+        for (int k = 0; k < kGatherBatch; ++k) {
+            const long long d = d0 + k * stride;
+            s[k] = d < n ? perm[d] : -1;
+        }
+        int cell[kGatherBatch], id[kGatherBatch];
+        T v[6][kGatherBatch];
+#pragma unroll
+        for (int k = 0; k < kGatherBatch; ++k) {
+            if (s[k] < 0) continue;
+            cell[k] = src.cell[s[k]]; id[k] = src.id[s[k]];
+            v[0][k] = src.ox[s[k]]; v[1][k] = src.oy[s[k]]; v[2][k] = src.oz[s[k]];
+            v[3][k] = src.px[s[k]]; v[4][k] = src.py[s[k]]; v[5][k] = src.pz[s[k]];
+        }
+#pragma unroll
+        for (int k = 0; k < kGatherBatch; ++k) {
+            if (s[k] < 0) continue;
+            const long long d = d0 + k * stride;
+            dst.cell[d] = cell[k]; dst.id[d] = id[k];
+            dst.ox[d] = v[0][k]; dst.oy[d] = v[1][k]; dst.oz[d] = v[2][k];
+            dst.px[d] = v[3][k]; dst.py[d] = v[4][k]; dst.pz[d] = v[5][k];
+        }
     }
 }
 

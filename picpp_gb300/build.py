@@ -24,7 +24,7 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
                  # register budget of the fused explicit kernel: CTAs per SM
                  f"-DPIC_TILE_MIN_BLOCKS={int(os.environ.get('PICPP_TILE_MIN_BLOCKS', '2'))}",
                  f"-DPIC_TILE_THREADS={int(os.environ.get('PICPP_TILE_THREADS', '512'))}",
-                 f"-DPIC_IMP_THREADS={int(os.environ.get('PICPP_IMP_THREADS', '512'))}",
+                 f"-DPIC_IMP_THREADS={int(os.environ.get('PICPP_IMP_THREADS', '256'))}",
                  f"-DPIC_MOVER_THREADS={int(os.environ.get('PICPP_MOVER_THREADS', '256'))}"]
 UNITS = {
     "api.cu": [],

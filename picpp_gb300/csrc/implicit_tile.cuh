@@ -10,10 +10,12 @@
 // A warp takes one cell key at a time and walks its particles 32 at a time.
 // Lanes holding the same (current) cell share one stencil base, so their
 // 96 node and 189 cell products (27 slots, zero weight outside the
-// particle's octant) are summed with a butterfly transpose-reduction: after
-// five exchange rounds lane L holds the warp total of product L of a
-// 32-product pass, and adds it to shared memory with one atomic.  Runs of
-// only a few lanes add their products directly; particles more than h cells
+// particle's octant) are summed over the run before one shared-memory atomic
+// per sum: with FP32 accumulators as small TF32 tensor-core products at FP32
+// accuracy (tc_run_sums), with FP64 accumulators by a butterfly
+// transpose-reduction (after five exchange rounds lane L holds the warp total
+// of product L of a 32-product pass).  Runs of only a few lanes add their
+// products directly; particles more than h cells
 // outside the tile add theirs to the FP64 grids with global atomics.  The
 // tile's block is finally added to the FP64 grids (global atomics only on
 // block entries, 22 per node/cell).
@@ -23,7 +25,7 @@
 namespace pic {
 
 #ifndef PIC_IMP_THREADS
-#define PIC_IMP_THREADS 512   // threads per CTA of the tiled implicit deposit (2 CTAs/SM, 64 registers)
+#define PIC_IMP_THREADS 256   // threads per CTA of the tiled implicit deposit (2 CTAs/SM, 128 registers)
 #endif
 #ifndef PIC_MOVER_THREADS
 #define PIC_MOVER_THREADS 256   // threads per CTA of the tiled implicit mover (2 CTAs/SM)
@@ -89,6 +91,151 @@ __device__ __forceinline__ T tri_block(const T* __restrict__ F, int base, int sx
     return uz * (uy * (ux * F[base] + wx * F[base + sx]) + wy * (ux * F[base + sy] + wx * F[base + sy + sx])) +
            wz * (uy * (ux * F[base + sz] + wx * F[base + sz + sx]) +
                  wy * (ux * F[base + sz + sy] + wx * F[base + sz + sy + sx]));
+}
+
+// ---- tensor-core reduction of one run (FP32 accumulators) -------------------
+// The 96 node sums  N[q][c] = sum_p QN_p[q] wn_p[c]  and 189 cell sums
+// C[s][q] = sum_p wc_p[s] QC_p[q]  of a run of particles are small matrix
+// products with the particles as the inner dimension.  Each lane writes its
+// particle's raw quantities (rv 3, alpha 9, per-axis node weights 2 x 3,
+// per-axis cell weights 3 x 3) to a per-warp scratch of 16 rows; the warp
+// then runs m16n8k8 TF32 MMAs, eight particles per MMA, in the 3 x TF32 form
+// (x = hi + lo, products hi*hi + hi*lo + lo*hi, FP32 accumulation), which
+// keeps the sums at FP32 accuracy.  The per-species factors (cq, cm) are
+// applied to the sums.
+constexpr int kScrRow = 27;         // scratch floats per particle
+constexpr int kScrParticles = 16;   // scratch rows per warp
+
+// Round to the 19-bit TF32 format (ties away from zero); low 13 bits zero.
+__device__ __forceinline__ unsigned tf32_round(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
+
+__device__ __forceinline__ void tf32_split(float x, unsigned& hi, unsigned& lo) {
+    hi = tf32_round(x);
+    lo = tf32_round(x - __uint_as_float(hi));
+}
+
+// D (16x8, FP32) += A (16x8, TF32, row) * B (8x8, TF32, col)
+__device__ __forceinline__ void mma_tf32(float d[4], const unsigned a[4], const unsigned b[2]) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// D += A * B at FP32 accuracy from pre-split B
+__device__ __forceinline__ void mma_tf32x3(float d[4], const float a[4], const unsigned bh[2], const unsigned bl[2]) {
+    unsigned ah[4], al[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) tf32_split(a[i], ah[i], al[i]);
+    mma_tf32(d, al, bh);
+    mma_tf32(d, ah, bl);
+    mma_tf32(d, ah, bh);
+}
+
+// Cell-slot weight of scratch row P for slot s (x fastest, three per axis).
+__device__ __forceinline__ float slot_w(const float* P, int s) {
+    return P[18 + s % 3] * P[21 + (s / 3) % 3] * P[24 + s / 9];
+}
+
+// Sums of one run over the warp: mem = lanes in the run; row = this lane's
+// raw quantities (written only when the lane is in the run).  On return,
+// lane (g = lane/4, t = lane%4) holds dn[i] = N[g + 8(i/2)][2t + i%2] and
+// dc[4k + i] = C[16k + g + 8(i/2)][2t + i%2].
+__device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, bool me, unsigned mem,
+                                            const float row[kScrRow], float dn[4], float dc[8]) {
+    const int g = lane >> 2, tq = lane & 3;
+    const int gx = g & 1, gy = (g >> 1) & 1, gz = g >> 2;
+    const int ia = g >= 1 && g <= 6 ? sym_a(g - 1) : 0, ib = g >= 1 && g <= 6 ? sym_b(g - 1) : 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dn[i] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) dc[i] = 0.f;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const unsigned hm = (mem >> (16 * h)) & 0xffffu;
+        if (hm == 0) continue;
+        if ((lane >> 4) == h) {
+            float* r = scr + (lane & 15) * kScrRow;
+#pragma unroll
+            for (int f = 0; f < kScrRow; ++f) r[f] = me ? row[f] : 0.f;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+            if (((hm >> (8 * s2)) & 0xffu) == 0) continue;
+            const float* P0 = scr + (8 * s2 + tq) * kScrRow;
+            const float* P1 = P0 + 4 * kScrRow;
+            unsigned bh[2], bl[2];
+            float a[4];
+            // nodes: A[q][p] = (rv, alpha)[q], q = g and g + 8 (< 12); B[p][c] = node weight of corner c = g
+            tf32_split(P0[12 + gx] * P0[14 + gy] * P0[16 + gz], bh[0], bl[0]);
+            tf32_split(P1[12 + gx] * P1[14 + gy] * P1[16 + gz], bh[1], bl[1]);
+            a[0] = P0[g];
+            a[1] = g < 4 ? P0[g + 8] : 0.f;
+            a[2] = P1[g];
+            a[3] = g < 4 ? P1[g + 8] : 0.f;
+            mma_tf32x3(dn, a, bh, bl);
+            // cells: A[s][p] = slot weight, s = 16k + g (+ 8); B[p][q] = 1, rv_a rv_b (q = g < 7)
+            tf32_split(g == 0 ? 1.f : (g < 7 ? P0[ia] * P0[ib] : 0.f), bh[0], bl[0]);
+            tf32_split(g == 0 ? 1.f : (g < 7 ? P1[ia] * P1[ib] : 0.f), bh[1], bl[1]);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int s0 = 16 * k + g, s1 = s0 + 8;
+                a[0] = slot_w(P0, s0);
+                a[1] = s1 < 27 ? slot_w(P0, s1) : 0.f;
+                a[2] = slot_w(P1, s0);
+                a[3] = s1 < 27 ? slot_w(P1, s1) : 0.f;
+                mma_tf32x3(dc + 4 * k, a, bh, bl);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Deposited quantities of one particle from its raw row: QN = (rv cq, alpha cm),
+// QC = (cq, cq rv_a rv_b) over the symmetric pressure components.
+template <typename A, typename T>
+__device__ __forceinline__ void run_quantities(const T row[kScrRow], double cq, double cm, A QN[12], A QC[7]) {
+    const A rv[3] = {A(row[0]), A(row[1]), A(row[2])};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) QN[d] = rv[d] * A(cq);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) QN[3 + d] = A(row[3 + d]) * A(cm);
+    QC[0] = A(cq);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) QC[1 + q] = A(cq) * (rv[sym_a(q)] * rv[sym_b(q)]);
+}
+
+// Node (8 corners) and cell (27 slots) weights from the per-axis weights of a row.
+template <typename A, typename T>
+__device__ __forceinline__ void run_weights(const T row[kScrRow], A wn[8], A wc[27]) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) wn[c] = A(row[12 + (c & 1)] * row[14 + ((c >> 1) & 1)] * row[16 + (c >> 2)]);
+#pragma unroll
+    for (int q = 0; q < 27; ++q) wc[q] = A(row[18 + q % 3] * row[21 + (q / 3) % 3] * row[24 + q / 9]);
+}
+
+// Direct shared-memory adds of one particle of a short run.
+template <typename A, typename T>
+__device__ __forceinline__ void imp_deposit_direct(const T row[kScrRow], double cq, double cm, A* __restrict__ sN,
+                                                A* __restrict__ sC, int NB, int CB, int nb, int cb, int oxn, int oyn,
+                                                int ozn, int oxc, int oyc, int ozc) {
+    A QN[12], QC[7], wn[8], wc[27];
+    run_quantities<A, T>(row, cq, cm, QN, QC);
+    run_weights<A, T>(row, wn, wc);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (wn[c] == A(0)) continue;
+        const int o = nb + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) atomicAdd(&sN[q * NB + o], QN[q] * wn[c]);
+    }
+#pragma unroll
+    for (int sl = 0; sl < 27; ++sl) {
+        if (wc[sl] == A(0)) continue;
+        const int o = cb + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) atomicAdd(&sC[q * CB + o], QC[q] * wc[sl]);
+    }
 }
 
 // All 8 node and 8 cell contributions of one particle to the FP64 grids
@@ -163,6 +310,10 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
     const int oxn = ax ? 1 : 0, oyn = ay ? nsy : 0, ozn = az ? nsz : 0;   // corner strides
     const int oxc = ax ? 1 : 0, oyc = ay ? csy : 0, ozc = az ? csz : 0;   // slot strides
     const int tot = 12 * bk.NB + 7 * bk.CB;
+    constexpr bool kTc = sizeof(A) == sizeof(float);   // FP32 accumulators: tensor-core run sums
+    float* scr = reinterpret_cast<float*>(imp_smem + (size_t)tot * sizeof(A) +
+                                          (kStaged ? (size_t)3 * (bk.NB + bk.CB) * sizeof(T) : 0)) +
+                 warp * (kScrParticles * kScrRow);
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
@@ -196,7 +347,10 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                 for (int c0 = b0; c0 < b1; c0 += 32) {
                     const int n = c0 + lane;
                     const bool valid = n < b1;
-                    A QN[12], QC[7], wn[8], wc[27];
+                    // raw quantities: rv (3), alpha (9), node weights x/y/z (2 each), cell weights x/y/z (3 each)
+                    T row[kScrRow];
+#pragma unroll
+                    for (int f = 0; f < kScrRow; ++f) row[f] = T(0);
                     int cell = -1, nb = 0, cb = 0;
                     bool inb = false;
                     if (valid) {
@@ -207,10 +361,11 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         T mom[3] = {p.px[n], p.py[n], p.pz[n]};
                         T gam, v[3];
                         gamma_vel<T>(mom, T(ms), gam, v);
-                        T nwx[2], nwy[2], nwz[2], cwx[3], cwy[3], cwz[3];
-                        axis_weights<T>(ox, ax, nwx, cwx);
-                        axis_weights<T>(oy, ay, nwy, cwy);
-                        axis_weights<T>(oz, az, nwz, cwz);
+                        T* nw = row + 12;
+                        T* cw = row + 18;
+                        axis_weights<T>(ox, ax, nw, cw);
+                        axis_weights<T>(oy, ay, nw + 2, cw + 3);
+                        axis_weights<T>(oz, az, nw + 4, cw + 6);
                         int li = 0, lj = 0, lk = 0;
                         inb = local_axis(i, x0, t.tx, hx, g.nx, li) && local_axis(j, y0, t.ty, hy, g.ny, lj) &&
                               local_axis(k, z0, t.tz, hz, g.nz, lk);
@@ -222,12 +377,12 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         if (kStaged && inb) {
                             // node pair (c, c+1); cell pair (c-1, c) below the centre, (c, c+1) above
                             const int cbase = cb + (ox < T(0.5) ? 0 : oxc) + (oy < T(0.5) ? 0 : oyc) + (oz < T(0.5) ? 0 : ozc);
-                            const T ux = ox < T(0.5) ? cwx[1] : cwx[2];
-                            const T uy = oy < T(0.5) ? cwy[1] : cwy[2];
-                            const T uz = oz < T(0.5) ? cwz[1] : cwz[2];
+                            const T ux = ox < T(0.5) ? cw[1] : cw[2];
+                            const T uy = oy < T(0.5) ? cw[4] : cw[5];
+                            const T uz = oz < T(0.5) ? cw[7] : cw[8];
 #pragma unroll
                             for (int c = 0; c < 3; ++c) {
-                                e[c] = tri_block<T>(sE + c * bk.NB, nb, oxn, oyn, ozn, nwx[1], nwy[1], nwz[1]);
+                                e[c] = tri_block<T>(sE + c * bk.NB, nb, oxn, oyn, ozn, nw[1], nw[3], nw[5]);
                                 bf[c] = tri_block<T>(sB + c * bk.CB, cbase, oxc, oyc, ozc, ux, uy, uz);
                             }
                         } else if (kStaged) {
@@ -239,22 +394,13 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         T al[9];
                         alpha_tensor<T>(beta, v, gam, e, bf, al);
                         const T vg[3] = {v[0] * gam, v[1] * gam, v[2] * gam};
-                        A rv[3];
 #pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            rv[a] = A(al[3 * a] * vg[0] + al[3 * a + 1] * vg[1] + al[3 * a + 2] * vg[2]);
+                        for (int a = 0; a < 3; ++a) row[a] = al[3 * a] * vg[0] + al[3 * a + 1] * vg[1] + al[3 * a + 2] * vg[2];
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) QN[d] = rv[d] * A(cq);
-#pragma unroll
-                        for (int d = 0; d < 9; ++d) QN[3 + d] = A(al[d]) * A(cm);
-                        QC[0] = A(cq);
-#pragma unroll
-                        for (int q = 0; q < 6; ++q) QC[1 + q] = A(cq) * (rv[sym_a(q)] * rv[sym_b(q)]);
-#pragma unroll
-                        for (int c = 0; c < 8; ++c) wn[c] = A(nwx[c & 1] * nwy[(c >> 1) & 1] * nwz[c >> 2]);
-#pragma unroll
-                        for (int q = 0; q < 27; ++q) wc[q] = A(cwx[q % 3] * cwy[(q / 3) % 3] * cwz[q / 9]);
+                        for (int d = 0; d < 9; ++d) row[3 + d] = al[d];
                         if (!inb) {
+                            A QN[12], QC[7];
+                            run_quantities<A, T>(row, cq, cm, QN, QC);
                             double qn[12], qc[7];
 #pragma unroll
                             for (int d = 0; d < 12; ++d) qn[d] = double(QN[d]);
@@ -273,48 +419,57 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         if (__popc(mem) >= kXposeMin) {
                             const int nbL = __shfl_sync(0xffffffffu, nb, leader);
                             const int cbL = __shfl_sync(0xffffffffu, cb, leader);
-                            A v[32];
+                            if constexpr (kTc) {
+                                float dn[4], dc[8];
+                                tc_run_sums(scr, lane, me, mem, row, dn, dc);
+                                const int gq = lane >> 2, tq = lane & 3;
 #pragma unroll
-                            for (int r = 0; r < 3; ++r) {
-#pragma unroll
-                                for (int x = 0; x < 32; ++x) v[x] = me ? QN[4 * r + x / 8] * wn[x % 8] : A(0);
-                                const A sum = xpose_sum<A>(v, lane);
-                                const int q = 4 * r + lane / 8, c = lane % 8;
-                                if (sum != A(0))
-                                    atomicAdd(&sN[q * bk.NB + nbL + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn],
-                                              sum);
-                            }
-#pragma unroll
-                            for (int r = 0; r < 6; ++r) {
-#pragma unroll
-                                for (int x = 0; x < 32; ++x) {
-                                    const int idx = 32 * r + x;
-                                    v[x] = (idx < 189 && me) ? QC[idx / 27] * wc[idx % 27] : A(0);
+                                for (int i = 0; i < 4; ++i) {
+                                    const int q = gq + 8 * (i >> 1), c = 2 * tq + (i & 1);
+                                    if (q < 12 && dn[i] != 0.f)
+                                        atomicAdd(&sN[q * bk.NB + nbL + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn],
+                                                  dn[i] * (q < 3 ? A(cq) : A(cm)));
                                 }
-                                const A sum = xpose_sum<A>(v, lane);
-                                const int idx = 32 * r + lane;
-                                if (idx < 189 && sum != A(0)) {
-                                    const int q = idx / 27, sl = idx % 27;
-                                    atomicAdd(&sC[q * bk.CB + cbL + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc],
-                                              sum);
+#pragma unroll
+                                for (int i = 0; i < 8; ++i) {
+                                    const int sl = 16 * (i >> 2) + gq + 8 * ((i >> 1) & 1), q = 2 * tq + (i & 1);
+                                    if (sl < 27 && q < 7 && dc[i] != 0.f)
+                                        atomicAdd(&sC[q * bk.CB + cbL + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc],
+                                                  dc[i] * A(cq));
+                                }
+                            } else {
+                                A QN[12], QC[7], wn[8], wc[27];
+                                run_quantities<A, T>(row, cq, cm, QN, QC);
+                                run_weights<A, T>(row, wn, wc);
+                                A vv[32];
+#pragma unroll
+                                for (int r = 0; r < 3; ++r) {
+#pragma unroll
+                                    for (int x = 0; x < 32; ++x) vv[x] = me ? QN[4 * r + x / 8] * wn[x % 8] : A(0);
+                                    const A sum = xpose_sum<A>(vv, lane);
+                                    const int q = 4 * r + lane / 8, c = lane % 8;
+                                    if (sum != A(0))
+                                        atomicAdd(&sN[q * bk.NB + nbL + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn],
+                                                  sum);
+                                }
+#pragma unroll
+                                for (int r = 0; r < 6; ++r) {
+#pragma unroll
+                                    for (int x = 0; x < 32; ++x) {
+                                        const int idx = 32 * r + x;
+                                        vv[x] = (idx < 189 && me) ? QC[idx / 27] * wc[idx % 27] : A(0);
+                                    }
+                                    const A sum = xpose_sum<A>(vv, lane);
+                                    const int idx = 32 * r + lane;
+                                    if (idx < 189 && sum != A(0)) {
+                                        const int q = idx / 27, sl = idx % 27;
+                                        atomicAdd(&sC[q * bk.CB + cbL + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc],
+                                                  sum);
+                                    }
                                 }
                             }
-
                         } else if (me) {
-#pragma unroll
-                            for (int c = 0; c < 8; ++c) {
-                                if (wn[c] == A(0)) continue;
-                                const int o = nb + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn;
-#pragma unroll
-                                for (int q = 0; q < 12; ++q) atomicAdd(&sN[q * bk.NB + o], QN[q] * wn[c]);
-                            }
-#pragma unroll
-                            for (int sl = 0; sl < 27; ++sl) {
-                                if (wc[sl] == A(0)) continue;
-                                const int o = cb + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc;
-#pragma unroll
-                                for (int q = 0; q < 7; ++q) atomicAdd(&sC[q * bk.CB + o], QC[q] * wc[sl]);
-                            }
+                            imp_deposit_direct<A, T>(row, cq, cm, sN, sC, bk.NB, bk.CB, nb, cb, oxn, oyn, ozn, oxc, oyc, ozc);
                         }
                     }
                 }

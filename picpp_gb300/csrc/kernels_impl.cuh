@@ -239,7 +239,9 @@ ImpBlock PK<T>::implicit_block(const GridP& g, const TileGeom& t, int h) {
 
 template <typename T>
 size_t PK<T>::implicit_tile_smem(const ImpBlock& bk) {
-    return (12 * (size_t)bk.NB + 7 * (size_t)bk.CB + (bk.stage ? 3 * ((size_t)bk.NB + bk.CB) : 0)) * sizeof(T);
+    // FP32 accumulators add the per-warp rows of the tensor-core run sums
+    const size_t scratch = sizeof(T) == sizeof(float) ? (size_t)(imp_threads<T>() / 32) * kScrParticles * kScrRow * sizeof(float) : 0;
+    return (12 * (size_t)bk.NB + 7 * (size_t)bk.CB + (bk.stage ? 3 * ((size_t)bk.NB + bk.CB) : 0)) * sizeof(T) + scratch;
 }
 
 template <typename T>

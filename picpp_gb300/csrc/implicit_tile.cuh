@@ -159,7 +159,7 @@ __device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, b
             for (int f = 0; f < kScrRow; ++f) r[f] = me ? row[f] : 0.f;
         }
         __syncwarp();
-#pragma unroll
+#pragma unroll 1
         for (int s2 = 0; s2 < 2; ++s2) {
             if (((hm >> (8 * s2)) & 0xffu) == 0) continue;
             const float* P0 = scr + (8 * s2 + tq) * kScrRow;
@@ -214,27 +214,34 @@ __device__ __forceinline__ void run_weights(const T row[kScrRow], A wn[8], A wc[
     for (int q = 0; q < 27; ++q) wc[q] = A(row[18 + q % 3] * row[21 + (q / 3) % 3] * row[24 + q / 9]);
 }
 
-// Direct shared-memory adds of one particle of a short run.
+// Direct shared-memory adds of one particle of a short run (rolled loops:
+// rare, so kept small next to the hot code).
+template <typename T>
+__device__ __forceinline__ T pick2(const T* w, int i) { return i ? w[1] : w[0]; }
+template <typename T>
+__device__ __forceinline__ T pick3(const T* w, int i) { return i == 0 ? w[0] : (i == 1 ? w[1] : w[2]); }
+
 template <typename A, typename T>
 __device__ __forceinline__ void imp_deposit_direct(const T row[kScrRow], double cq, double cm, A* __restrict__ sN,
-                                                A* __restrict__ sC, int NB, int CB, int nb, int cb, int oxn, int oyn,
-                                                int ozn, int oxc, int oyc, int ozc) {
-    A QN[12], QC[7], wn[8], wc[27];
+                                                   A* __restrict__ sC, int NB, int CB, int nb, int cb, int oxn, int oyn,
+                                                   int ozn, int oxc, int oyc, int ozc) {
+    A QN[12], QC[7];
     run_quantities<A, T>(row, cq, cm, QN, QC);
-    run_weights<A, T>(row, wn, wc);
-#pragma unroll
+#pragma unroll 1
     for (int c = 0; c < 8; ++c) {
-        if (wn[c] == A(0)) continue;
+        const A w = A(pick2(row + 12, c & 1) * pick2(row + 14, (c >> 1) & 1) * pick2(row + 16, c >> 2));
+        if (w == A(0)) continue;
         const int o = nb + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn;
 #pragma unroll
-        for (int q = 0; q < 12; ++q) atomicAdd(&sN[q * NB + o], QN[q] * wn[c]);
+        for (int q = 0; q < 12; ++q) atomicAdd(&sN[q * NB + o], QN[q] * w);
     }
-#pragma unroll
+#pragma unroll 1
     for (int sl = 0; sl < 27; ++sl) {
-        if (wc[sl] == A(0)) continue;
+        const A w = A(pick3(row + 18, sl % 3) * pick3(row + 21, (sl / 3) % 3) * pick3(row + 24, sl / 9));
+        if (w == A(0)) continue;
         const int o = cb + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc;
 #pragma unroll
-        for (int q = 0; q < 7; ++q) atomicAdd(&sC[q * CB + o], QC[q] * wc[sl]);
+        for (int q = 0; q < 7; ++q) atomicAdd(&sC[q * CB + o], QC[q] * w);
     }
 }
 

@@ -12,6 +12,7 @@
 //      restores input order inside every key: stable and run-independent
 //   5. gather of the payload arrays through the permutation.
 #pragma once
+#include <climits>
 #include "common.cuh"
 #include "types.cuh"
 
@@ -128,9 +129,65 @@ __global__ void k_scatter_atomic(const int* __restrict__ key, long long n, int* 
     }
 }
 
-// Rank-count sort of each key segment [off[k], off[k+1]) of tmp into perm:
-// element x goes to off[k] + #{y in segment : y < x}.  Segments up to
-// kWarpSeg elements use one warp; longer ones are left to k_segsort_block.
+// Ascending sort of one segment of up to 32 R distinct source indices held
+// by a warp, element i = 32 r + lane in v[r] (padding INT_MAX): bitonic
+// network, exchanges across lanes by shuffles and across registers in place.
+template <int R>
+__device__ __forceinline__ void warp_bitonic(int v[R], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jr = j >> 5;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (r & jr) continue;
+                    const bool up = (((32 * r + lane) & k) == 0);
+                    const int lo = min(v[r], v[r | jr]), hi = max(v[r], v[r | jr]);
+                    v[r] = up ? lo : hi;
+                    v[r | jr] = up ? hi : lo;
+                }
+            } else {
+                const bool lower = (lane & j) == 0;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int y = __shfl_xor_sync(0xffffffffu, v[r], j);
+                    const bool up = (((32 * r + lane) & k) == 0);
+                    v[r] = (lower == up) ? min(v[r], y) : max(v[r], y);
+                }
+            }
+        }
+    }
+}
+
+// One segment [b, b + len) of tmp, 32 R >= len, sorted into perm by a warp:
+// copied when already ascending (the scatter keeps each warp's particles in
+// order, so a segment filled by one warp, or by warps in index order, is),
+// else sorted in registers.
+template <int R>
+__device__ __forceinline__ void warp_sort_segment(const int* __restrict__ tmp, int* __restrict__ perm, int b, int len,
+                                                  int lane) {
+    int v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = 32 * r + lane < len ? tmp[b + 32 * r + lane] : INT_MAX;
+    bool sorted = true;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int nx = __shfl_down_sync(0xffffffffu, v[r], 1);
+        const int first_next = r + 1 < R ? __shfl_sync(0xffffffffu, v[r + 1 < R ? r + 1 : r], 0) : INT_MAX;
+        const int next = lane < 31 ? nx : first_next;
+        if (32 * r + lane + 1 < len && v[r] > next) sorted = false;
+    }
+    if (!__all_sync(0xffffffffu, sorted)) warp_bitonic<R>(v, lane);
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (32 * r + lane < len) perm[b + 32 * r + lane] = v[r];
+}
+
+// Stable order of each key segment [off[k], off[k+1]) of tmp into perm
+// (ascending source index).  Segments up to kWarpSeg elements use one warp;
+// longer ones are left to k_segsort_block.
 constexpr int kWarpSeg = 256;
 __global__ void k_segsort_warp(const int* __restrict__ off, int nkeys, const int* __restrict__ tmp, int* __restrict__ perm,
                                int* __restrict__ long_count, int* __restrict__ long_list) {
@@ -146,12 +203,10 @@ __global__ void k_segsort_warp(const int* __restrict__ off, int nkeys, const int
             if (lane == 0) { int slot = atomicAdd(long_count, 1); long_list[slot] = (int)kk; }
             continue;
         }
-        for (int a = lane; a < len; a += 32) {
-            int x = tmp[b + a];
-            int r = 0;
-            for (int c = 0; c < len; ++c) r += tmp[b + c] < x;
-            perm[b + r] = x;
-        }
+        if (len <= 32) warp_sort_segment<1>(tmp, perm, b, len, lane);
+        else if (len <= 64) warp_sort_segment<2>(tmp, perm, b, len, lane);
+        else if (len <= 128) warp_sort_segment<4>(tmp, perm, b, len, lane);
+        else warp_sort_segment<8>(tmp, perm, b, len, lane);
     }
 }
 

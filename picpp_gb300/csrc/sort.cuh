@@ -28,12 +28,19 @@ __device__ __forceinline__ int sort_key(const GridP& g, const TileGeom& t, int c
     return tile * (t.tx * t.ty * t.tz) + local;
 }
 
+// Sort key of every particle and the per-key counts, one atomic per distinct
+// key per warp (consecutive particles mostly share a key: the input is the
+// previous sort order).
 __global__ void k_keys_hist(GridP g, TileGeom t, const int* __restrict__ cell, long long n, int* __restrict__ key,
                             int* __restrict__ counts) {
-    for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < n; a += (long long)gridDim.x * blockDim.x) {
-        int kk = sort_key(g, t, cell[a]);
-        key[a] = kk;
-        atomicAdd(&counts[kk], 1);
+    const int lane = threadIdx.x & 31;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
+        const long long a = base + lane;
+        const int kk = a < n ? sort_key(g, t, cell[a]) : -1;
+        if (a < n) key[a] = kk;
+        const unsigned m = __match_any_sync(0xffffffffu, kk);
+        if (kk >= 0 && lane == __ffs(m) - 1) atomicAdd(&counts[kk], __popc(m));
     }
 }
 

@@ -55,6 +55,9 @@ __device__ __forceinline__ void alpha_tensor(T beta, const T v[3], T gamma, cons
     T bs = beta / G;
     T b2c = bs * bs;
     T den = G * (T(1) + b2c * (B[0] * B[0] + B[1] * B[1] + B[2] * B[2]));
+    // FP32: one reciprocal for the nine quotients (within 1 ulp of them);
+    // FP64 keeps the divisions of the reference
+    const T iden = T(1) / den;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -65,7 +68,8 @@ __device__ __forceinline__ void alpha_tensor(T beta, const T v[3], T gamma, cons
                 T e = ((i - j + 3) % 3 == 1) ? T(1) : T(-1);   // LeviCivita[j][i][l]
                 r -= (bs * e * B[l]);
             }
-            al[3 * i + j] = r / den;
+            if constexpr (sizeof(T) == sizeof(float)) al[3 * i + j] = r * iden;
+            else al[3 * i + j] = r / den;
         }
 }
 
@@ -79,11 +83,31 @@ template <> __device__ __forceinline__ float picard_mom_tol<float>() { return 4.
 template <typename T> __device__ __forceinline__ T picard_pos_tol() { return T(1e-8); }
 template <> __device__ __forceinline__ float picard_pos_tol<float>() { return 4.8e-7f; }
 
+// Picard tests compare a norm with tol x a reference norm; FP32 compares the
+// squares (no square roots), FP64 the norms as the reference does.
+template <typename T> __device__ __forceinline__ T picard_norm(T sq) {
+    if constexpr (sizeof(T) == sizeof(float)) return sq;
+    else return dev_sqrt(sq);
+}
+template <typename T> __device__ __forceinline__ T picard_ref(T x) {   // a reference length in picard_norm's form
+    if constexpr (sizeof(T) == sizeof(float)) return x * x;
+    else return x;
+}
+template <typename T> __device__ __forceinline__ T picard_bound(T tol, T ref) {   // ref in picard_norm's form
+    if constexpr (sizeof(T) == sizeof(float)) return (tol * tol) * ref;
+    else return tol * ref;
+}
+
 template <typename T>
 __device__ __forceinline__ void gamma_vel(const T mom[3], T m, T& gam, T v[3]) {
     T p2 = mom[0] * mom[0] + mom[1] * mom[1] + mom[2] * mom[2];
     gam = dev_sqrt(p2 / (m * m) + T(1));
-    v[0] = mom[0] / (m * gam); v[1] = mom[1] / (m * gam); v[2] = mom[2] / (m * gam);
+    if constexpr (sizeof(T) == sizeof(float)) {   // one reciprocal for the three quotients
+        const T r = T(1) / (m * gam);
+        v[0] = mom[0] * r; v[1] = mom[1] * r; v[2] = mom[2] * r;
+    } else {
+        v[0] = mom[0] / (m * gam); v[1] = mom[1] / (m * gam); v[2] = mom[2] / (m * gam);
+    }
 }
 
 // evaluateParticlesRotationTensor (PIC++/mover.cpp:810-841) and the particle
@@ -168,7 +192,10 @@ __global__ void __launch_bounds__(128) k_implicit_deposit(GridP g, PartView<T> p
 template <typename T>
 __device__ __forceinline__ void evaluate_velocity(const T p[3], T m, T v[3]) {
     T p2 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
-    if (p2 < T(1e-4) * m * m) {
+    if constexpr (sizeof(T) == sizeof(float)) {   // one reciprocal for the three quotients
+        const T r = T(1) / (p2 < T(1e-4) * m * m ? m : dev_sqrt(p2 + m * m));
+        v[0] = p[0] * r; v[1] = p[1] * r; v[2] = p[2] * r;
+    } else if (p2 < T(1e-4) * m * m) {
         v[0] = p[0] / m; v[1] = p[1] / m; v[2] = p[2] / m;
     } else {
         T gg = dev_sqrt(p2 + m * m) / m;
@@ -219,14 +246,15 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
 #pragma unroll
         for (int a = 0; a < 3; ++a)
             vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
-        T momNorm = dev_sqrt(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
-        T err = dev_sqrt((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
+        const T momNorm = picard_norm<T>(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
+        T err = picard_norm<T>((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
                          (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
-        T cerr = dxT;
+        const T dxN = picard_ref<T>(dxT);
+        T cerr = dxN;
         T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
         T prevDisp[3];
         int it = 0;
-        while (err > picard_mom_tol<T>() * momNorm && cerr > picard_pos_tol<T>() * dxT && it < 3) {
+        while (err > picard_bound<T>(picard_mom_tol<T>(), momNorm) && cerr > picard_bound<T>(picard_pos_tol<T>(), dxN) && it < 3) {
             ++it;
             T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
 #pragma unroll
@@ -250,9 +278,9 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
             T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
 #pragma unroll
             for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
-            err = dev_sqrt((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) + (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
+            err = picard_norm<T>((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) + (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
                            (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
-            cerr = dev_sqrt((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
+            cerr = picard_norm<T>((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
                             (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
                             (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
         }

@@ -651,14 +651,15 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
                     vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
-                const T momNorm = dev_sqrt(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
-                T err = dev_sqrt((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
+                const T momNorm = picard_norm<T>(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
+                T err = picard_norm<T>((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
                                  (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
-                T cerr = dxT;
+                const T dxN = picard_ref<T>(dxT);
+                T cerr = dxN;
                 T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
                 T prevDisp[3];
                 int it = 0;
-                while (err > picard_mom_tol<T>() * momNorm && cerr > picard_pos_tol<T>() * dxT && it < 3) {
+                while (err > picard_bound<T>(picard_mom_tol<T>(), momNorm) && cerr > picard_bound<T>(picard_pos_tol<T>(), dxN) && it < 3) {
                     ++it;
                     const T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
 #pragma unroll
@@ -682,10 +683,10 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     const T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
 #pragma unroll
                     for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
-                    err = dev_sqrt((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) +
+                    err = picard_norm<T>((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) +
                                    (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
                                    (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
-                    cerr = dev_sqrt((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
+                    cerr = picard_norm<T>((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
                                     (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
                                     (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
                 }

@@ -131,11 +131,6 @@ __device__ __forceinline__ void mma_tf32x3(float d[4], const float a[4], const u
     mma_tf32(d, ah, bh);
 }
 
-// Cell-slot weight of scratch row P for slot s (x fastest, three per axis).
-__device__ __forceinline__ float slot_w(const float* P, int s) {
-    return P[18 + s % 3] * P[21 + (s / 3) % 3] * P[24 + s / 9];
-}
-
 // Sums of one run over the warp: mem = lanes in the run; row = this lane's
 // raw quantities (written only when the lane is in the run).  On return,
 // lane (g = lane/4, t = lane%4) holds dn[i] = N[g + 8(i/2)][2t + i%2] and
@@ -145,6 +140,15 @@ __device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, b
     const int g = lane >> 2, tq = lane & 3;
     const int gx = g & 1, gy = (g >> 1) & 1, gz = g >> 2;
     const int ia = g >= 1 && g <= 6 ? sym_a(g - 1) : 0, ib = g >= 1 && g <= 6 ? sym_b(g - 1) : 0;
+    // this lane's four cell slots g, g + 8, g + 16, g + 24: row offsets of their x, y, z weights
+    int sox[4], soy[4], soz[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int sl = g + 8 * k;
+        sox[k] = 18 + sl % 3;
+        soy[k] = 21 + (sl / 3) % 3;
+        soz[k] = sl < 27 ? 24 + sl / 9 : 24;
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) dn[i] = 0.f;
 #pragma unroll
@@ -179,11 +183,12 @@ __device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, b
             tf32_split(g == 0 ? 1.f : (g < 7 ? P1[ia] * P1[ib] : 0.f), bh[1], bl[1]);
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
-                const int s0 = 16 * k + g, s1 = s0 + 8;
-                a[0] = slot_w(P0, s0);
-                a[1] = s1 < 27 ? slot_w(P0, s1) : 0.f;
-                a[2] = slot_w(P1, s0);
-                a[3] = s1 < 27 ? slot_w(P1, s1) : 0.f;
+                const int j0 = 2 * k, j1 = 2 * k + 1;   // slots 16k + g and 16k + g + 8
+                const bool v1 = 16 * k + g + 8 < 27;
+                a[0] = P0[sox[j0]] * P0[soy[j0]] * P0[soz[j0]];
+                a[1] = v1 ? P0[sox[j1]] * P0[soy[j1]] * P0[soz[j1]] : 0.f;
+                a[2] = P1[sox[j0]] * P1[soy[j0]] * P1[soz[j0]];
+                a[3] = v1 ? P1[sox[j1]] * P1[soy[j1]] * P1[soz[j1]] : 0.f;
                 mma_tf32x3(dc + 4 * k, a, bh, bl);
             }
         }

@@ -35,7 +35,8 @@ constexpr int kImpThreads = PIC_IMP_THREADS;
 template <typename T>
 __host__ __device__ constexpr int imp_threads() { return sizeof(T) == sizeof(float) ? kImpThreads : 256; }
 constexpr int kMoverThreads = PIC_MOVER_THREADS;
-constexpr int kXposeMin = 4;   // fewest lanes of one cell that take the transpose-reduction
+constexpr int kXposeMin = 4;   // fewest lanes of one cell that take the transpose-reduction (FP64)
+constexpr int kTcMin = 1;      // fewest lanes of one cell that take the tensor-core run sums (FP32)
 
 
 // Symmetric pressure components kept in shared memory, q = 0..5:
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         const bool me = ((pending >> lane) & 1u) && cell == lcell;
                         const unsigned mem = __ballot_sync(0xffffffffu, me);
                         pending &= ~mem;
-                        if (__popc(mem) >= kXposeMin) {
+                        if (__popc(mem) >= (kTc ? kTcMin : kXposeMin)) {
                             const int nbL = __shfl_sync(0xffffffffu, nb, leader);
                             const int cbL = __shfl_sync(0xffffffffu, cb, leader);
                             if constexpr (kTc) {
@@ -534,6 +535,15 @@ struct MoverBlock {
     int cbx, cby, cbz, CB;
 };
 
+// Global trilinear gather of one node (E) or cell (B) field for a particle
+// whose stencil leaves the staged block (out of line: rare).
+template <typename T>
+__device__ __noinline__ void gather_global_1(const GridP& g, const int c[3], const T u[3], const double* __restrict__ F,
+                                             bool node, T out[3]) {
+    if (node) gather_node<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], F, out);
+    else gather_cell<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], F, out);
+}
+
 // moveParticle (PIC++/mover.cpp:194-491), periodic box, one CTA per tile of
 // tile-ordered particles: E^n and E^{n+theta} (nodes) and B^n (cells) of
 // the tile and a two-cell halo are staged in shared memory in the particle
@@ -598,8 +608,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                                      local_axis(c[1], y0, t.ty, hy, g.ny, l[1]) &&
                                      local_axis(c[2], z0, t.tz, hz, g.nz, l[2]);
                     if (!inb) {
-                        if (node) gather_node<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], glbN, out);
-                        else gather_cell<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], glbN, out);
+                        gather_global_1<T>(g, c, u, glbN, node, out);
                         return;
                     }
                     T w[3];

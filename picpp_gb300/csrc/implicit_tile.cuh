@@ -599,48 +599,50 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
             for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x) {
                 int ci[3];
                 decode(g, p.cell[n], ci[0], ci[1], ci[2]);
-                // gathers at (cell c, offset u): shared block when the whole
-                // stencil is staged, else the FP64 grids
-                auto gat = [&](const int c[3], const T u[3], const T* __restrict__ blkN, const double* __restrict__ glbN,
-                               bool node, T out[3]) {
+                // A position (cell c, offset u) is located once: its node and cell
+                // stencils in the staged block (bases, upper weights), shared by the
+                // two or three gathers there; a stencil that leaves the block
+                // gathers from the FP64 grids.
+                struct Loc {
+                    bool inb;
+                    int nbase, cbase;
+                    T wn[3], wc[3];
+                };
+                auto locate = [&](const int c[3], const T u[3], Loc& L) {
                     int l[3];
-                    const bool inb = local_axis(c[0], x0, t.tx, hx, g.nx, l[0]) &&
-                                     local_axis(c[1], y0, t.ty, hy, g.ny, l[1]) &&
-                                     local_axis(c[2], z0, t.tz, hz, g.nz, l[2]);
-                    if (!inb) {
+                    L.inb = local_axis(c[0], x0, t.tx, hx, g.nx, l[0]) && local_axis(c[1], y0, t.ty, hy, g.ny, l[1]) &&
+                            local_axis(c[2], z0, t.tz, hz, g.nz, l[2]);
+                    if (!L.inb) return;
+                    int lo[3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        T w2[2];
+                        int idx[2];
+                        node_w<T>(u[a], c[a], nn[a], idx, w2);
+                        L.wn[a] = w2[1];
+                        cell_w<T>(u[a], c[a], nn[a], idx, w2);
+                        L.wc[a] = w2[1];
+                        // lower cell of the pair: c - 1 below the centre, c above
+                        lo[a] = (nn[a] > 1 && u[a] < T(0.5)) ? l[a] - 1 : l[a];
+                    }
+                    L.nbase = (l[2] + hz) * nsz + (l[1] + hy) * nsy + (l[0] + hx) * nsx;
+                    const int ex = ax ? 1 : 0, ey = ay ? 1 : 0, ez = az ? 1 : 0;
+                    L.cbase = (lo[2] + hz + ez) * csz + (lo[1] + hy + ey) * csy + (lo[0] + hx + ex) * csx;
+                };
+                auto gat = [&](const Loc& L, const int c[3], const T u[3], const T* __restrict__ blkN,
+                               const double* __restrict__ glbN, bool node, T out[3]) {
+                    if (!L.inb) {
                         gather_global_1<T>(g, c, u, glbN, node, out);
                         return;
                     }
-                    T w[3];
-                    int base;
                     if (node) {
-                        T wn[2];
-                        int dummy[2];
-#pragma unroll
-                        for (int a = 0; a < 3; ++a) {
-                            node_w<T>(u[a], c[a], nn[a], dummy, wn);
-                            w[a] = wn[1];
-                        }
-                        base = (l[2] + hz) * nsz + (l[1] + hy) * nsy + (l[0] + hx) * nsx;
 #pragma unroll
                         for (int q = 0; q < 3; ++q)
-                            out[q] = tri_block<T>(blkN + q * mb.NB, base, nsx, nsy, nsz, w[0], w[1], w[2]);
+                            out[q] = tri_block<T>(blkN + q * mb.NB, L.nbase, nsx, nsy, nsz, L.wn[0], L.wn[1], L.wn[2]);
                     } else {
-                        T wc[2];
-                        int idx[2];
-                        int lo[3];
-#pragma unroll
-                        for (int a = 0; a < 3; ++a) {
-                            cell_w<T>(u[a], c[a], nn[a], idx, wc);
-                            w[a] = wc[1];
-                            // lower cell of the pair: c - 1 below the centre, c above
-                            lo[a] = (nn[a] > 1 && u[a] < T(0.5)) ? l[a] - 1 : l[a];
-                        }
-                        const int ex = ax ? 1 : 0, ey = ay ? 1 : 0, ez = az ? 1 : 0;
-                        base = (lo[2] + hz + ez) * csz + (lo[1] + hy + ey) * csy + (lo[0] + hx + ex) * csx;
 #pragma unroll
                         for (int q = 0; q < 3; ++q)
-                            out[q] = tri_block<T>(blkN + q * mb.CB, base, csx, csy, csz, w[0], w[1], w[2]);
+                            out[q] = tri_block<T>(blkN + q * mb.CB, L.cbase, csx, csy, csz, L.wc[0], L.wc[1], L.wc[2]);
                     }
                 };
                 T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
@@ -648,10 +650,12 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T gam, v[3];
                 gamma_vel<T>(mom0, mm, gam, v);
                 T e[3], b[3], al[9];
-                gat(ci, u0, sE, E, true, e);
-                gat(ci, u0, sB, B, false, b);
+                Loc L0;
+                locate(ci, u0, L0);
+                gat(L0, ci, u0, sE, E, true, e);
+                gat(L0, ci, u0, sB, B, false, b);
                 alpha_tensor<T>(beta, v, gam, e, b, al);
-                gat(ci, u0, sEt, Et, true, e);
+                gat(L0, ci, u0, sEt, Et, true, e);
                 T vxb[3] = {v[1] * b[2] - v[2] * b[1], -v[0] * b[2] + v[2] * b[0], v[0] * b[1] - v[1] * b[0]};
                 T pnew[3];
 #pragma unroll
@@ -692,8 +696,10 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                         tc[d] = ci[d]; tu[d] = u0[d];
                         advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
                     }
-                    gat(tc, tu, sEt, Et, true, e);
-                    gat(tc, tu, sB, B, false, b);
+                    Loc L1;
+                    locate(tc, tu, L1);
+                    gat(L1, tc, tu, sEt, Et, true, e);
+                    gat(L1, tc, tu, sB, B, false, b);
                     const T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
 #pragma unroll
                     for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;

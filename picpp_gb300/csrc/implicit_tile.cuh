@@ -99,13 +99,13 @@ __device__ __forceinline__ T tri_block(const T* __restrict__ F, int base, int sx
 // C[s][q] = sum_p wc_p[s] QC_p[q]  of a run of particles are small matrix
 // products with the particles as the inner dimension.  Each lane writes its
 // particle's raw quantities (rv 3, alpha 9, per-axis node weights 2 x 3,
-// per-axis cell weights 3 x 3) to a per-warp scratch of 16 rows; the warp
+// per-axis cell weights 3 x 3) to a per-warp scratch of 32 rows; the warp
 // then runs m16n8k8 TF32 MMAs, eight particles per MMA, in the 3 x TF32 form
 // (x = hi + lo, products hi*hi + hi*lo + lo*hi, FP32 accumulation), which
 // keeps the sums at FP32 accuracy.  The per-species factors (cq, cm) are
 // applied to the sums.
 constexpr int kScrRow = 27;         // scratch floats per particle
-constexpr int kScrParticles = 16;   // scratch rows per warp
+constexpr int kScrParticles = 32;   // scratch rows per warp
 
 // Round to the 19-bit TF32 format (ties away from zero); low 13 bits zero.
 __device__ __forceinline__ unsigned tf32_round(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
@@ -132,9 +132,9 @@ __device__ __forceinline__ void mma_tf32x3(float d[4], const float a[4], const u
     mma_tf32(d, ah, bh);
 }
 
-// Sums of one run over the warp: mem = lanes in the run; row = this lane's
-// raw quantities (written only when the lane is in the run).  On return,
-// lane (g = lane/4, t = lane%4) holds dn[i] = N[g + 8(i/2)][2t + i%2] and
+// Sums of one run over the warp, added to dn and dc: mem = lanes in the run;
+// row = this lane's raw quantities (used only when the lane is in the run).
+// Lane (g = lane/4, t = lane%4) holds dn[i] = N[g + 8(i/2)][2t + i%2] and
 // dc[4k + i] = C[16k + g + 8(i/2)][2t + i%2].
 __device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, bool me, unsigned mem,
                                             const float row[kScrRow], float dn[4], float dc[8]) {
@@ -150,50 +150,61 @@ __device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, b
         soy[k] = 21 + (sl / 3) % 3;
         soz[k] = sl < 27 ? 24 + sl / 9 : 24;
     }
+    {
+        float* r = scr + lane * kScrRow;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) dn[i] = 0.f;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) dc[i] = 0.f;
+        for (int f = 0; f < kScrRow; ++f) r[f] = me ? row[f] : 0.f;
+    }
+    __syncwarp();
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        const unsigned hm = (mem >> (16 * h)) & 0xffffu;
-        if (hm == 0) continue;
-        if ((lane >> 4) == h) {
-            float* r = scr + (lane & 15) * kScrRow;
+    for (int s2 = 0; s2 < 4; ++s2) {
+        if (((mem >> (8 * s2)) & 0xffu) == 0) continue;
+        const float* P0 = scr + (8 * s2 + tq) * kScrRow;
+        const float* P1 = P0 + 4 * kScrRow;
+        unsigned bh[2], bl[2];
+        float a[4];
+        // nodes: A[q][p] = (rv, alpha)[q], q = g and g + 8 (< 12); B[p][c] = node weight of corner c = g
+        tf32_split(P0[12 + gx] * P0[14 + gy] * P0[16 + gz], bh[0], bl[0]);
+        tf32_split(P1[12 + gx] * P1[14 + gy] * P1[16 + gz], bh[1], bl[1]);
+        a[0] = P0[g];
+        a[1] = g < 4 ? P0[g + 8] : 0.f;
+        a[2] = P1[g];
+        a[3] = g < 4 ? P1[g + 8] : 0.f;
+        mma_tf32x3(dn, a, bh, bl);
+        // cells: A[s][p] = slot weight, s = 16k + g (+ 8); B[p][q] = 1, rv_a rv_b (q = g < 7)
+        tf32_split(g == 0 ? 1.f : (g < 7 ? P0[ia] * P0[ib] : 0.f), bh[0], bl[0]);
+        tf32_split(g == 0 ? 1.f : (g < 7 ? P1[ia] * P1[ib] : 0.f), bh[1], bl[1]);
 #pragma unroll
-            for (int f = 0; f < kScrRow; ++f) r[f] = me ? row[f] : 0.f;
+        for (int k = 0; k < 2; ++k) {
+            const int j0 = 2 * k, j1 = 2 * k + 1;   // slots 16k + g and 16k + g + 8
+            const bool v1 = 16 * k + g + 8 < 27;
+            a[0] = P0[sox[j0]] * P0[soy[j0]] * P0[soz[j0]];
+            a[1] = v1 ? P0[sox[j1]] * P0[soy[j1]] * P0[soz[j1]] : 0.f;
+            a[2] = P1[sox[j0]] * P1[soy[j0]] * P1[soz[j0]];
+            a[3] = v1 ? P1[sox[j1]] * P1[soy[j1]] * P1[soz[j1]] : 0.f;
+            mma_tf32x3(dc + 4 * k, a, bh, bl);
         }
-        __syncwarp();
-#pragma unroll 1
-        for (int s2 = 0; s2 < 2; ++s2) {
-            if (((hm >> (8 * s2)) & 0xffu) == 0) continue;
-            const float* P0 = scr + (8 * s2 + tq) * kScrRow;
-            const float* P1 = P0 + 4 * kScrRow;
-            unsigned bh[2], bl[2];
-            float a[4];
-            // nodes: A[q][p] = (rv, alpha)[q], q = g and g + 8 (< 12); B[p][c] = node weight of corner c = g
-            tf32_split(P0[12 + gx] * P0[14 + gy] * P0[16 + gz], bh[0], bl[0]);
-            tf32_split(P1[12 + gx] * P1[14 + gy] * P1[16 + gz], bh[1], bl[1]);
-            a[0] = P0[g];
-            a[1] = g < 4 ? P0[g + 8] : 0.f;
-            a[2] = P1[g];
-            a[3] = g < 4 ? P1[g + 8] : 0.f;
-            mma_tf32x3(dn, a, bh, bl);
-            // cells: A[s][p] = slot weight, s = 16k + g (+ 8); B[p][q] = 1, rv_a rv_b (q = g < 7)
-            tf32_split(g == 0 ? 1.f : (g < 7 ? P0[ia] * P0[ib] : 0.f), bh[0], bl[0]);
-            tf32_split(g == 0 ? 1.f : (g < 7 ? P1[ia] * P1[ib] : 0.f), bh[1], bl[1]);
+    }
+    __syncwarp();
+}
+
+// Adds the run sums of tc_run_sums (lane layout as there) to the shared
+// blocks at node base nb and cell base cb, times the species factors.
+__device__ __forceinline__ void add_run_sums(float* __restrict__ sN, float* __restrict__ sC, int NB, int CB, int nb,
+                                             int cb, int oxn, int oyn, int ozn, int oxc, int oyc, int ozc, int lane,
+                                             const float dn[4], const float dc[8], float cq, float cm) {
+    const int gq = lane >> 2, tq = lane & 3;
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int j0 = 2 * k, j1 = 2 * k + 1;   // slots 16k + g and 16k + g + 8
-                const bool v1 = 16 * k + g + 8 < 27;
-                a[0] = P0[sox[j0]] * P0[soy[j0]] * P0[soz[j0]];
-                a[1] = v1 ? P0[sox[j1]] * P0[soy[j1]] * P0[soz[j1]] : 0.f;
-                a[2] = P1[sox[j0]] * P1[soy[j0]] * P1[soz[j0]];
-                a[3] = v1 ? P1[sox[j1]] * P1[soy[j1]] * P1[soz[j1]] : 0.f;
-                mma_tf32x3(dc + 4 * k, a, bh, bl);
-            }
-        }
-        __syncwarp();
+    for (int i = 0; i < 4; ++i) {
+        const int q = gq + 8 * (i >> 1), c = 2 * tq + (i & 1);
+        if (q < 12 && dn[i] != 0.f)
+            atomicAdd(&sN[q * NB + nb + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn], dn[i] * (q < 3 ? cq : cm));
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int sl = 16 * (i >> 2) + gq + 8 * ((i >> 1) & 1), q = 2 * tq + (i & 1);
+        if (sl < 27 && q < 7 && dc[i] != 0.f)
+            atomicAdd(&sC[q * CB + cb + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc], dc[i] * cq);
     }
 }
 
@@ -357,6 +368,18 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
             for (int lc = warp; lc < T3; lc += nwarps) {
                 const int kk = tile * T3 + lc;
                 const int b0 = off[kk], b1 = off[kk + 1];
+                // Right after a sort the particles of this key lie in the key's cell:
+                // the tensor-core sums of all its chunks accumulate and reach the
+                // block once.
+                constexpr bool kCellAcc = kStaged && kTc;
+                float an[4] = {0.f, 0.f, 0.f, 0.f}, ac[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                bool acc_any = false;
+                int nbK = 0, cbK = 0;
+                if constexpr (kCellAcc) {
+                    const int li = lc % t.tx, lj = (lc / t.tx) % t.ty, lk = lc / (t.tx * t.ty);
+                    nbK = (lk + hz) * nsz + (lj + hy) * nsy + (li + hx);
+                    cbK = (lk + hz) * csz + (lj + hy) * csy + (li + hx);
+                }
                 for (int c0 = b0; c0 < b1; c0 += 32) {
                     const int n = c0 + lane;
                     const bool valid = n < b1;
@@ -423,6 +446,15 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         }
                     }
                     unsigned pending = __ballot_sync(0xffffffffu, valid && inb);
+                    if constexpr (kCellAcc) {
+                        const bool mine = valid && inb && nb == nbK;
+                        const unsigned mm = __ballot_sync(0xffffffffu, mine);
+                        if (mm) {
+                            tc_run_sums(scr, lane, mine, mm, row, an, ac);
+                            acc_any = true;
+                        }
+                        pending &= ~mm;
+                    }
                     while (pending) {
                         const int leader = __ffs(pending) - 1;
                         const int lcell = __shfl_sync(0xffffffffu, cell, leader);
@@ -433,23 +465,10 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                             const int nbL = __shfl_sync(0xffffffffu, nb, leader);
                             const int cbL = __shfl_sync(0xffffffffu, cb, leader);
                             if constexpr (kTc) {
-                                float dn[4], dc[8];
+                                float dn[4] = {0.f, 0.f, 0.f, 0.f}, dc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                                 tc_run_sums(scr, lane, me, mem, row, dn, dc);
-                                const int gq = lane >> 2, tq = lane & 3;
-#pragma unroll
-                                for (int i = 0; i < 4; ++i) {
-                                    const int q = gq + 8 * (i >> 1), c = 2 * tq + (i & 1);
-                                    if (q < 12 && dn[i] != 0.f)
-                                        atomicAdd(&sN[q * bk.NB + nbL + (c & 1) * oxn + ((c >> 1) & 1) * oyn + (c >> 2) * ozn],
-                                                  dn[i] * (q < 3 ? A(cq) : A(cm)));
-                                }
-#pragma unroll
-                                for (int i = 0; i < 8; ++i) {
-                                    const int sl = 16 * (i >> 2) + gq + 8 * ((i >> 1) & 1), q = 2 * tq + (i & 1);
-                                    if (sl < 27 && q < 7 && dc[i] != 0.f)
-                                        atomicAdd(&sC[q * bk.CB + cbL + (sl % 3) * oxc + ((sl / 3) % 3) * oyc + (sl / 9) * ozc],
-                                                  dc[i] * A(cq));
-                                }
+                                add_run_sums(sN, sC, bk.NB, bk.CB, nbL, cbL, oxn, oyn, ozn, oxc, oyc, ozc, lane, dn, dc,
+                                             float(cq), float(cm));
                             } else {
                                 A QN[12], QC[7], wn[8], wc[27];
                                 run_quantities<A, T>(row, cq, cm, QN, QC);
@@ -485,6 +504,11 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                             imp_deposit_direct<A, T>(row, cq, cm, sN, sC, bk.NB, bk.CB, nb, cb, oxn, oyn, ozn, oxc, oyc, ozc);
                         }
                     }
+                }
+                if constexpr (kCellAcc) {
+                    if (acc_any)
+                        add_run_sums(sN, sC, bk.NB, bk.CB, nbK, cbK, oxn, oyn, ozn, oxc, oyc, ozc, lane, an, ac, float(cq),
+                                     float(cm));
                 }
             }
         }

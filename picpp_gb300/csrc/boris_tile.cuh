@@ -147,13 +147,13 @@ __device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restric
     const float hf = floorf(m * 4.656612873077393e-10f);            // m / 2^31, exact power-of-two scaling
     const unsigned h = (unsigned)hf;
     const unsigned l = __float2uint_rn(m - hf * 2147483648.0f);      // exact remainder, rounded to an integer
-    unsigned xl = ((h & 1u) << 31) | l;                              // |x| in base 2^32
-    unsigned xh = h >> 1;
-    if (xl == 0u && xh == 0u) return;
-    if (xf < 0.f) {                                                  // two's complement of the 64-bit value
-        xl = ~xl + 1u;
-        xh = ~xh + (xl == 0u ? 1u : 0u);
-    }
+    const unsigned al = ((h & 1u) << 31) | l;                        // |x| in base 2^32
+    const unsigned ah = h >> 1;
+    // two's complement of the 64-bit value for x < 0, without branches (a
+    // zero x adds nothing)
+    const unsigned sg = xf < 0.f ? 0xffffffffu : 0u;
+    const unsigned xl = (al ^ sg) - sg;
+    const unsigned xh = (ah ^ sg) + (sg & (xl == 0u ? 1u : 0u));
     const unsigned old = atomicAdd(&lo[e], xl);
     const unsigned carry = (old + xl < old) ? 1u : 0u;
     const int add_hi = (int)(xh + carry);

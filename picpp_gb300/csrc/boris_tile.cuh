@@ -156,8 +156,7 @@ __device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restric
     const unsigned xh = (ah ^ sg) + (sg & (xl == 0u ? 1u : 0u));
     const unsigned old = atomicAdd(&lo[e], xl);
     const unsigned carry = (old + xl < old) ? 1u : 0u;
-    const int add_hi = (int)(xh + carry);
-    if (add_hi != 0) atomicAdd(&hi[e], add_hi);
+    atomicAdd(&hi[e], (int)(xh + carry));
 }
 
 // add_slots in fixed point.

@@ -561,11 +561,19 @@ struct MoverBlock {
 
 // Global trilinear gather of one node (E) or cell (B) field for a particle
 // whose stencil leaves the staged block (out of line: rare).
+// Scalars in, the three components out by value: no caller array has its
+// address taken, so nothing goes through the stack on the common path.
 template <typename T>
-__device__ __noinline__ void gather_global_1(const GridP& g, const int c[3], const T u[3], const double* __restrict__ F,
-                                             bool node, T out[3]) {
-    if (node) gather_node<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], F, out);
-    else gather_cell<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], F, out);
+struct Comp3 {
+    T v[3];
+};
+template <typename T>
+__device__ __noinline__ Comp3<T> gather_global_1(const GridP g, int c0, int c1, int c2, T u0, T u1, T u2,
+                                                 const double* __restrict__ F, bool node) {
+    Comp3<T> r;
+    if (node) gather_node<T>(g, c0, c1, c2, u0, u1, u2, F, r.v);
+    else gather_cell<T>(g, c0, c1, c2, u0, u1, u2, F, r.v);
+    return r;
 }
 
 // moveParticle (PIC++/mover.cpp:194-491), periodic box, one CTA per tile of
@@ -656,7 +664,8 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 auto gat = [&](const Loc& L, const int c[3], const T u[3], const T* __restrict__ blkN,
                                const double* __restrict__ glbN, bool node, T out[3]) {
                     if (!L.inb) {
-                        gather_global_1<T>(g, c, u, glbN, node, out);
+                        const Comp3<T> r = gather_global_1<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], glbN, node);
+                        out[0] = r.v[0]; out[1] = r.v[1]; out[2] = r.v[2];
                         return;
                     }
                     if (node) {

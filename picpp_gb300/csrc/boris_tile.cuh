@@ -142,7 +142,7 @@ __device__ __forceinline__ void add_slots(TP* __restrict__ sJ, long long JC, int
 // independent of the order of the adds.  The split uses 32-bit conversions
 // and integer operations only (64-bit integer conversions run on the FP64
 // pipe, which is slow on this GPU): |x| = h 2^31 + l with h < 2^9, l < 2^31.
-__device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restrict__ hi, long long e, float xf) {
+__device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restrict__ hi, int e, float xf) {
     const float m = fabsf(xf);
     const float hf = floorf(m * 4.656612873077393e-10f);            // m / 2^31, exact power-of-two scaling
     const unsigned h = (unsigned)hf;
@@ -160,9 +160,10 @@ __device__ __forceinline__ void fx_add(unsigned* __restrict__ lo, int* __restric
 }
 
 // add_slots in fixed point.
-__device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __restrict__ hi, long long JC, int c,
+// 32-bit offsets: a block holds 3 x (tile + 4)^3 entries at most.
+__device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __restrict__ hi, int JC, int c,
                                              int X0, int XY, int ey, int ez, const float a[12], float sc) {
-    const long long off[12] = {c, c + X0, c + XY, c + X0 + XY,
+    const int off[12] = {c, c + X0, c + XY, c + X0 + XY,
                                JC + c, JC + c + 1, JC + c + XY, JC + c + 1 + XY,
                                2 * JC + c, 2 * JC + c + 1, 2 * JC + c + X0, 2 * JC + c + 1 + X0};
     const bool use[12] = {true, ey != 0, ez != 0, ey && ez, true, true, ez != 0, ez != 0, true, true, ey != 0, ey != 0};
@@ -300,10 +301,12 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                     const TP RY = ry == 0 ? (Y + PY) / TP(2) : TP(ry > 0 ? ry : 0) * dy;
                     const TP RZ = rz == 0 ? (Z + PZ) / TP(2) : TP(rz > 0 ? rz : 0) * dz;
                     const int ax = bx + rx, ay = by + ry, az = bz + rz;   // block cell of the old-side segment
-                    const bool inblock = fast && rx >= -1 && rx <= 1 && ry >= -1 && ry <= 1 && rz >= -1 && rz <= 1 &&
-                                         ax >= 0 && bx >= 0 && ax + 1 < jx && bx + 1 < jx && ay >= 0 && by >= 0 &&
-                                         ay + ey < jy && by + ey < jy && az >= 0 && bz >= 0 && az + ez < jz &&
-                                         bz + ez < jz;
+                    // unsigned compares: (unsigned)x < n is 0 <= x < n
+                    const bool inblock = fast && (unsigned)(rx + 1) <= 2u && (unsigned)(ry + 1) <= 2u &&
+                                         (unsigned)(rz + 1) <= 2u && (unsigned)ax < (unsigned)(jx - 1) &&
+                                         (unsigned)bx < (unsigned)(jx - 1) && (unsigned)ay < (unsigned)(jy - ey) &&
+                                         (unsigned)by < (unsigned)(jy - ey) && (unsigned)az < (unsigned)(jz - ez) &&
+                                         (unsigned)bz < (unsigned)(jz - ez);
                     if (inblock) {
                         const TP F1x = divd<TP>(fcd * (RX - PX), dt, idt);
                         const TP F1y = divd<TP>(fcd * (RY - PY), dt, idt);
@@ -333,9 +336,9 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                 segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);   // zeros off the reduction
                 if constexpr (kFixed) {
                     if (run_sum<TP>(keyB, aB) && keyB >= 0)
-                        add_slots_fx(sLo, sHi, JC, keyB, jx, jx * jy, ey, ez, (const float*)aB, fx_scale);
+                        add_slots_fx(sLo, sHi, (int)JC, keyB, jx, jx * jy, ey, ez, (const float*)aB, fx_scale);
                     if (run_sum<TP>(keyA, aA) && keyA >= 0)
-                        add_slots_fx(sLo, sHi, JC, keyA, jx, jx * jy, ey, ez, (const float*)aA, fx_scale);
+                        add_slots_fx(sLo, sHi, (int)JC, keyA, jx, jx * jy, ey, ez, (const float*)aA, fx_scale);
                 } else {
                     if (run_sum<TP>(keyB, aB) && keyB >= 0) add_slots<TP>(sJ, JC, keyB, jx, jx * jy, ey, ez, aB);
                     if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);

@@ -231,8 +231,9 @@ def test_implicit_moments_and_rhs_match_oracle(pg, compat):
 @pytest.mark.parametrize("real,tile,ppc", [(1, (4, 3, 5), 6), (0, (8, 6, 5), 6), (1, (2, 2, 1), 2),
                                            (1, (1, 1, 1), 5), (0, (8, 3, 5), 2)])
 def test_implicit_tiled_moments_match_oracle(pg, real, tile, ppc):
-    """Tile-order deposit (shared-memory blocks, transpose-reduced runs and
-    direct adds) against the oracle; pressure tensor at the particle's cells."""
+    """Tile-order deposit (shared-memory blocks; run sums on the tensor cores
+    for FP32 particles, transpose-reduced runs and direct adds for FP64)
+    against the oracle; pressure tensor at the particle's cells."""
     st = implicit_state(ppc=ppc)
     sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1, tile=tile)
     sim.upload_state(st)

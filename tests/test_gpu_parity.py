@@ -57,6 +57,22 @@ def compare_particles(box, gpu, ref, tol_p, tol_x):
         assert rel_err(gpu[k], ref[k]) <= tol_p
 
 
+def test_buneman_dense_cells_match_oracle(pg):
+    """40 particles per cell and species (FP32): runs of a whole warp in the
+    segmented sums and the fixed-point block."""
+    st = noisy(I.buneman_plasma(8, 8, 8, ppc=40, seed=39))
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=0, sort_every=1)
+    sim.upload_state(st)
+    sim.buneman_step(1)
+    E, B, J = sim.download_fields()
+    sp, Eo, Bo, Jo = oracle_buneman(st, 1)
+    assert rel_err(E, Eo) < TOL32
+    assert rel_err(B, Bo) < TOL32
+    assert rel_err(J, Jo.reshape(J.shape)) < TOL32
+    for s in range(2):
+        compare_particles(st.box, sim.download_particles(s), sp[s], TOL32, 1e-5)
+
+
 @pytest.mark.parametrize("real", [1, 0])
 def test_buneman_phase_calls_match_oracle(pg, real):
     st = noisy(I.buneman_plasma(8, 8, 8, ppc=4, seed=31))
@@ -207,6 +223,38 @@ def test_sort_is_bit_exact_with_oracle(pg):
     assert np.array_equal(out["px"], sp["px"][ref])
 
 
+@pytest.mark.parametrize("presorted", [0, 1])
+def test_sort_segments_of_every_length_bit_exact(pg, presorted):
+    """Key segments of 1 to 300 particles (one warp's register widths of 32,
+    64, 128 and 256 and the block fallback above), scattered over the input
+    or already in key order (the ascending fast path), against the oracle's
+    stable counting sort."""
+    box = I.Box(16, 8, 8, 0.1, 0.1, 0.1, 0.01)
+    lengths = [1, 2, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129, 200, 255, 256, 257, 300]
+    rng = np.random.default_rng(9)
+    counts = np.zeros(box.ncells, dtype=np.int64)
+    cells = rng.choice(box.ncells, size=3 * len(lengths), replace=False)
+    counts[cells] = np.tile(lengths, 3)
+    cell = np.repeat(np.arange(box.ncells), counts).astype(np.int32)
+    g = O.make_grid(box, tile=(8, 4, 4))
+    if presorted:
+        cell = cell[O.counting_sort(g, cell)]
+    else:
+        cell = cell[rng.permutation(cell.size)]
+    n = cell.size
+    sp = dict(q=-1.0, m=1.0, w=1.0, cell=cell, ox=rng.random(n), oy=rng.random(n), oz=rng.random(n),
+              px=rng.standard_normal(n), py=rng.standard_normal(n), pz=rng.standard_normal(n))
+    sim = pg.GpuSimulation(box, pg.BUNEMAN, particle_real=1, sort_every=0, tile=(8, 4, 4))
+    sid = sim.add_species(sp["q"], sp["m"], sp["w"], n)
+    sim.upload_particles(sid, sp)
+    sim.sort()
+    ref = O.counting_sort(g, sp["cell"])
+    assert np.array_equal(sim.download_permutation(sid).astype(np.int64), ref)
+    out = sim.download_particles(sid)
+    assert np.array_equal(out["cell"], sp["cell"][ref])
+    assert np.array_equal(out["px"], sp["px"][ref])
+
+
 def implicit_state(nx=8, ny=6, nz=5, ppc=3, seed=41, gamma=2.0):
     return noisy(I.beams_plasma(nx, ny, nz, ppc=ppc, beam_gamma=gamma, dt=0.2, seed=seed), seed=seed + 1)
 
@@ -236,6 +284,28 @@ def test_implicit_tiled_moments_match_oracle(pg, real, tile, ppc):
     against the oracle; pressure tensor at the particle's cells."""
     st = implicit_state(ppc=ppc)
     sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1, tile=tile)
+    sim.upload_state(st)
+    sim.updateElectroMagneticParameters()
+    J, mu, rho, rhs = sim.download_moments()
+    g = O.make_grid(st.box, pressure_compat=0)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    Jo, muo, rhoo, Pio, raw = O.implicit_moments(g, copy_species(st.species), E, B)
+    rhso = O.maxwell_rhs(g, E, B, Jo, rhoo)
+    tol = 1e-12 if real else TOL32
+    assert rel_err(mu, muo) < tol
+    assert rel_err(J, Jo) < tol
+    assert rel_err(rho, rhoo) < tol
+    assert rel_err(rhs, rhso) < tol
+
+
+@pytest.mark.parametrize("real,ppc", [(0, 40), (0, 70), (1, 40)])
+def test_implicit_tiled_moments_dense_cells_match_oracle(pg, real, ppc):
+    """Cells of 40 and 70 particles per species: several 32-particle chunks
+    per cell, every k-step of the tensor-core run sums and their
+    accumulation over the chunks of a cell (FP32), the transpose-reduction
+    over full warps (FP64)."""
+    st = implicit_state(ppc=ppc, seed=47)
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1, tile=(8, 6, 5))
     sim.upload_state(st)
     sim.updateElectroMagneticParameters()
     J, mu, rho, rhs = sim.download_moments()

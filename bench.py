@@ -422,10 +422,10 @@ def run_gb300(a):
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
     # DRAM bytes of one launch from an ncu capture of the same kernel on the
-    # 64^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 504.1 MB),
+    # 64^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 504.7 MB),
     # scaled by the units a launch processes (particles and cells grow alike)
     units = npart / (64 ** 3 * 2 * a.ppc) if a.ppc else 0.0
-    traffic = 504.1e6 * units if (nx * ny * nz) * 2 * a.ppc == npart else None
+    traffic = 504.7e6 * units if (nx * ny * nz) * 2 * a.ppc == npart else None
     roof = {"kernel": "k_push_deposit_tile<float,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "traffic_source": "ncu dram bytes of the 64^3 launch scaled by the particles per launch",

@@ -282,19 +282,22 @@ pic_status pic_profile(pic_ctx* ctx, int enable, double* phase_ms, long* launche
 /* ---- allocation-free diagnostics ---------------------------------------- */
 /* No counterpart in the reference.  The sums of pic_energy (same order of
  * outputs) for device arrays owned by the caller, for callers that cannot
- * allocate device memory where they need them: code inside CUDA stream
- * capture, hosts that fix a memory pool at start-up, embedders with their own
- * allocator.  Nothing is allocated: the partial sums live in a file-scope
- * device array of 548,864 bytes that every GPU loading the library keeps
- * until exit and that every call shares, so calls that overlap on the GPU
- * race.  The first call on a device looks that array's device address up
- * (cudaGetSymbolAddress) with the device current; make it before any stream
- * capture.  Limit: at most PIC_NOALLOC_MAX_SPECIES species (more returns
- * PIC_ERR_ARG) and fewer than 2^31 cells.
+ * allocate device memory where they need them: hosts that fix a memory pool
+ * at start-up and forbid later allocations, embedders whose device memory
+ * comes from their own allocator.  Nothing is allocated: the partial sums
+ * live in a file-scope device array of 548,864 bytes that every GPU loading
+ * the library keeps until exit and that every call shares, so calls that
+ * overlap on the GPU race.  The first call on a device looks that array's
+ * device address up (cudaGetSymbolAddress) with the device current and
+ * caches it; make it before any stream capture, and make no call on a
+ * device after a cudaDeviceReset of it.  Limit: at most
+ * PIC_NOALLOC_MAX_SPECIES species (more returns PIC_ERR_ARG) and fewer than
+ * 2^31 cells.
  * E, B: 3*nx*ny*nz FP64 device arrays (either may be NULL); per species s,
  * counts[s] particles of mass masses[s] and weight weights[s] with FP64
- * device momenta px[s], py[s], pz[s].  Runs on the given cudaStream_t and
- * returns when out (host) holds the result. */
+ * device momenta px[s], py[s], pz[s].  Runs on the given cudaStream_t, copies
+ * the sums to the host array out and synchronises that stream before it
+ * returns. */
 #define PIC_NOALLOC_MAX_SPECIES 16
 pic_status pic_energy_noalloc(int nx, int ny, int nz, double dx, double dy, double dz,
                               const double* E, const double* B, int nspecies, const long* counts,

@@ -17,7 +17,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "picpp_ref")
-REF_SRC = "/root/reference/PIC++"
+# PIC++ source directory (PIC++/*.cpp) for the reference build; the
+# reference is only built where this environment variable names it.
+REF_SRC = os.environ.get("PICPP_REFERENCE_SRC", "")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -213,11 +215,13 @@ def density_moments(grid, species):
 
 # ---------------------------------------------------------------- reference
 def reference_available() -> bool:
-    return os.path.isdir(REF_SRC)
+    return bool(REF_SRC) and os.path.isdir(REF_SRC)
 
 
 def build_reference() -> str:
-    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"])
+    if not reference_available():
+        raise RuntimeError("PICPP_REFERENCE_SRC does not name the PIC++ source directory")
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={REF_SRC}"])
     return REF_BIN
 
 

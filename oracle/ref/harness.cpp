@@ -10,9 +10,9 @@
 // output files are written.
 //
 // Input file (little endian):
-//   int32[8]   solver (0 Buneman, 1 implicit), nx, ny, nz, nspecies, steps,
-//              dump_first_step_moments, reserved
-//   float64[4] dx, dt, theta, eta
+//   int32[9]   solver (0 Buneman, 1 implicit), nx, ny, nz, nspecies, steps,
+//              dump_first_step_moments, density_pass, smoothing_count
+//   float64[5] dx, dt, theta, eta, smoothing_parameter
 //   per species: float64 q, m, w; int64 n; float64 x[n], y[n], z[n] (in
 //              [0, L) of the periodic box), px[n], py[n], pz[n]
 //   float64 E[3][nz][ny][nx], B[3][nz][ny][nx] on our periodic layout

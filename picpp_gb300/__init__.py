@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpicpp_gb300.so")
 
 PIC_OK = 0
+PIC_ERR_ARG = 1
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_STATE", 4: "ERR_NOMEM", 5: "ERR_NUMERIC",
           6: "ERR_NOT_CONVERGED"}
 PIC_NOALLOC_MAX_SPECIES = 16

@@ -2,11 +2,12 @@
 // pic_energy for device arrays the caller owns, without allocating anything.
 //
 // Who needs it: callers that may not allocate device memory at the point
-// where they want the diagnostics -- code running inside CUDA stream
-// capture (cudaMalloc is not capturable), hosts that hand the GPU to a
-// fixed memory pool and forbid allocations after start-up, and embedders
-// whose allocator is not the CUDA runtime's.  They keep E, B and the
-// momenta in their own buffers and pass device pointers in.
+// where they want the diagnostics -- hosts that hand the GPU to a fixed
+// memory pool at start-up and forbid allocations afterwards, and embedders
+// whose device memory comes from their own allocator rather than the CUDA
+// runtime's.  They keep E, B and the momenta in their own buffers and pass
+// device pointers in.  The call copies the six sums to the caller's host
+// array and synchronises the given stream before it returns.
 //
 // Scratch: the reduction partial sums live in one file-scope device array,
 // g_energy_scratch (548,864 bytes, 67 rows of 1024 doubles), which every GPU
@@ -19,7 +20,9 @@
 // symbol is only a stand-in).  The first call on a device looks the device
 // address up with cudaGetSymbolAddress while that device is current and
 // caches it; make that first call before any stream capture begins, since
-// the lookup may initialise the module.
+// the lookup may initialise the module.  cudaDeviceReset unloads the module,
+// so the cached address is not valid after a reset: do not call this entry
+// point on a device that was reset since its first call.
 #include <cmath>
 #include <mutex>
 

@@ -84,9 +84,8 @@ def test_gradients_match_oracle(pg):
     assert abs(L - Le) <= 2e-3 * Le
     offs, _ = NN.layer_offsets()
     for name, ci, co, w0, b0 in offs:
-        # the coarsest level sums over 64x fewer voxels: a BF16 rounding or
-        # ReLU decision that differs between FP32 and FP64 accumulation
-        # weighs more there
+        # the coarsest level sums over 64x fewer voxels: a BF16 rounding
+        # that differs between FP32 and FP64 accumulation weighs more there
         tol = 5e-2 if name.startswith("e2") else 2e-2
         assert rel_err(g[w0:b0], ge[w0:b0]) < tol, name
         assert rel_err(g[b0:b0 + co], ge[b0:b0 + co]) < tol, name

@@ -47,6 +47,9 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--implicit-grid", type=int, nargs=3, default=[256, 256, 64])
     p.add_argument("--implicit-ppc", type=int, default=64)
+    p.add_argument("--implicit-steps", type=int, default=200, help="steps of the implicit run (2 untimed)")
+    p.add_argument("--drift-steps", type=int, default=500, help="steps of the FP32-vs-FP64 explicit energy run")
+    p.add_argument("--no-energy", action="store_true")
     p.add_argument("--nn-steps", type=int, default=4000, help="training steps of the learned preconditioner")
     p.add_argument("--nn-batch", type=int, default=4, help="random fields per training step (Adam, lr 1e-3)")
     p.add_argument("--no-implicit", action="store_true")
@@ -91,27 +94,148 @@ def implicit_section(a):
     opts = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=600, tol=1e-8)
     out = {"workload": f"implicit_beams_{nx}x{ny}x{nz}_{ppc}ppc_2species", "particles": npart, "unknowns": 3 * N}
     stream = torch.cuda.ExternalStream(sim.stream)
-    # step 1 as warm-up, step 2 timed, each with the plain solve
-    sim.implicit_step(opts)
+    # the stated run: a.implicit_steps steps from the initial state, the first
+    # two untimed (warm-up), every later one bracketed by CUDA events on the
+    # library stream, the phase split accumulated over the timed steps; the
+    # total energy at the start and every 20 steps (outside the timed steps)
+    energy = [(0, sim.updateEnergy().tolist())]
+    for _ in range(2):
+        sim.implicit_step(opts)
     sim.profile(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    info = sim.implicit_step(opts)
-    e1.record(stream)
-    e1.synchronize()
+    times, its, restarts = [], [], []
+    for k in range(2, a.implicit_steps):
+        e0.record(stream)
+        info = sim.implicit_step(opts)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        its.append(info["iterations"])
+        restarts.append(info["restarts"])
+        if (k + 1) % 20 == 0 or k + 1 == a.implicit_steps:
+            energy.append((k + 1, sim.updateEnergy().tolist()))
     phases, launches = sim.profile(False)
-    ms = e0.elapsed_time(e1)
-    out["step_ms"] = ms
+    nt = len(times)
+    ms = statistics.median(times)
+    per = {k: v / nt for k, v in phases.items() if v > 0}
+    out["steps_run"] = a.implicit_steps
+    out["timed_steps"] = nt
+    out["step_ms"] = {"median": ms, "mean": statistics.fmean(times), "min": min(times), "max": max(times),
+                      "stdev": statistics.pstdev(times)}
     out["particle_steps_per_s"] = npart / (ms * 1e-3)
-    out["phase_ms"] = {k: v for k, v in phases.items() if v > 0}
-    out["plain"] = {"solver": "GMRES(30), classical Gram-Schmidt with selective second pass, FP64", "iterations": info["iterations"],
-                    "restarts": info["restarts"], "rel_residual": info["rel_residual"],
-                    "seconds": info["seconds"]}
+    out["phase_ms"] = per
+    out["phase_note"] = "deposit (the particle deposit kernel) is part of moments"
+    peak, src = _hbm_peak()
+    dep_bytes = 28 * npart + 352 * N    # particles read; J-hat, mu, rho-hat, Pi FP64 read-modify-write per cell
+    mov_bytes = 56 * npart + 96 * N     # particles read and written; E, B FP64 gathers per cell
+    roof = {}
+    for kern, ph, b, per_unit in (("k_implicit_deposit_tile<float>", "deposit", dep_bytes, "28 B/particle + 352 B/cell"),
+                                  ("k_implicit_push_tile<float>", "mover", mov_bytes, "56 B/particle + 96 B/cell")):
+        if per.get(ph):
+            ach = b / (per[ph] * 1e-3) / 1e9
+            roof[kern] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                          "peak_source": src, "algorithmic_bytes_per_launch": b, "bytes_per_unit": per_unit,
+                          "launch_ms": per[ph]}
+    # GMRES(30) bytes: Arnoldi step j (j basis vectors) moves 120 + 24 (2j + 5) B per cell, plus one
+    # operator apply (120 B/cell) for the residual at the start of each cycle and for the true residual
+    it_med = statistics.median(its)
+    gm_bytes = statistics.fmean(
+        N * (sum(120 + 24 * (2 * (i % 30 + 1) + 5) for i in range(n_it)) + 240 * (n_rs + 1))
+        for n_it, n_rs in zip(its, restarts))
+    if per.get("solve"):
+        ach = gm_bytes / (per["solve"] * 1e-3) / 1e9
+        roof["gmres_solve"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                               "peak_source": src, "algorithmic_bytes_per_solve": gm_bytes,
+                               "bytes_per_unit": "sum over iterations of 120 + 24 (2j + 5) B/cell + 240 B/cell per cycle",
+                               "solve_ms": per["solve"]}
+    out["roofline"] = roof
+    if per.get("moments"):
+        out["mass_matrix_deposits_per_s"] = npart * 8 * 9 / (per["moments"] * 1e-3)
+    if per.get("deposit"):
+        out["mass_matrix_deposits_per_s_kernel"] = npart * 8 * 9 / (per["deposit"] * 1e-3)
+    if per.get("solve"):
+        out["field_solves_per_s"] = 1.0 / (per["solve"] * 1e-3)
+    out["gmres_iterations"] = {"median": it_med, "min": min(its), "max": max(its)}
+    out["energy_drift"] = _drift(energy)
+    out["plain"] = {"solver": "GMRES(30), classical Gram-Schmidt with selective second pass, FP64",
+                    "iterations": info["iterations"], "restarts": info["restarts"],
+                    "rel_residual": info["rel_residual"], "seconds": info["seconds"]}
     if a.nn_steps > 0:
         out["learned_vs_plain"] = learned_solve(a, sim, box, w, opts)
     sim.close()
     if a.nn_steps > 0:
         out["learned_vs_plain_stiff"] = stiff_solve(a, w)
+    return out
+
+
+def _hbm_peak():
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _drift(series):
+    """Total energy (kinetic + electric + magnetic) of (step, pic_energy)
+    samples: relative change from the first sample to the last, and the
+    largest relative excursion."""
+    w = [(k, e[0] + e[1] + e[2]) for k, e in series]
+    w0 = w[0][1]
+    return {"steps": w[-1][0], "samples": len(w), "total_initial": w0, "total_final": w[-1][1],
+            "drift": (w[-1][1] - w0) / w0, "max_excursion": max(abs(v - w0) for _, v in w) / w0,
+            "field_energy_final": series[-1][1][1] + series[-1][1][2]}
+
+
+def energy_section(a, st):
+    """Energy bookkeeping of two stated runs (pic_energy, the reference's
+    updateEnergy): the Weibel pairs (32x32x1, 32 ppc per species, dt = 0.1,
+    seed 1) for 100 implicit steps in FP64, and the explicit workload's
+    state run for a.drift_steps steps with FP32 particles and fields and
+    with FP64 throughout from the same initial state, energy every 10
+    steps, with the FP32 run's field and energy differences from FP64."""
+    import numpy as np
+    import torch
+    import picpp_gb300 as P
+    from picpp_gb300 import initstate as I
+    out = {}
+    ws = I.weibel_pairs(32, 32, 1, seed=1)
+    sim = P.GpuSimulation(ws.box, P.IMPLICIT, particle_real=P.F64, pressure_compat=0, sort_every=1)
+    sim.upload_state(ws)
+    ser = [(0, sim.updateEnergy().tolist())]
+    t0 = time.perf_counter()
+    for k in range(100):
+        sim.implicit_step(P.solve_opts(P.GMRES_REFERENCE))
+        ser.append((k + 1, sim.updateEnergy().tolist()))
+    out["weibel_32x32x1_fp64"] = dict(_drift(ser), wall_s=time.perf_counter() - t0,
+                                      solver="GMRES, reference stopping rule")
+    sim.close()
+    runs = {}
+    for name, real in (("fp32", P.F32), ("fp64", P.F64)):
+        sim = P.GpuSimulation(st.box, P.BUNEMAN, particle_real=real, sort_every=a.sort_every)
+        sim.upload_state(st)
+        ser = [(0, sim.updateEnergy().tolist())]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(0, a.drift_steps, 10):
+            n = min(10, a.drift_steps - k)
+            sim.buneman_step(n)
+            ser.append((k + n, sim.updateEnergy().tolist()))
+        wall = time.perf_counter() - t0
+        E, B, _ = sim.download_fields()
+        runs[name] = (ser, E, B, wall)
+        sim.close()
+    s32, E32, B32, w32 = runs["fp32"]
+    s64, E64, B64, w64 = runs["fp64"]
+    tot32 = np.array([e[0] + e[1] + e[2] for _, e in s32])
+    tot64 = np.array([e[0] + e[1] + e[2] for _, e in s64])
+    rel = lambda x, y: float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))  # noqa: E731
+    nx, ny, nz = a.grid
+    out[f"buneman_{nx}x{ny}x{nz}_fp32_vs_fp64"] = {
+        "steps": a.drift_steps, "fp32": dict(_drift(s32), wall_s=w32), "fp64": dict(_drift(s64), wall_s=w64),
+        "energy_series_max_rel_diff": float(np.abs(tot32 - tot64).max() / np.abs(tot64).max()),
+        "field_rel_l2_diff_final": {"E": rel(E32, E64), "B": rel(B32, B64),
+                                    "B_minus_B0": rel(B32 - st.B, B64 - st.B)}}
     return out
 
 
@@ -419,12 +543,7 @@ def run_gb300(a):
     push_ms = phases["push_deposit"] / a.steps
     N = nx * ny * nz
     alg_bytes = 56 * npart + 24 * N   # particles r+w (28 B each way) + E,B gather (FP32) once per cell
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = peaks.get("hbm_gbs", 6800.0)
+    peak, peak_src = _hbm_peak()
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
     # DRAM bytes of one launch from an ncu capture of the same kernel on the
     # 64^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 504.7 MB),
@@ -434,7 +553,7 @@ def run_gb300(a):
     roof = {"kernel": "k_push_deposit_tile<float,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "traffic_source": "ncu dram bytes of the 64^3 launch scaled by the particles per launch",
-            "peak_source": "measured" if peaks else "fallback",
+            "peak_source": peak_src,
             "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": push_ms,
             "phase_ms_per_step": {k: v / a.steps for k, v in phases.items() if v > 0}}
 
@@ -483,6 +602,10 @@ def run_gb300(a):
     e2e_val = replica_value(npart, world, e2e_ms)
 
     sim.close()
+    energy = None
+    if not a.no_energy:
+        energy = energy_section(a, st)
+    del st
     imp = None
     if not a.no_implicit:
         imp = implicit_section(a)
@@ -499,7 +622,7 @@ def run_gb300(a):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms},
             "gpu_launches": int(round(launches_per_step * a.steps)), "clocks": ck,
-            "implicit_solve": imp,
+            "implicit_solve": imp, "energy_drift": energy,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -275,7 +275,10 @@ pic_status pic_download_density(pic_ctx* ctx, int species, double* conc, double*
  * kernels launched while recording. */
 typedef enum {
     PIC_PHASE_SORT = 0, PIC_PHASE_FIELDS = 1, PIC_PHASE_PUSH_DEPOSIT = 2, PIC_PHASE_ASSEMBLE = 3,
-    PIC_PHASE_MOMENTS = 4, PIC_PHASE_SOLVE = 5, PIC_PHASE_MOVER = 6, PIC_PHASE_COUNT = 7
+    PIC_PHASE_MOMENTS = 4, PIC_PHASE_SOLVE = 5, PIC_PHASE_MOVER = 6,
+    PIC_PHASE_DEPOSIT = 7,   /* the particle deposit kernels of the implicit moments alone
+                                (part of PIC_PHASE_MOMENTS, which adds the grid passes) */
+    PIC_PHASE_COUNT = 8
 } pic_phase;
 pic_status pic_profile(pic_ctx* ctx, int enable, double* phase_ms, long* launches);
 

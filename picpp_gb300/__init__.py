@@ -36,7 +36,7 @@ EXPORTS = [
     "pic_nn_train", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
     "pic_save_checkpoint", "pic_load_checkpoint",
 ]
-PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover"]
+PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover", "deposit"]
 
 
 class PicError(RuntimeError):

@@ -274,7 +274,7 @@ pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
             int grid = ctx->ntiles < kNumSM * 8 ? ctx->ntiles : kNumSM * 8;
             {
                 Phase ph(ctx, PIC_PHASE_PUSH_DEPOSIT, 1);
-                PK<T>::push_deposit_tiled(s, g, ctx->tg, ctx->ts, S, ctx->E, ctx->B, (T*)ctx->Jpart, ctx->Jfix,
+                PK<T>::push_deposit_tiled(s, g, ctx->tg, ctx->ts, S, ctx->E, ctx->B, (double*)ctx->Jpart, ctx->Jfix,
                                           grid, PK<T>::tile_smem_bytes(ctx->ts));
             }
             {
@@ -283,7 +283,7 @@ pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
             }
             {
                 Phase ph(ctx, PIC_PHASE_ASSEMBLE, 1);
-                PK<T>::assemble_j(s, g, ctx->tg, ctx->ts, (const T*)ctx->Jpart, ctx->Jfix, ctx->J);
+                PK<T>::assemble_j(s, g, ctx->tg, ctx->ts, (const double*)ctx->Jpart, ctx->Jfix, ctx->J);
             }
         } else {
             {
@@ -350,8 +350,10 @@ pic_status implicit_moments(pic_ctx* ctx) {
             Ef = (const T*)ctx->fields32;
             Bf = (const T*)(ctx->fields32 + 3 * N);
         }
+        Phase dep(ctx, PIC_PHASE_DEPOSIT, 0);
         PK<T>::implicit_deposit_tiled(s, g, ctx->tg, bk, S, Ef, Bf, ctx->Jh, ctx->mu, ctx->rho, ctx->Pi);
     } else {
+        Phase dep(ctx, PIC_PHASE_DEPOSIT, 0);
         for (auto& sp : ctx->sp)
             PK<T>::implicit_deposit(s, g, view<T>(sp), sp.q, sp.m, sp.w, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu,
                                     ctx->rho, ctx->Pi, compat, ctx->ga);
@@ -521,7 +523,7 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
         ok = ok && A(&ctx->B, ctx->rsz * 3 * N);
         ok = ok && A(&ctx->J, sizeof(double) * 3 * N);
         ok = ok && A(&ctx->Jfix, sizeof(double) * 3 * N);
-        ok = ok && A(&ctx->Jpart, ctx->rsz * 3 * (size_t)ts.jcells * ctx->ntiles);
+        ok = ok && A(&ctx->Jpart, sizeof(double) * 3 * (size_t)ts.jcells * ctx->ntiles);
     } else {
         ctx->pi_len = c.pressure_compat ? 9LL * ga.cex * ga.cey * ga.cez : 9 * N;
         ctx->jg_len = c.pressure_compat ? 3LL * ctx->nex * ctx->ney * ctx->nez : 3 * N;

@@ -21,7 +21,8 @@
 //      atomics are compare-and-swap loops that collapse under address
 //      conflicts); the block sums are exact and order-independent.  FP64
 //      particles: FP64 shared atomics;
-//   3. writes the block, unreduced, to a per-tile partial buffer.
+//   3. writes the block, unreduced, to a per-tile FP64 partial buffer (for
+//      FP32 particles the exact fixed-point sums).
 // k_assemble_j then sums the partials of every cell in a fixed order into
 // the FP64 current grid: no global floating-point atomics on the fast path.
 // A particle more than one cell outside its tile takes the global path
@@ -177,7 +178,7 @@ __device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __r
 template <typename TP, typename TF, int CT>
 __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
                                                                        const TF* __restrict__ E, const TF* __restrict__ B,
-                                                                       TP* __restrict__ Jpart, double* __restrict__ Jfix,
+                                                                       double* __restrict__ Jpart, double* __restrict__ Jfix,
                                                                        float fx_scale) {
     constexpr bool kFixed = sizeof(TP) == sizeof(float);   // FP32 particles: fixed-point block
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -332,26 +333,47 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
 #pragma unroll
                     for (int q2 = 0; q2 < 12; ++q2) aB[q2] = TP(0);
                 }
-                TP aA[12];
-                segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);   // zeros off the reduction
+                // a particle that stays in its cell (no relay shift) has both
+                // segments in that cell: one set of 12 sums carries both, and
+                // the old-side pass is left to the particles that crossed (its
+                // 12 values are formed only then, from the six kept in s1)
+                if (keyA == keyB && keyA >= 0) {
+                    TP aA[12];
+                    segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);
+#pragma unroll
+                    for (int q2 = 0; q2 < 12; ++q2) aB[q2] += aA[q2];
+                    keyA = -1 - lane;
+                }
+                const bool crossed = __any_sync(0xffffffffu, keyA >= 0);
                 if constexpr (kFixed) {
                     if (run_sum<TP>(keyB, aB) && keyB >= 0)
                         add_slots_fx(sLo, sHi, (int)JC, keyB, jx, jx * jy, ey, ez, (const float*)aB, fx_scale);
-                    if (run_sum<TP>(keyA, aA) && keyA >= 0)
-                        add_slots_fx(sLo, sHi, (int)JC, keyA, jx, jx * jy, ey, ez, (const float*)aA, fx_scale);
                 } else {
                     if (run_sum<TP>(keyB, aB) && keyB >= 0) add_slots<TP>(sJ, JC, keyB, jx, jx * jy, ey, ez, aB);
-                    if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);
+                }
+                if (crossed) {
+                    // lanes without an old-side segment hold unique negative
+                    // keys: runs of one lane, whatever their values
+                    TP aA[12];
+                    segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);
+                    if constexpr (kFixed) {
+                        if (run_sum<TP>(keyA, aA) && keyA >= 0)
+                            add_slots_fx(sLo, sHi, (int)JC, keyA, jx, jx * jy, ey, ez, (const float*)aA, fx_scale);
+                    } else {
+                        if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);
+                    }
                 }
             }
         }
         __syncthreads();
-        TP* dst = Jpart + (long long)tile * 3 * JC;
+        double* dst = Jpart + (long long)tile * 3 * JC;
         if (kFixed) {
+            // the exact block sum: |v| < 2^53 and a power-of-two scale, so the
+            // FP64 partial is the fixed-point value itself
             const double inv = 1.0 / (double)fx_scale;
             for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) {
                 const long long v = (long long)sHi[e] * 4294967296ll + (long long)sLo[e];
-                dst[e] = TP((double)v * inv);
+                dst[e] = (double)v * inv;
             }
         } else {
             for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) dst[e] = sJ[e];
@@ -363,7 +385,7 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
 // J[c] = Jfix[c] + sum of every tile partial that covers cell c, tiles and
 // periodic images visited in a fixed order (deterministic, FP64).
 template <typename TP>
-__global__ void __launch_bounds__(256) k_assemble_j(GridP g, TileGeom t, TileShape s, const TP* __restrict__ Jpart,
+__global__ void __launch_bounds__(256) k_assemble_j(GridP g, TileGeom t, TileShape s, const double* __restrict__ Jpart,
                                                     const double* __restrict__ Jfix, double* __restrict__ J) {
     const long long JC = s.jcells;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
@@ -403,10 +425,10 @@ __global__ void __launch_bounds__(256) k_assemble_j(GridP g, TileGeom t, TileSha
                 for (int d = 0; d < cnt[2]; ++d) {
                     long long tile = ((long long)cand_t[2][d] * t.nty + cand_t[1][b]) * t.ntx + cand_t[0][a];
                     long long e = ((long long)cand_l[2][d] * s.jy + cand_l[1][b]) * s.jx + cand_l[0][a];
-                    const TP* src = Jpart + tile * 3 * JC;
-                    acc[0] += double(src[e]);
-                    acc[1] += double(src[JC + e]);
-                    acc[2] += double(src[2 * JC + e]);
+                    const double* src = Jpart + tile * 3 * JC;
+                    acc[0] += src[e];
+                    acc[1] += src[JC + e];
+                    acc[2] += src[2 * JC + e];
                 }
         J[c] = acc[0]; J[g.N + c] = acc[1]; J[2 * g.N + c] = acc[2];
     }

@@ -710,7 +710,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
                 T prevDisp[3];
                 int it = 0;
-                while (err > picard_bound<T>(picard_mom_tol<T>(), momNorm) && cerr > picard_bound<T>(picard_pos_tol<T>(), dxN) && it < 3) {
+                while (picard_continue<T>(err, momNorm, cerr, dxN, it)) {
                     ++it;
                     const T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
 #pragma unroll

@@ -38,9 +38,9 @@ struct PK {
     // fused gather/push/deposit over tiles (boris_tile.cuh); smem bytes and
     // grid size chosen by the caller
     static void push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh,
-                                   const SpeciesSet<T>& S, const void* E, const void* B, T* Jpart, double* Jfix,
+                                   const SpeciesSet<T>& S, const void* E, const void* B, double* Jpart, double* Jfix,
                                    int grid, size_t smem);
-    static void assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const T* Jpart,
+    static void assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const double* Jpart,
                            const double* Jfix, double* J);
     static size_t tile_smem_bytes(const TileShape& sh);
     static void implicit_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w,

@@ -182,7 +182,7 @@ size_t PK<T>::tile_smem_bytes(const TileShape& sh) {
 
 template <typename T>
 void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh,
-                               const SpeciesSet<T>& S, const void* E, const void* B, T* Jpart, double* Jfix,
+                               const SpeciesSet<T>& S, const void* E, const void* B, double* Jpart, double* Jfix,
                                int grid, size_t smem) {
     static bool attr_set = false;
     if (!attr_set) {
@@ -209,7 +209,7 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
 }
 
 template <typename T>
-void PK<T>::assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const T* Jpart,
+void PK<T>::assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const double* Jpart,
                        const double* Jfix, double* J) {
     k_assemble_j<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, t, sh, Jpart, Jfix, J);
 }

@@ -1,0 +1,164 @@
+"""The seeded workloads at their stated sizes (or, where the single-threaded
+oracle cannot finish a step in seconds, the same physics on a smaller box)
+on the CUDA path against the FP64 oracle, through the C ABI.
+
+Bounds: FP64 path 1e-11 relative (max norm over the array, relative to the
+array's largest entry), FP32 push 1e-5 relative after one step, positions
+in units of the cell size.  Every measured error is printed (pytest -rP
+shows it) so that the numbers behind the bounds can be read off a run.
+
+* Weibel pairs, 32x32x1, 32 particles per cell and species, dx = 0.2,
+  dt = 0.1, theta = 0.5, zero initial fields, 100 implicit steps in FP64
+  (GMRES with the reference's stopping rule), seed 1: every field, momentum
+  and position, and the total energy after every step.
+* Electron-proton plasma (mass ratio 100, theta_e = 0.1, theta_p = 1e-3,
+  B0 along x with sigma = 0.1, dx = 0.1, Courant 0.45, 16 particles per cell
+  and species) on a 32^3 box, seed 2: one explicit step with FP32 particles
+  and fields against FP64, and the FP64 path against the oracle.
+* Counter-streaming beams (gamma = 10, mass ratio 25, 64 particles per cell
+  and species, dx = dt = 0.5, B0 along z with sigma = 0.01) on a 64x64x16
+  box, seed 3: one implicit step on the FP32 push and on the FP64 path.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from fixtures import copy_species, periodic_dist, rel_err
+from picpp_gb300 import initstate as I
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-11
+TOL32 = 1e-5
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import picpp_gb300 as P
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    P.load_library()
+    return P
+
+
+def by_id(d):
+    o = np.argsort(d["id"])
+    return {k: v[o] for k, v in d.items()}
+
+
+def particle_errors(box, gpu, ref):
+    """(largest position difference in cells, largest momentum error relative
+    to the species' largest momentum component) of one species."""
+    L = (box.nx * box.dx, box.ny * box.dy, box.nz * box.dz)
+    x, y, z = I.positions(box, gpu)
+    xr, yr, zr = I.positions(box, ref)
+    dpos = max(periodic_dist(a, r, l).max() / d
+               for a, r, l, d in ((x, xr, L[0], box.dx), (y, yr, L[1], box.dy), (z, zr, L[2], box.dz)))
+    pscale = max(np.abs(ref[k]).max() for k in ("px", "py", "pz"))
+    dmom = max(np.abs(gpu[k] - ref[k]).max() for k in ("px", "py", "pz")) / pscale
+    return dpos, dmom
+
+
+def report(name, **errs):
+    print(f"[parity] {name}: " + ", ".join(f"{k}={v:.3e}" for k, v in errs.items()))
+
+
+def total_energy(e):
+    return e[0] + e[1] + e[2]
+
+
+# ------------------------------------------------------------------ Weibel 32x32x1, 100 steps, FP64
+@pytest.fixture(scope="module")
+def weibel_oracle():
+    st = I.weibel_pairs(32, 32, 1, seed=1)
+    g = O.make_grid(st.box, pressure_compat=0)
+    sp = copy_species(st.species)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    energy = [O.energy(g, sp, E, B)]
+    for _ in range(100):
+        O.implicit_step(g, sp, E, B)
+        energy.append(O.energy(g, sp, E, B))
+    return st, sp, E, B, np.array(energy)
+
+
+def test_weibel_32x32x1_100_steps_fp64_matches_oracle(pg, weibel_oracle):
+    st, spo, Eo, Bo, eo = weibel_oracle
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, pressure_compat=0, sort_every=1)
+    sim.upload_state(st)
+    energy = [sim.updateEnergy()]
+    for _ in range(100):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+        energy.append(sim.updateEnergy())
+    energy = np.array(energy)
+    E, B, _ = sim.download_fields()
+    eE, eB = rel_err(E.reshape(-1), Eo), rel_err(B.reshape(-1), Bo)
+    pe = [particle_errors(st.box, by_id(sim.download_particles(s)), spo[s]) for s in range(2)]
+    tot, toto = total_energy(energy.T), total_energy(eo.T)
+    e_err = np.abs(tot - toto).max() / np.abs(toto).max()
+    drift, drifto = (tot[-1] - tot[0]) / tot[0], (toto[-1] - toto[0]) / toto[0]
+    report("weibel 32x32x1 100 steps fp64", E=eE, B=eB, pos_cells=max(p[0] for p in pe),
+           mom=max(p[1] for p in pe), energy_series=e_err, drift_gpu=drift, drift_oracle=drifto)
+    assert eE < TOL64 and eB < TOL64
+    for dpos, dmom in pe:
+        assert dpos < TOL64 and dmom < TOL64
+    assert e_err < TOL64
+    sim.close()
+
+
+# ------------------------------------------------------------------ electron-proton, 32^3, one explicit step
+@pytest.fixture(scope="module")
+def buneman_oracle():
+    st = I.buneman_plasma(32, 32, 32, ppc=16, seed=2)
+    g = O.make_grid(st.box)
+    sp = copy_species(st.species)
+    E, B = st.E.copy(), st.B.copy()
+    J = O.buneman_step(g, sp, E, B)
+    return st, sp, E, B, J
+
+
+@pytest.mark.parametrize("real", [0, 1])
+def test_buneman_32cubed_one_step_matches_fp64_oracle(pg, buneman_oracle, real):
+    st, spo, Eo, Bo, Jo = buneman_oracle
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real, sort_every=1)
+    sim.upload_state(st)
+    sim.buneman_step(1)
+    E, B, J = sim.download_fields()
+    eE, eB, eJ = rel_err(E, Eo), rel_err(B, Bo), rel_err(J, Jo.reshape(J.shape))
+    pe = [particle_errors(st.box, by_id(sim.download_particles(s)), spo[s]) for s in range(2)]
+    report(f"buneman 32^3 one step {'fp64' if real else 'fp32'}", E=eE, B=eB, J=eJ,
+           pos_cells=max(p[0] for p in pe), mom=max(p[1] for p in pe))
+    tol = TOL64 if real else TOL32
+    assert eE < tol and eB < tol and eJ < tol
+    for dpos, dmom in pe:
+        assert dpos < tol and dmom < tol
+    sim.close()
+
+
+# ------------------------------------------------------------------ beams, 64x64x16, one implicit step
+@pytest.fixture(scope="module")
+def beams_oracle():
+    st = I.beams_plasma(64, 64, 16, ppc=64, seed=3)
+    g = O.make_grid(st.box, pressure_compat=0)
+    sp = copy_species(st.species)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    O.implicit_step(g, sp, E, B)
+    return st, sp, E, B
+
+
+@pytest.mark.parametrize("real", [0, 1])
+def test_beams_64x64x16_one_implicit_step_matches_fp64_oracle(pg, beams_oracle, real):
+    st, spo, Eo, Bo = beams_oracle
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1)
+    sim.upload_state(st)
+    info = sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    E, B, _ = sim.download_fields()
+    eE, eB = rel_err(E.reshape(-1), Eo), rel_err(B.reshape(-1), Bo)
+    pe = [particle_errors(st.box, by_id(sim.download_particles(s)), spo[s]) for s in range(2)]
+    report(f"beams 64x64x16 one step {'fp64' if real else 'fp32'}", E=eE, B=eB, pos_cells=max(p[0] for p in pe),
+           mom=max(p[1] for p in pe), gmres_iterations=info["iterations"])
+    tol = TOL64 if real else TOL32
+    assert eE < tol and eB < tol
+    for dpos, dmom in pe:
+        assert dpos < tol and dmom < tol
+    sim.close()

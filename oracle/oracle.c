@@ -472,6 +472,7 @@ void orc_implicit_deposit(const orc_grid* g, const orc_particles* p,
     gaxis ax = mk_axis(g->nx), ay = mk_axis(g->ny), az = mk_axis(g->nz);
     const long PN = g->pressure_compat ? (long)ax.ce * ay.ce * az.ce : N;
     for (long n = 0; n < p->n; ++n) {
+        if (p->cell[n] < 0) continue;   /* escaped (wall_x), erased after the step */
         double mom[3] = {p->px[n], p->py[n], p->pz[n]};
         double gam = gamma_of(mom, p->m);
         double v[3]; velocity_of(mom, p->m, v);
@@ -503,7 +504,11 @@ void orc_implicit_deposit(const orc_grid* g, const orc_particles* p,
             for (int bb = 0; bb < 2; ++bb)
                 for (int c = 0; c < 2; ++c) {
                     if ((g->ny == 1 && bb) || (g->nz == 1 && c)) continue;
-                    long id = IX(g, X[a], Y[bb], Z[c]);
+                    /* conductor wall: the ghost cell left of the wall is
+                     * mirrored onto the first cell (momentum_collecting.cpp:
+                     * 560-568) */
+                    const int mirror = g->wall_x && X[a] < 0;
+                    long id = IX(g, mirror ? -X[a] - 1 : X[a], Y[bb], Z[c]);
                     double corr = wx[a] * wy[bb] * wz[c] / vol;
                     rho[id] += qw * corr;
                     long pid;
@@ -512,7 +517,7 @@ void orc_implicit_deposit(const orc_grid* g, const orc_particles* p,
                          * (interior cell i is r = i + 2, neighbours r +- 1,
                          * no wrap); y, z: the loop counters j, k
                          * (momentum_collecting.cpp:565,577). */
-                        int rx = ax.n > 1 ? X[a] + ax.g : 0;
+                        int rx = ax.n > 1 ? (mirror ? -X[a] - 1 : X[a]) + ax.g : 0;
                         int ry = ay.n > 1 ? bb : 0;
                         int rz = az.n > 1 ? c : 0;
                         pid = ((long)rz * ay.ce + ry) * ax.ce + rx;
@@ -531,7 +536,7 @@ static void pi_fold_reference(const orc_grid* g, double* P) {
     const long PN = (long)ax.ce * ay.ce * az.ce;
 #define PG(d, x, y, z) P[(d) * PN + ((long)(z) * ay.ce + (y)) * ax.ce + (x)]
     for (int d = 0; d < 9; ++d) {
-        if (ax.n > 1)
+        if (ax.n > 1 && !g->wall_x)   /* no x fold next to a wall (one rank) */
             for (int y = 0; y < ay.ce; ++y)
                 for (int z = 0; z < az.ce; ++z)
                     for (int t = 0; t < 3; ++t) {
@@ -592,6 +597,19 @@ static void pi_fold_reference(const orc_grid* g, double* P) {
         div = ((rX - lX) / g->dx) + ((rY - lY) / g->dy) + ((rZ - lZ) / g->dz);                         \
     }
 
+/* The node moments at a conductor wall after the particle deposits
+ * (momentum_collecting.cpp:496-505): J-hat and mu vanish on the wall node. */
+void orc_wall_node_moments(const orc_grid* g, double* J, double* mu) {
+    if (!g->wall_x) return;
+    const long N = NC(g);
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j) {
+            const long c = IX(g, 0, j, k);
+            for (int d = 0; d < 3; ++d) J[d * N + c] = 0;
+            for (int d = 0; d < 9; ++d) mu[d * N + c] = 0;
+        }
+}
+
 /* updateElectroMagneticParameters after the deposits
  * (momentum_collecting.cpp:590-663): fold Pi, J-hat -= eta dt div(Pi) at
  * every node, rho-hat -= theta dt div(J-hat) at every cell.  Writes J-hat on
@@ -618,6 +636,10 @@ void orc_implicit_moments_finish(const orc_grid* g, double* J, const double* rho
 #undef PT
         for (long c = 0; c < 3 * N; ++c) J[c] = J[c] - dJ[c] * g->eta * g->dt;
         free(dJ);
+        if (g->wall_x)   /* J-hat at the wall node (momentum_collecting.cpp:638-646) */
+            for (int k = 0; k < g->nz; ++k)
+                for (int j = 0; j < g->ny; ++j)
+                    for (int d = 0; d < 3; ++d) J[d * N + IX(g, 0, j, k)] = 0;
 #define JF(d, ii, jj, kk) J[(d) * N + IX(g, ii, jj, kk)]
         for (int k = -1; k < ez - 1; ++k)
             for (int j = -1; j < ey - 1; ++j)
@@ -647,6 +669,8 @@ void orc_implicit_moments_finish(const orc_grid* g, double* J, const double* rho
                 int edge = (i == 0 || i == ax.ne - 1 || j == 0 || j == ay.ne - 1 || k == 0 || k == az.ne - 1);
                 if (!single && !edge) { DIV_PI_BODY(PT, i, j, k, out) }
                 for (int d = 0; d < 3; ++d) JG(d, i, j, k) = J[d * N + src] - out[d] * g->eta * g->dt;
+                if (g->wall_x && i <= ax.g)   /* the wall node and the ghosts left of it */
+                    for (int d = 0; d < 3; ++d) JG(d, i, j, k) = 0;
             }
     for (int k = 0; k < ez; ++k)
         for (int j = 0; j < ey; ++j)
@@ -712,8 +736,52 @@ void orc_maxwell_rhs(const orc_grid* g, const double* E, const double* B,
                     rhs[d * N + c] = E[d * N + c] + (rot[d] * cf - (J[d * N + c] * 4 * PI_D)) * td
                                    - (grad[d] * cf2 * g->theta * g->theta * g->dt * g->dt * 4 * PI_D);
             }
+    if (g->wall_x) {
+        /* right parts of the boundary rows (wall_rows_apply): the wall's
+         * Gauss row -pi (four cells of rho-hat around the node, fields.cpp:
+         * 759-760), E_y = E_z = 0; the open boundary's constant field
+         * (ConstantBoundaryFieldEvaluator, initializeFluxFromRight,
+         * initialization.cpp:5207) */
+        for (int k = 0; k < g->nz; ++k)
+            for (int j = 0; j < g->ny; ++j) {
+                const long c0 = IX(g, 0, j, k);
+                rhs[c0] = -PI_D * (RH(0, j, k) + RH(0, j - 1, k) + RH(0, j, k - 1) + RH(0, j - 1, k - 1));
+                rhs[N + c0] = 0;
+                rhs[2 * N + c0] = 0;
+                for (int i = g->nx - 2; i < g->nx; ++i) {
+                    const long c = IX(g, i, j, k);
+                    for (int d = 0; d < 3; ++d) rhs[d * N + c] = g->e_right[d];
+                }
+            }
+    }
 #undef BF
 #undef RH
+}
+
+/* Rows of the Maxwell system at the x boundaries of a conductor-wall box
+ * (evaluateMaxwellEquationMatrix, fields.cpp:519-548, one rank).  Storage
+ * column 0 is the wall node (reference index 2): createSuperConductorLeft-
+ * Equation (fields.cpp:690-765), E_x(0) - E_x(1) for 3-D boxes and
+ * E_y = E_z = 0; columns nx - 2 and nx - 1 are the open boundary node and
+ * the ghost node beyond it (reference xnumber + 2 and + 3): identity rows
+ * of createFreeRightEquation (fields.cpp:767-781).  The physical nodes are
+ * 0 .. nx - 2 and the cells 0 .. nx - 3; cell nx - 2 is the ghost cell
+ * beyond the open boundary and cell nx - 1 the ghost cell left of the wall
+ * (reference index 1), so the periodic index wrap of every stencil reaches
+ * the reference's ghost values. */
+static void wall_rows_apply(const orc_grid* g, const double* x, double* y) {
+    const long N = NC(g);
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j) {
+            const long c0 = IX(g, 0, j, k), c1 = IX(g, 1, j, k);
+            y[c0] = x[c0] * 1.0 + x[c1] * -1.0;
+            y[N + c0] = x[N + c0];
+            y[2 * N + c0] = x[2 * N + c0];
+            for (int i = g->nx - 2; i < g->nx; ++i) {
+                const long c = IX(g, i, j, k);
+                for (int d = 0; d < 3; ++d) y[d * N + c] = x[d * N + c];
+            }
+        }
 }
 
 /* Matrix-free restatement of the Maxwell operator rows assembled by
@@ -819,6 +887,7 @@ void orc_maxwell_apply(const orc_grid* g, const double* mu, const double* x, dou
                     y[a * N + c0] = acc;
                 }
             }
+    if (g->wall_x) wall_rows_apply(g, x, y);
 #undef MU
 #undef XV
 }
@@ -846,7 +915,8 @@ int orc_gmres(const orc_grid* g, const double* mu, const double* rhs, double* x,
     V[0] = (double*)malloc(sizeof(double) * L);
     for (long c = 0; c < L; ++c) V[0][c] = rhs[c] / norm;
     double normR = sqrt(dotv(L, V[0], V[0]));
-    long dim = L;
+    /* matrixDimension of the reference: 3 x the physical cells */
+    long dim = g->wall_x ? 3L * (g->nx - 2) * g->ny * g->nz : L;
     double tolRel = g->gmres_tol / (double)dim;
     if (tolRel < 1e-15) tolRel = 1e-15;
     /* H[i][j], Q[i][j], R[i][j] dense, (cap x cap) */
@@ -953,14 +1023,74 @@ void orc_field_update(const orc_grid* g, const double* Et, const double* E,
                 long c = IX(g, i, j, k);
                 for (int d = 0; d < 3; ++d) Bnew[d * N + c] = B[d * N + c] - rot[d] * (g->cfix * g->dt);
             }
+    if (g->wall_x) {
+        /* the ghost cell beyond the open boundary takes the boundary field,
+         * the ghost cell left of the wall the first cell's new field
+         * (evaluateMagneticField, fields.cpp:2738-2756) */
+        for (int k = 0; k < g->nz; ++k)
+            for (int j = 0; j < g->ny; ++j) {
+                const long cr = IX(g, g->nx - 2, j, k), cl = IX(g, g->nx - 1, j, k), c0 = IX(g, 0, j, k);
+                for (int d = 0; d < 3; ++d) {
+                    Bnew[d * N + cr] = g->b_right[d];
+                    Bnew[d * N + cl] = Bnew[d * N + c0];
+                }
+            }
+    }
 #undef EF
 }
 
-/* moveParticle (mover.cpp:194-491), periodic box: predictor, then up to 3
- * Picard iterations re-gathering E^{n+theta} (nodes) and B^n (cells) at
+/* Particle::setMomentumByV (particle.cpp:337-364): p = m v below
+ * v^2 < relativisticPrecision = 1e-4 (constants.h:39), m gamma(v) v above. */
+static inline void momentum_by_v(const double v[3], double m, double p[3]) {
+    const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    if (v2 < 1e-4) {
+        for (int d = 0; d < 3; ++d) p[d] = v[d] * m;
+        return;
+    }
+    const double gam = 1 / sqrt(1 - v2);
+    for (int d = 0; d < 3; ++d) p[d] = v[d] * (m * gam);
+}
+
+/* x in length units from the origin of our storage -> cell and offset. */
+static inline void set_x(double x, double idx, int* c, double* u) {
+    const double a = x * idx;
+    const double f = floor(a);
+    *c = (int)f;
+    *u = a - f;
+    if (*u >= 1.0) { *u -= 1.0; *c += 1; }
+}
+
+/* The reflection of moveParticle at the conductor wall (mover.cpp:247-260
+ * after the predictor, mover.cpp:312-330 inside the Picard loop), wall at
+ * x = 0: the trial position x = x^n + eta dt vbar crossed the wall; the
+ * particle is mirrored with the rest of the step, |vbar_x| (1 - eta) dt,
+ * carries on in y and z by vbar (1 - eta) dt, and leaves with the
+ * predictor's velocity, its x component made positive. */
+static void wall_reflect(const orc_grid* g, const double id[3], const int nn[3], int ci[3], double u0[3],
+                         const double xtrial, const double mv[3], const double vnew[3], double m, double pout[3]) {
+    const double redt = (1 - g->eta) * g->dt;
+    const double edt = g->eta * g->dt;
+    set_x(-xtrial + fabs(mv[0] * redt), id[0], &ci[0], &u0[0]);
+    for (int d = 1; d < 3; ++d) {
+        advance_axis(&u0[d], &ci[d], (mv[d] * edt) * id[d], nn[d]);
+        advance_axis(&u0[d], &ci[d], (mv[d] * redt) * id[d], nn[d]);
+    }
+    const double vr[3] = {fabs(vnew[0]), vnew[1], vnew[2]};
+    momentum_by_v(vr, m, pout);
+}
+
+/* moveParticle (mover.cpp:194-491): predictor, then up to 3 Picard
+ * iterations re-gathering E^{n+theta} (nodes) and B^n (cells) at
  * x^n + eta dt vbar, then x^{n+1} = x^n + dt vbar.  alpha is recomputed
  * from E^n, B^n at x^n, exactly as evaluateParticlesRotationTensor
- * (mover.cpp:810-841) stored it. */
+ * (mover.cpp:810-841) stored it.  With a conductor wall (g->wall_x) a trial
+ * position left of the wall reflects the particle there and then
+ * (mover.cpp:247-260, 312-330); a final position left of it is mirrored
+ * with p_x reversed (mover.cpp:435-445); a final position right of the open
+ * boundary x = (nx - 2) dx marks the particle escaped (cell = -1,
+ * mover.cpp:447-458), to be erased after the step
+ * (eraseEscapedPaticles, mover.cpp:167-192).  Escaped particles are
+ * skipped. */
 void orc_implicit_push(const orc_grid* g, orc_particles* p, const double* E,
                        const double* B, const double* Et) {
     const double beta = 0.5 * p->q * g->dt / p->m;
@@ -968,9 +1098,12 @@ void orc_implicit_push(const orc_grid* g, orc_particles* p, const double* E,
     const double qdt = p->q * g->dt;
     const double id[3] = {1.0 / g->dx, 1.0 / g->dy, 1.0 / g->dz};
     const int nn[3] = {g->nx, g->ny, g->nz};
+    const double xright = (g->nx - 2) * g->dx;
     for (long n = 0; n < p->n; ++n) {
+        if (p->cell[n] < 0) continue;
         int ci[3]; decode(g, p->cell[n], &ci[0], &ci[1], &ci[2]);
         double u0[3] = {p->ox[n], p->oy[n], p->oz[n]};
+        const double xold = (ci[0] + u0[0]) * g->dx;
         double mom0[3] = {p->px[n], p->py[n], p->pz[n]};
         double gam = gamma_of(mom0, p->m);
         double v[3]; velocity_of(mom0, p->m, v);
@@ -988,45 +1121,73 @@ void orc_implicit_push(const orc_grid* g, orc_particles* p, const double* E,
         double vnew[3]; evaluate_velocity(pnew, p->m, vnew);
         double mv[3];
         for (int d = 0; d < 3; ++d) mv[d] = v[d] * (1 - g->eta) + vnew[d] * g->eta;
-        double disp[3];   /* current trial displacement from x^n, length units */
-        for (int d = 0; d < 3; ++d) disp[d] = mv[d] * edt;
-        /* velocityHat = (alpha * gamma) * v (mover.cpp:276) */
-        double vh[3];
-        for (int a = 0; a < 3; ++a)
-            vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
-        double momNorm = sqrt(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
-        double err = sqrt((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
-                          (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
-        double cerr = g->dx;
-        double prevDisp[3] = {disp[0], disp[1], disp[2]};
-        double newDisp[3] = {disp[0], disp[1], disp[2]};
-        int it = 0;
-        while (err > 1e-14 * momNorm && cerr > 1e-8 * g->dx && it < 3) {
-            ++it;
-            double prevMom[3] = {pnew[0], pnew[1], pnew[2]};
-            for (int d = 0; d < 3; ++d) prevDisp[d] = newDisp[d];
-            double re[3];
-            for (int a = 0; a < 3; ++a) re[a] = al[3 * a] * e[0] + al[3 * a + 1] * e[1] + al[3 * a + 2] * e[2];
-            for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
-            for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
-            /* trial position and re-gather */
-            int tc[3]; double tu[3];
-            for (int d = 0; d < 3; ++d) {
-                tc[d] = ci[d]; tu[d] = u0[d];
-                advance_axis(&tu[d], &tc[d], newDisp[d] * id[d], nn[d]);
+        int reflected = 0;
+        if (g->wall_x && xold + mv[0] * edt < 0) {
+            wall_reflect(g, id, nn, ci, u0, xold + mv[0] * edt, mv, vnew, p->m, pnew);
+            reflected = 1;
+        }
+        if (!reflected) {
+            double disp[3];   /* current trial displacement from x^n, length units */
+            for (int d = 0; d < 3; ++d) disp[d] = mv[d] * edt;
+            /* velocityHat = (alpha * gamma) * v (mover.cpp:276) */
+            double vh[3];
+            for (int a = 0; a < 3; ++a)
+                vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
+            double momNorm = sqrt(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
+            double err = sqrt((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
+                              (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
+            double cerr = g->dx;
+            double prevDisp[3] = {disp[0], disp[1], disp[2]};
+            double newDisp[3] = {disp[0], disp[1], disp[2]};
+            int it = 0;
+            while (err > 1e-14 * momNorm && cerr > 1e-8 * g->dx && it < 3) {
+                ++it;
+                double prevMom[3] = {pnew[0], pnew[1], pnew[2]};
+                for (int d = 0; d < 3; ++d) prevDisp[d] = newDisp[d];
+                double re[3];
+                for (int a = 0; a < 3; ++a) re[a] = al[3 * a] * e[0] + al[3 * a + 1] * e[1] + al[3 * a + 2] * e[2];
+                for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
+                for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
+                if (g->wall_x && xold + newDisp[0] < 0) {
+                    wall_reflect(g, id, nn, ci, u0, xold + newDisp[0], mv, vnew, p->m, pnew);
+                    reflected = 1;
+                    break;
+                }
+                /* trial position and re-gather */
+                int tc[3]; double tu[3];
+                for (int d = 0; d < 3; ++d) {
+                    tc[d] = ci[d]; tu[d] = u0[d];
+                    advance_axis(&tu[d], &tc[d], newDisp[d] * id[d], nn[d]);
+                }
+                int tcell = (int)IX(g, tc[0], tc[1], tc[2]);
+                orc_gather_node(g, tcell, tu[0], tu[1], tu[2], Et, e);
+                orc_gather_cell(g, tcell, tu[0], tu[1], tu[2], B, b);
+                double mvxb[3]; cross(mv, b, mvxb);
+                for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
+                err = sqrt((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) + (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
+                           (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
+                cerr = sqrt((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) + (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
+                            (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
             }
-            int tcell = (int)IX(g, tc[0], tc[1], tc[2]);
-            orc_gather_node(g, tcell, tu[0], tu[1], tu[2], Et, e);
-            orc_gather_cell(g, tcell, tu[0], tu[1], tu[2], B, b);
-            double mvxb[3]; cross(mv, b, mvxb);
-            for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
-            err = sqrt((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) + (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
-                       (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
-            cerr = sqrt((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) + (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
-                        (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
+            if (!reflected) {
+                if (g->wall_x) {
+                    const double xn = xold + mv[0] * g->dt;
+                    if (xn < 0) {            /* mirrored, p_x reversed (reflectMomentumX) */
+                        set_x(-xn, id[0], &ci[0], &u0[0]);
+                        pnew[0] = -pnew[0];
+                    } else if (xn > xright) {
+                        p->cell[n] = -1;     /* escaped through the open boundary */
+                        continue;
+                    } else {
+                        advance_axis(&u0[0], &ci[0], (mv[0] * g->dt) * id[0], nn[0]);
+                    }
+                    for (int d = 1; d < 3; ++d) advance_axis(&u0[d], &ci[d], (mv[d] * g->dt) * id[d], nn[d]);
+                } else {
+                    for (int d = 0; d < 3; ++d) advance_axis(&u0[d], &ci[d], (mv[d] * g->dt) * id[d], nn[d]);
+                }
+            }
         }
         p->px[n] = pnew[0]; p->py[n] = pnew[1]; p->pz[n] = pnew[2];
-        for (int d = 0; d < 3; ++d) advance_axis(&u0[d], &ci[d], (mv[d] * g->dt) * id[d], nn[d]);
         p->ox[n] = u0[0]; p->oy[n] = u0[1]; p->oz[n] = u0[2];
         p->cell[n] = (int)IX(g, ci[0], ci[1], ci[2]);
     }
@@ -1082,6 +1243,7 @@ int orc_implicit_step(const orc_grid* g, orc_particles* sp, int nspecies,
     double* rho_ext = Pi + orc_pi_size(g);
     memset(work, 0, sizeof(double) * (size_t)orc_implicit_work_size(g));
     for (int s = 0; s < nspecies; ++s) orc_implicit_deposit(g, &sp[s], E, B, J, mu, rho, Pi);
+    orc_wall_node_moments(g, J, mu);
     orc_implicit_moments_finish(g, J, rho, Pi, rho_ext);
     if (!g->pressure_compat)
         for (int q = 0; q < g->smoothing_count; ++q) orc_smooth_moments(g, J, mu, rho_ext);

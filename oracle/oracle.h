@@ -41,6 +41,13 @@ typedef struct {
     double gmres_tol;       /* reference: maxErrorLevel = 1e-8               */
     int smoothing_count;    /* Simulation::smoothingCount passes per step     */
     double smoothing_parameter; /* Simulation::smoothingParameter             */
+    int wall_x;             /* 1: conductor wall at x = 0 and an open boundary
+                               at x = (nx - 2) dx (SUPER_CONDUCTOR_LEFT, one
+                               rank); storage columns nx - 2 and nx - 1 are the
+                               ghost cells beyond the open boundary and left of
+                               the wall (implicit path, 3-D boxes)           */
+    double e_right[3], b_right[3]; /* the open boundary's constant E and B
+                               (ConstantBoundaryFieldEvaluator)              */
 } orc_grid;
 
 typedef struct {
@@ -84,6 +91,9 @@ void orc_implicit_deposit(const orc_grid* g, const orc_particles* p,
                           double* J, double* mu, double* rho, double* Pi);
 long orc_pi_size(const orc_grid* g);
 long orc_rho_ext_size(const orc_grid* g);
+/* J-hat and mu vanish on the wall node of a conductor-wall box (no-op
+ * otherwise), after the deposits and before orc_implicit_moments_finish. */
+void orc_wall_node_moments(const orc_grid* g, double* J, double* mu);
 void orc_implicit_moments_finish(const orc_grid* g, double* J, const double* rho, double* Pi,
                                  double* rho_ext);
 void orc_maxwell_rhs(const orc_grid* g, const double* E, const double* B,

@@ -32,7 +32,8 @@ class Grid(C.Structure):
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
                 ("theta", C.c_double), ("eta", C.c_double), ("cfix", C.c_double),
                 ("pressure_compat", C.c_int), ("gmres_max_iter", C.c_int), ("gmres_tol", C.c_double),
-                ("smoothing_count", C.c_int), ("smoothing_parameter", C.c_double)]
+                ("smoothing_count", C.c_int), ("smoothing_parameter", C.c_double),
+                ("wall_x", C.c_int), ("e_right", C.c_double * 3), ("b_right", C.c_double * 3)]
 
 
 class Particles(C.Structure):
@@ -68,6 +69,7 @@ def lib():
         L.orc_counting_sort.argtypes = [g, C.c_long, _ip, _lp]
         L.orc_implicit_deposit.argtypes = [g, p, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_implicit_moments_finish.argtypes = [g, _dp, _dp, _dp, _dp]
+        L.orc_wall_node_moments.argtypes = [g, _dp, _dp]
         L.orc_pi_size.argtypes = [g]
         L.orc_pi_size.restype = C.c_long
         L.orc_rho_ext_size.argtypes = [g]
@@ -95,11 +97,26 @@ def _d(a: np.ndarray):
 
 
 def make_grid(box, tile=(8, 8, 8), pressure_compat=1, gmres_max_iter=50, gmres_tol=1e-8, smoothing_count=0,
-              smoothing_parameter=0.5) -> Grid:
+              smoothing_parameter=0.5, wall_x=0, e_right=(0.0, 0.0, 0.0), b_right=(0.0, 0.0, 0.0)) -> Grid:
+    """wall_x: conductor wall at x = 0 and open boundary at x = (nx - 2) dx,
+    with the boundary's constant fields e_right, b_right (oracle.h)."""
     t = [min(tile[0], box.nx), min(tile[1], box.ny), min(tile[2], box.nz)]
     return Grid(box.nx, box.ny, box.nz, t[0], t[1], t[2], box.dx, box.dy, box.dz, box.dt,
                 box.theta, box.eta, box.cfix, pressure_compat, gmres_max_iter, gmres_tol, smoothing_count,
-                smoothing_parameter)
+                smoothing_parameter, int(wall_x), (C.c_double * 3)(*e_right), (C.c_double * 3)(*b_right))
+
+
+def erase_escaped(species):
+    """eraseEscapedPaticles (mover.cpp:167-192): drops the particles the
+    mover marked escaped (cell = -1) from every array of each species dict,
+    keeping the order of the others."""
+    for sp in species:
+        keep = np.asarray(sp["cell"]) >= 0
+        if keep.all():
+            continue
+        for k, v in list(sp.items()):
+            if isinstance(v, np.ndarray) and v.shape[:1] == keep.shape:
+                sp[k] = np.ascontiguousarray(v[keep])
 
 
 def _as_particles(sp: dict) -> Particles:
@@ -128,6 +145,8 @@ def implicit_step(grid: Grid, species, E, B):
     work = np.zeros(lib().orc_implicit_work_size(C.byref(grid)))
     arr = _plist(species)
     it = lib().orc_implicit_step(C.byref(grid), arr, len(species), _d(E), _d(B), _d(work))
+    if grid.wall_x:
+        erase_escaped(species)
     return it
 
 
@@ -142,6 +161,7 @@ def implicit_moments(grid: Grid, species, E, B):
     for s in species:
         ps = _as_particles(s)
         L.orc_implicit_deposit(C.byref(grid), C.byref(ps), _d(E), _d(B), _d(J), _d(mu), _d(rho), _d(Pi))
+    L.orc_wall_node_moments(C.byref(grid), _d(J), _d(mu))
     raw = dict(J=J.copy(), rho=rho.copy(), Pi=Pi.copy())
     L.orc_implicit_moments_finish(C.byref(grid), _d(J), _d(rho), _d(Pi), _d(rho_ext))
     return J, mu, rho_ext, Pi, raw
@@ -226,18 +246,21 @@ def build_reference() -> str:
 
 
 def run_reference(solver: int, box, species, E, B, steps: int, dump: bool = False, density: bool = False,
-                  smoothing_count: int = 0, smoothing_parameter: float = 0.5):
+                  smoothing_count: int = 0, smoothing_parameter: float = 0.5, wall_x: int = 0,
+                  e_right=(0.0, 0.0, 0.0), b_right=(0.0, 0.0, 0.0)):
     """Runs the PIC++ reference (compiled from its own sources) on the state
-    and returns (species positions/momenta by input order, E, B, extras)."""
+    and returns (species positions/momenta by input order, E, B, extras).
+    With wall_x the reference runs SUPER_CONDUCTOR_LEFT on the nx - 2
+    physical cells of the box; escaped particles come back as NaN."""
     from picpp_gb300.initstate import positions
     exe = build_reference()
     N = box.ncells
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            f.write(struct.pack("<9i", solver, box.nx, box.ny, box.nz, len(species), steps, int(dump), int(density),
-                                smoothing_count))
-            f.write(struct.pack("<5d", box.dx, box.dt, box.theta, box.eta, smoothing_parameter))
+            f.write(struct.pack("<10i", solver, box.nx, box.ny, box.nz, len(species), steps, int(dump), int(density),
+                                smoothing_count, int(wall_x)))
+            f.write(struct.pack("<11d", box.dx, box.dt, box.theta, box.eta, smoothing_parameter, *e_right, *b_right))
             for sp in species:
                 x, y, z = positions(box, sp)
                 f.write(struct.pack("<3dq", sp["q"], sp["m"], sp["w"], len(sp["cell"])))

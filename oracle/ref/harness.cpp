@@ -10,9 +10,15 @@
 // output files are written.
 //
 // Input file (little endian):
-//   int32[9]   solver (0 Buneman, 1 implicit), nx, ny, nz, nspecies, steps,
-//              dump_first_step_moments, density_pass, smoothing_count
-//   float64[5] dx, dt, theta, eta, smoothing_parameter
+//   int32[10]  solver (0 Buneman, 1 implicit), nx, ny, nz, nspecies, steps,
+//              dump_first_step_moments, density_pass, smoothing_count, wall_x
+//   float64[11] dx, dt, theta, eta, smoothing_parameter, E_right[3], B_right[3]
+// wall_x = 1 (implicit runs): SUPER_CONDUCTOR_LEFT with a constant field
+// E_right, B_right at the open right boundary (initializeFluxFromRight,
+// initialization.cpp:5201-5207); the reference box then has nx - 2 cells
+// along x, the two remaining storage columns being its ghost cells beyond
+// the open boundary and left of the wall.  Particles that escape are
+// written back with NaN coordinates; no particles are injected.
 //   per species: float64 q, m, w; int64 n; float64 x[n], y[n], z[n] (in
 //              [0, L) of the periodic box), px[n], py[n], pz[n]
 //   float64 E[3][nz][ny][nx], B[3][nz][ny][nx] on our periodic layout
@@ -32,6 +38,7 @@
 #include "particle.h"
 #include "vector3d.h"
 #include "matrix3d.h"
+#include "boundaryFieldEvaluator.h"
 
 static void die(const char* m) { fprintf(stderr, "harness: %s\n", m); exit(2); }
 
@@ -49,13 +56,18 @@ int main(int argc, char** argv) {
     if (argc != 3) die("usage: harness in.bin out.bin");
     FILE* f = fopen(argv[1], "rb");
     if (!f) die("cannot open input");
-    int32_t hdr[9];
-    for (int a = 0; a < 9; ++a) hdr[a] = rd<int32_t>(f);
+    int32_t hdr[10];
+    for (int a = 0; a < 10; ++a) hdr[a] = rd<int32_t>(f);
     const int solver = hdr[0], nx = hdr[1], ny = hdr[2], nz = hdr[3], ns = hdr[4], steps = hdr[5], dump = hdr[6];
     const int density = hdr[7];   // 1: append updateDensityParameters' grids after the run
     const int smoothing = hdr[8];  // smoothingCount
     double dx = rd<double>(f), dt = rd<double>(f), theta = rd<double>(f), eta = rd<double>(f);
     const double smoothing_parameter = rd<double>(f);
+    const int wall = hdr[9];
+    double eright[3], bright[3];
+    for (int a = 0; a < 3; ++a) eright[a] = rd<double>(f);
+    for (int a = 0; a < 3; ++a) bright[a] = rd<double>(f);
+    if (wall && (solver != 1 || nx < 4 || ny < 2 || nz < 2)) die("wall_x needs an implicit 3-D box");
     Box bx{nx, ny, nz};
     const long N = (long)nx * ny * nz;
 
@@ -76,13 +88,13 @@ int main(int argc, char** argv) {
     int ppb[8] = {1, 0, 0, 0, 0, 0, 0, 0};
     double conc[8] = {1, 0, 0, 0, 0, 0, 0, 0};
     // Theoretical input type (1) keeps dx as given (initialization.cpp:449-460).
-    Simulation* S = new Simulation(nx, ny, nz, dx, 0.0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 1.0,
+    Simulation* S = new Simulation(wall ? nx - 2 : nx, ny, nz, dx, 0.0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 1.0,
                                    steps, 1e300, 1 << 30, 1 << 30, 1 << 30, 1 << 30, 0, 0.0, false, 8, ppb,
                                    conc, 1, 1, 0, dt, 1.0, comm);
     S->timing = false;
     S->verbosity = 0;
     S->solverType = solver == 0 ? BUNEMAN : IMPLICIT;
-    S->boundaryConditionTypeX = PERIODIC;
+    S->boundaryConditionTypeX = wall ? SUPER_CONDUCTOR_LEFT : PERIODIC;
     S->boundaryConditionTypeY = PERIODIC;
     S->boundaryConditionTypeZ = PERIODIC;
     S->smoothingCount = smoothing;
@@ -94,6 +106,8 @@ int main(int argc, char** argv) {
     S->E0 = Vector3d(0, 0, 0);
     S->B0 = Vector3d(0, 0, 0);
     S->createArrays();
+    Vector3d Er(eright[0], eright[1], eright[2]), Br(bright[0], bright[1], bright[2]);
+    if (wall) S->rightBoundaryFieldEvaluator = new ConstantBoundaryFieldEvaluator(Er, Br);
     // grid coordinates as Simulation::initialize builds them (initialization.cpp:1989-2023)
     S->xgrid[0] = S->leftX;
     for (int i = 1; i <= S->xnumberAdded; ++i) S->xgrid[i] = S->xgrid[0] + i * S->deltaX;
@@ -241,15 +255,19 @@ int main(int argc, char** argv) {
         if (p->number < 0 || p->number >= total) die("bad particle number");
         byNum[p->number] = p;
     }
-    for (long a = 0; a < total; ++a) if (!byNum[a]) die("particle lost");
+    for (long a = 0; a < total; ++a) if (!byNum[a] && !wall) die("particle lost");
     FILE* o = fopen(argv[2], "wb");
     if (!o) die("cannot open output");
-    const double Lx = nx * S->deltaX, Ly = ny * S->deltaY, Lz = nz * S->deltaZ;
+    const double Lx = (wall ? nx - 2 : nx) * S->deltaX, Ly = ny * S->deltaY, Lz = nz * S->deltaZ;
     for (int s = 0; s < ns; ++s) {
         int64_t n = sp[s].n; fwrite(&n, sizeof(n), 1, o);
         std::vector<double> X(n), Y(n), Z(n), PX(n), PY(n), PZ(n);
         for (long a = 0; a < n; ++a) {
             Particle* p = byNum[base[s] + a];
+            if (!p) {   // escaped through the open boundary
+                X[a] = Y[a] = Z[a] = PX[a] = PY[a] = PZ[a] = std::nan("");
+                continue;
+            }
             double x = p->coordinates.x - S->xgrid[2];
             double y = ny > 1 ? p->coordinates.y - S->ygrid[2] : p->coordinates.y - S->ygrid[0];
             double z = nz > 1 ? p->coordinates.z - S->zgrid[2] : p->coordinates.z - S->zgrid[0];

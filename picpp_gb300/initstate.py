@@ -166,6 +166,62 @@ def weibel_pairs(nx, ny, nz, dx=0.2, dt=0.1, ppc=32, theta_t=0.01, drift_v=0.5,
     return State(box, species, E, B)
 
 
+@dataclass
+class FlowState(State):
+    """A State of a box with a conductor wall at x = 0 and an open boundary
+    at x = (nx - 2) dx (storage columns nx - 2 and nx - 1 are the ghost
+    cells beyond the open boundary and left of the wall), with the
+    boundary's constant fields and the upstream flow that feeds it."""
+    e_right: tuple = (0.0, 0.0, 0.0)
+    b_right: tuple = (0.0, 0.0, 0.0)
+    flow_gamma: float = 1.0
+    temperatures: tuple = ()   # theta = kT / m c^2 per species
+    ppc: tuple = ()
+
+
+def shock_plasma(nx, ny, nz, dx=0.5, dt=0.4, ppc=(32, 32, 8), flow_gamma=1.5, theta_e=1e-3, sigma=0.04,
+                 angle_deg=60.0, mass_ratio=64.0, he_mass=256.0, he_fraction=0.1, theta=0.5, seed=5) -> FlowState:
+    """The reflecting-wall shock setup: a plasma of electrons, protons
+    (mass_ratio) and fully ionised helium (charge 2, mass he_mass, number
+    density he_fraction of the protons'), charge neutral, flowing towards
+    -x with Lorentz factor flow_gamma into a conductor wall at x = 0; every
+    species at the electron temperature (theta_e m_e / m_s); B0 at angle_deg
+    to x in the x-y plane with sigma = B0^2 / (4 pi flow_gamma sum_s n_s m_s);
+    E0 = -V0 x B0 (initializeFluxFromRight, PIC++/initialization.cpp:
+    5201-5207), Ey = Ez = 0 on the wall node.  Particles fill the nx - 2
+    physical cells; electron density 1 / (4 pi) (omega_pe = 1)."""
+    box = Box(nx, ny, nz, dx, dx, dx, dt, theta=theta)
+    rng = np.random.default_rng(seed)
+    n_e = 1.0 / FOUR_PI
+    n_p = n_e / (1.0 + 2.0 * he_fraction)
+    n_he = he_fraction * n_p
+    specs = ((-1.0, 1.0, n_e, ppc[0]), (1.0, mass_ratio, n_p, ppc[1]), (2.0, he_mass, n_he, ppc[2]))
+    v0 = math.sqrt(1.0 - 1.0 / (flow_gamma * flow_gamma))
+    phys = Box(nx - 2, ny, nz, dx, dx, dx, dt, theta=theta)
+    species, temps = [], []
+    for q, m, n, c in specs:
+        th = theta_e / m
+        sp = uniform_species(rng, phys, c, q, m, density_weight(box, n, c), th, flow_gamma, -1.0)
+        i = sp["cell"] % phys.nx
+        rest = sp["cell"] // phys.nx
+        sp["cell"] = (rest * nx + i).astype(np.int32)   # physical cells in the storage layout
+        species.append(sp)
+        temps.append(th)
+    rho_m = sum(n * m for _, m, n, _ in specs)
+    b0 = math.sqrt(sigma * FOUR_PI * flow_gamma * rho_m)
+    a = math.radians(angle_deg)
+    B0 = np.array([b0 * math.cos(a), b0 * math.sin(a), 0.0])
+    V0 = np.array([-v0, 0.0, 0.0])
+    E0 = -np.cross(V0, B0)
+    E = np.zeros((3, nz, ny, nx))
+    B = np.zeros((3, nz, ny, nx))
+    for d in range(3):
+        E[d] = E0[d]
+        B[d] = B0[d]
+    E[1, :, :, 0] = 0.0
+    E[2, :, :, 0] = 0.0
+    return FlowState(box, species, E, B, tuple(E0), tuple(B0), flow_gamma, tuple(temps), tuple(ppc))
+
 def positions(box: Box, sp: dict):
     """Physical positions in [0, L) from cell + offset (float64)."""
     c = sp["cell"].astype(np.int64)

@@ -52,3 +52,18 @@ def rel_err(a, b):
 def periodic_dist(a, b, L):
     d = np.asarray(a) - np.asarray(b)
     return np.abs((d + L / 2) % L - L / 2)
+
+
+def wall_of(f):
+    """(wall_x, e_right, b_right) of a golden case (the reflecting-wall
+    cases carry the open boundary's fields; the others are periodic)."""
+    w = f["extra"].get("wall")
+    if w is None:
+        return 0, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0)
+    return 1, tuple(float(v) for v in w[:3]), tuple(float(v) for v in w[3:6])
+
+
+def survivors(out):
+    """Indices of the particles a reference run kept (escaped ones come back
+    as NaN)."""
+    return np.nonzero(~np.isnan(np.asarray(out["x"])))[0]

@@ -62,6 +62,22 @@ def implicit(name, nx, ny, nz, ppc, steps, seed, beam_gamma=2.0, dt=0.2):
     _save(name, 1, st, steps, out_sp, E, B, extra)
 
 
+def wall(name, nx, ny, nz, ppc, steps, seed, flow_gamma=3.0, theta_e=0.3):
+    """The reflecting-wall setup (conductor wall at x = 0, open boundary at
+    x = (nx - 2) dx with constant fields) with a third of every species
+    turned towards the open boundary, so that particles both reflect and
+    escape; the reference runs SUPER_CONDUCTOR_LEFT without injection."""
+    st = I.shock_plasma(nx, ny, nz, ppc=ppc, flow_gamma=flow_gamma, theta_e=theta_e, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    for sp in st.species:
+        sp["px"][::3] = -sp["px"][::3]
+    st.E = st.E + 0.02 * rng.standard_normal(st.E.shape)
+    out_sp, E, B, extra = O.run_reference(1, st.box, st.species, st.E, st.B, steps, dump=True, wall_x=1,
+                                          e_right=st.e_right, b_right=st.b_right)
+    extra["wall"] = np.concatenate([np.asarray(st.e_right), np.asarray(st.b_right)])
+    _save(name, 1, st, steps, out_sp, E, B, extra)
+
+
 def density(name, nx, ny, nz, ppc, seed):
     """updateDensityParameters of a seeded state, one species per reference
     run (the harness gives every particle reference type 0)."""
@@ -78,7 +94,7 @@ def density(name, nx, ny, nz, ppc, seed):
 
 def main():
     if not O.reference_available():
-        sys.exit("the PIC++ reference tree is not available here")
+        sys.exit("the PIC++ reference tree is not available here (set PICPP_REFERENCE_SRC)")
     buneman("buneman_8x8x8_3steps", 8, 8, 8, 2, 3, 11)
     buneman("buneman_12x6x5_2steps", 12, 6, 5, 3, 2, 12)
     buneman("buneman_2d_16x8x1_3steps", 16, 8, 1, 4, 3, 13)
@@ -87,6 +103,8 @@ def main():
     implicit("implicit_gamma10_6x6x6_2steps", 6, 6, 6, 2, 2, 23, beam_gamma=10.0, dt=0.5)
     buneman("buneman_smooth_8x6x5_2steps", 8, 6, 5, 3, 2, 14, smoothing=(2, 0.4))
     buneman("buneman_smooth_2d_12x8x1_2steps", 12, 8, 1, 3, 2, 15, smoothing=(1, 0.5))
+    wall("wall_7x4x4_4steps", 7, 4, 4, (4, 4, 2), 4, 41)
+    wall("wall_10x6x5_2steps", 10, 6, 5, (3, 3, 2), 2, 42)
     density("density_8x6x5", 8, 6, 5, 3, 31)
     density("density_2d_8x8x1", 8, 8, 1, 4, 32)
 

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of
+from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of, survivors, wall_of
 from picpp_gb300 import initstate as I
 
 # The oracle keeps cell + offset where the reference keeps absolute FP64
@@ -117,3 +117,60 @@ def test_oracle_density_moments_match_reference(name):
     assert rel_err(en, x["energy"]) < 1e-13
     assert rel_err(vel, x["vel"]) < 1e-13
     assert rel_err(rho, x["rho"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", golden_names("wall"))
+def test_wall_moments_and_solve_match_reference(name):
+    """Conductor wall at x = 0, open boundary at x = (nx - 2) dx: the first
+    step's J-hat, mu, rho-hat, right part and E^{n+theta} on every node and
+    cell the reference keeps (the storage column nx - 1 is the reference's
+    ghost beyond the open boundary for nodes; its cell is the ghost left of
+    the wall, which the reference does not write out)."""
+    f = load(name)
+    st = f["state"]
+    w, er, br = wall_of(f)
+    g = O.make_grid(st.box, wall_x=w, e_right=er, b_right=br)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    J, mu, rho_ext, Pi, raw = O.implicit_moments(g, copy_species(st.species), E, B)
+    x = f["extra"]
+    b = st.box
+    node = lambda a, c: a.reshape(c, b.nz, b.ny, b.nx)[..., : b.nx - 1]   # noqa: E731
+    assert rel_err(node(mu, 9), node(x["mu"], 9)) < TOL
+    assert rel_err(node(J, 3), node(x["J"], 3)) < TOL
+    rho = O.rho_interior(g, rho_ext).reshape(b.nz, b.ny, b.nx)[..., : b.nx - 2]
+    assert rel_err(rho, x["rho"].reshape(b.nz, b.ny, b.nx)[..., : b.nx - 2]) < TOL
+    rhs = O.maxwell_rhs(g, E, B, J, rho_ext)
+    assert rel_err(node(rhs, 3), node(x["rhs"], 3)) < TOL
+    Et, it, relres = O.gmres(g, mu, rhs)
+    assert rel_err(node(Et, 3), node(x["Etheta"], 3)) < 1e-10
+
+
+@pytest.mark.parametrize("name", golden_names("wall"))
+def test_wall_steps_match_reference(name):
+    """Reflection at the wall, escape through the open boundary and the
+    fields after several steps: the same particles survive, with the
+    reference's positions and momenta."""
+    f = load(name)
+    st = f["state"]
+    w, er, br = wall_of(f)
+    g = O.make_grid(st.box, wall_x=w, e_right=er, b_right=br)
+    sp = copy_species(st.species)
+    for s in sp:
+        s["id"] = np.arange(len(s["cell"]))
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(f["steps"]):
+        O.implicit_step(g, sp, E, B)
+    b = st.box
+    sh = (3, b.nz, b.ny, b.nx)
+    assert rel_err(E.reshape(sh)[..., : b.nx - 1], f["E"].reshape(sh)[..., : b.nx - 1]) < TOL
+    assert rel_err(B.reshape(sh)[..., : b.nx - 2], f["B"].reshape(sh)[..., : b.nx - 2]) < TOL
+    escaped = 0
+    for s, o in zip(sp, f["out"]):
+        keep = survivors(o)
+        escaped += len(o["x"]) - len(keep)
+        assert np.array_equal(s["id"], keep)
+        x, y, z = I.positions(b, s)
+        assert np.abs(x - o["x"][keep]).max() < 1e-12
+        for k in ("px", "py", "pz"):
+            assert rel_err(s[k], o[k][keep]) < TOL
+    assert escaped > 0

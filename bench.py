@@ -50,6 +50,11 @@ def _args():
     p.add_argument("--implicit-steps", type=int, default=200, help="steps of the implicit run (2 untimed)")
     p.add_argument("--drift-steps", type=int, default=500, help="steps of the FP32-vs-FP64 explicit energy run")
     p.add_argument("--no-energy", action="store_true")
+    p.add_argument("--shock-grid", type=int, nargs=3, default=[4096, 256, 4])
+    p.add_argument("--shock-steps", type=int, default=20)
+    p.add_argument("--shock-drift-steps", type=int, default=100)
+    p.add_argument("--no-shock", action="store_true")
+    p.add_argument("--only-shock", action="store_true", help="run and print only the reflecting-wall shock section")
     p.add_argument("--nn-steps", type=int, default=4000, help="training steps of the learned preconditioner")
     p.add_argument("--nn-batch", type=int, default=4, help="random fields per training step (Adam, lr 1e-3)")
     p.add_argument("--no-implicit", action="store_true")
@@ -238,6 +243,140 @@ def energy_section(a, st):
                                     "B_minus_B0": rel(B32 - st.B, B64 - st.B)}}
     return out
 
+
+def _shock_sim(P, I, nx, ny, nz, real, seed, cap_factor=1.5, dt=0.4, dx=0.5):
+    """A wall box of the reflecting-wall shock setup filled on the device
+    (flow along -x), with its injector; returns (sim, injector, particles)."""
+    specs, E0, B0, v0 = I.shock_parameters(dx)
+    box = I.Box(nx, ny, nz, dx, dx, dx, dt, theta=0.5)
+    sim = P.GpuSimulation(box, P.IMPLICIT, particle_real=real, pressure_compat=0, sort_every=1,
+                          boundary_x=P.BOUNDARY_WALL_OPEN, e_right=tuple(E0), b_right=tuple(B0))
+    cells = (nx - 2) * ny * nz
+    total = 0
+    for s, (q, m, n, ppc, th) in enumerate(specs):
+        sim.add_species(q, m, I.density_weight(box, n, ppc), int(cap_factor * ppc * cells) + 64 * ny * nz)
+        sim.fill_species(s, ppc, seed * 10 + s, th, 1.5, -1)
+        total += ppc * cells
+    E, B = I.wall_fields(nx, ny, nz, E0, B0)
+    sim.upload_fields(E, B)
+    return sim, I.Injector(box, specs, 1.5, seed=seed), total
+
+
+def shock_section(a):
+    """The reflecting-wall shock: a conductor wall at x = 0 and an open
+    boundary on the right through which the upstream plasma (electrons 32,
+    protons of mass 64 32, He2+ of mass 256 8 particles per cell at 10% of
+    the proton density, flow gamma 1.5 towards -x, theta_e = 1e-3, B0 at 60
+    degrees to x with sigma = 0.04, dx = 0.5, dt = 0.4) keeps entering.
+    Storage a.shock_grid (the physical domain is two cells shorter along x),
+    FP32 push, FP64 GMRES(30) to a 1e-8 relative residual, a.shock_steps
+    timed steps with injection; the solve of the last step's system with
+    plain GMRES(30) and with FGMRES(30) + the network (trained on a periodic
+    64x64x4 box of the upstream plasma); and the total energy of an FP32 and
+    an FP64 run of a 512x64x4 box of the same setup for a.shock_drift_steps
+    steps with the same injected particles."""
+    import numpy as np
+    import torch
+    import picpp_gb300 as P
+    from picpp_gb300 import initstate as I
+    nx, ny, nz = a.shock_grid
+    out = {"workload": f"shock_wall_{nx}x{ny}x{nz}_32_32_8ppc_3species",
+           "physical_cells_x": nx - 2, "note": "storage nx includes the two ghost columns of the wall box"}
+    opts = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=600, tol=1e-8)
+    sim, inj, n0 = _shock_sim(P, I, nx, ny, nz, P.F32, 5)
+    out["particles_initial"] = n0
+    stream = torch.cuda.ExternalStream(sim.stream)
+
+    def count():
+        return sum(sim.download_particles(s, with_ids=False)["cell"].size for s in range(3))
+
+    def inject():
+        k = 0
+        for s, new in enumerate(inj.step()):
+            sim.append_particles(s, new)
+            k += new["cell"].size
+        return k
+
+    inject()
+    sim.implicit_step(opts)   # warm-up
+    e0 = sim.updateEnergy().tolist()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, its, injected, psteps = [], [], 0, 0
+    sim.profile(True)
+    for _ in range(a.shock_steps):
+        ev0.record(stream)
+        injected += inject()
+        info = sim.implicit_step(opts)
+        ev1.record(stream)
+        ev1.synchronize()
+        times.append(ev0.elapsed_time(ev1))
+        its.append(info["iterations"])
+    phases, _ = sim.profile(False)
+    n_end = count()
+    e1 = sim.updateEnergy().tolist()
+    ms = statistics.median(times)
+    out["timed_steps"] = a.shock_steps
+    out["step_ms"] = {"median": ms, "min": min(times), "max": max(times)}
+    out["particles_end"] = n_end
+    out["injected_per_step"] = injected / max(a.shock_steps, 1)
+    out["particle_steps_per_s"] = 0.5 * (n0 + n_end) / (ms * 1e-3)
+    out["phase_ms"] = {k: v / a.shock_steps for k, v in phases.items() if v > 0}
+    out["gmres_iterations"] = {"median": statistics.median(its), "max": max(its)}
+    out["total_energy"] = {"after_warmup": e0[0] + e0[1] + e0[2], "end": e1[0] + e1[1] + e1[2],
+                           "note": "open system: injected and escaped particles carry energy in and out"}
+    if a.nn_steps > 0:
+        # the network on a periodic box of the upstream plasma
+        specs, E0, B0, v0 = I.shock_parameters()
+        tb = I.Box(64, 64, 4, 0.5, 0.5, 0.5, 0.4, theta=0.5)
+        tsim = P.GpuSimulation(tb, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=1)
+        for s, (q, m, n, ppc, th) in enumerate(specs):
+            tsim.add_species(q, m, I.density_weight(tb, n, ppc), ppc * tb.ncells)
+            tsim.fill_species(s, ppc, 70 + s, th, 1.5, -1)
+        tsim.upload_fields(*I.wall_fields(64, 64, 4, E0, B0))
+        tsim.implicit_step(opts)
+        tsim.updateElectroMagneticParameters()
+        tsim.nn_init(1)
+        tr = tsim.nn_train(steps=a.nn_steps // 2, batch=a.nn_batch, lr=1e-3, seed=5, smooth_max=2)
+        params = tsim.nn_get_params()
+        tsim.close()
+        sim.nn_set_params(params)
+        sim.updateElectroMagneticParameters()
+        _, mu, _, rhs = sim.download_moments()
+        plain = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=600, tol=1e-8)
+        learned = P.solve_opts(P.FGMRES_LEARNED, restart=30, max_iter=600, tol=1e-8)
+        sim.maxwell_solve(mu, rhs, plain)
+        sim.maxwell_solve(mu, rhs, learned)
+        _, ip = sim.maxwell_solve(mu, rhs, plain)
+        _, il = sim.maxwell_solve(mu, rhs, learned)
+        out["learned_vs_plain"] = {
+            "plain": {k: ip[k] for k in ("iterations", "restarts", "rel_residual", "seconds")},
+            "learned": {k: il[k] for k in ("iterations", "restarts", "used_fallback", "rel_residual", "seconds")},
+            "speedup": ip["seconds"] / il["seconds"] if il["seconds"] > 0 else None,
+            "train": {"box": [64, 64, 4], "steps": tr["steps"], "seconds": tr["seconds"],
+                      "first_loss": tr["first_loss"], "last_loss": tr["last_loss"]}}
+    sim.close()
+    # FP32 against FP64 on a smaller box, the same injected particles
+    runs = {}
+    for name, real in (("fp32", P.F32), ("fp64", P.F64)):
+        s2, inj2, _ = _shock_sim(P, I, 512, 64, 4, real, 6)
+        ser = []
+        for k in range(a.shock_drift_steps):
+            for sp_id, new in enumerate(inj2.step()):
+                s2.append_particles(sp_id, new)
+            s2.implicit_step(opts)
+            if k % 10 == 9 or k == a.shock_drift_steps - 1:
+                ser.append(s2.updateEnergy())
+        E2, B2, _ = s2.download_fields()
+        runs[name] = (np.array(ser), E2, B2)
+        s2.close()
+    t32 = runs["fp32"][0][:, :3].sum(axis=1)
+    t64 = runs["fp64"][0][:, :3].sum(axis=1)
+    rel = lambda x, y: float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))  # noqa: E731
+    out["fp32_vs_fp64_512x64x4"] = {"steps": a.shock_drift_steps,
+                                    "energy_series_max_rel_diff": float(np.abs(t32 - t64).max() / np.abs(t64).max()),
+                                    "field_rel_l2_diff_final": {"E": rel(runs["fp32"][1], runs["fp64"][1]),
+                                                                "B": rel(runs["fp32"][2], runs["fp64"][2])}}
+    return out
 
 def _beams(box, ppc, w, seeds):
     """A simulation of the implicit beam plasma on box (device fill), with
@@ -609,6 +748,9 @@ def run_gb300(a):
     imp = None
     if not a.no_implicit:
         imp = implicit_section(a)
+    shock = None
+    if not a.no_shock:
+        shock = shock_section(a)
     if rank == 0:
         cpu = None
         if not a.no_cpu_baseline:
@@ -622,7 +764,7 @@ def run_gb300(a):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms},
             "gpu_launches": int(round(launches_per_step * a.steps)), "clocks": ck,
-            "implicit_solve": imp, "energy_drift": energy,
+            "implicit_solve": imp, "energy_drift": energy, "shock": shock,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -633,6 +775,10 @@ def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.only_shock:
+        import picpp_gb300 as P
+        P.load_library()
+        print(json.dumps({"shock": shock_section(a)}), flush=True)
     elif a.only_implicit:
         import picpp_gb300 as P
         P.load_library()

@@ -68,7 +68,26 @@ typedef struct {
                                 needs pressure_compat = 0)                              */
     double smoothing_parameter; /* smoothingParameter s: weights s/2, 1-s, s/2 per axis
                                 (createSmoothingMatrix, smoothing.cpp:105-137)          */
+    int boundary_x;          /* pic_boundary_x                                          */
+    double e_right[3], b_right[3]; /* PIC_BOUNDARY_WALL_OPEN: the open boundary's constant
+                                fields (ConstantBoundaryFieldEvaluator, set up by
+                                initializeFluxFromRight, initialization.cpp:5201-5207) */
 } pic_config;
+
+/* Boundary along x.  PIC_BOUNDARY_WALL_OPEN is boundaryConditionTypeX =
+ * SUPER_CONDUCTOR_LEFT of one rank (implicit runs of 3-D boxes, no
+ * smoothing): a conductor wall at x = 0 and an open
+ * boundary at x = (nx - 2) dx.  The physical domain is nodes 0 .. nx - 2 and
+ * cells 0 .. nx - 3 of the nx-cell storage; storage cell nx - 2 is the ghost
+ * cell beyond the open boundary (boundary field), cell nx - 1 the ghost cell
+ * left of the wall (the first cell's field), node nx - 1 the ghost node
+ * beyond the open boundary.  Particles may not be placed in the two ghost
+ * columns.  The mover reflects particles at the wall (mover.cpp:247-260,
+ * 312-330, 435-445) and erases those that cross the open boundary
+ * (mover.cpp:447-458, eraseEscapedPaticles mover.cpp:167-192); particles
+ * are fed in with pic_append_particles (injectNewParticles,
+ * mover.cpp:910-1000, with the caller's particles). */
+typedef enum { PIC_BOUNDARY_PERIODIC = 0, PIC_BOUNDARY_WALL_OPEN = 1 } pic_boundary_x;
 
 /* Field-solve options for the implicit Maxwell system. */
 typedef enum {
@@ -120,11 +139,21 @@ pic_status pic_upload_particles(pic_ctx* ctx, int species, long n, const int* ce
                                 const double* ox, const double* oy, const double* oz,
                                 const double* px, const double* py, const double* pz,
                                 const int* ids);
-/* Fills a species on the device with ppc particles per cell: uniform in-cell
- * offsets, Maxwell-Juttner momenta of temperature theta (kT/mc^2), boosted
- * along x with Lorentz factor drift_gamma (> 1) -- every other particle
- * towards -x when alternate_drift is set.  Seeded and independent of the
- * launch shape.  A workload generator for runs too large to build on the
+/* Appends n particles (same arrays as pic_upload_particles) to a species,
+ * after the ones it holds: the injection of new particles at an open
+ * boundary (injectNewParticles, PIC++/mover.cpp:910-1000, whose positions
+ * and momenta come from the caller here).  ids NULL numbers them on from
+ * the species' last number. */
+pic_status pic_append_particles(pic_ctx* ctx, int species, long n, const int* cell,
+                                const double* ox, const double* oy, const double* oz,
+                                const double* px, const double* py, const double* pz,
+                                const int* ids);
+/* Fills a species on the device with ppc particles per cell (the physical
+ * cells of a wall box): uniform in-cell offsets, Maxwell-Juttner momenta of
+ * temperature theta (kT/mc^2), boosted along x with Lorentz factor
+ * drift_gamma (> 1) -- towards +x with alternate_drift 0, every other
+ * particle towards -x with 1, all towards -x with -1.  Seeded and
+ * independent of the launch shape.  A workload generator for runs too large to build on the
  * host; no reference counterpart (the reference's initialisers,
  * PIC++/initialization.cpp:8145-8574, are out of scope). */
 pic_status pic_fill_species(pic_ctx* ctx, int species, int ppc, unsigned long long seed, double theta,

@@ -21,11 +21,13 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_STATE", 4: "ERR_NOMEM", 
           6: "ERR_NOT_CONVERGED"}
 PIC_NOALLOC_MAX_SPECIES = 16
 BUNEMAN, IMPLICIT = 0, 1
+BOUNDARY_PERIODIC, BOUNDARY_WALL_OPEN = 0, 1
 F32, F64 = 0, 1
 GMRES_REFERENCE, GMRES_RESTARTED, FGMRES_LEARNED = 0, 1, 2
 
 EXPORTS = [
     "pic_create", "pic_destroy", "pic_last_error", "pic_stream", "pic_add_species", "pic_upload_particles",
+    "pic_append_particles",
     "pic_download_particles", "pic_upload_fields", "pic_download_fields", "pic_tristan_evaluate_b_half_step",
     "pic_move_particles", "pic_tristan_update_flux", "pic_tristan_evaluate_e", "pic_buneman_step",
     "pic_update_electromagnetic_parameters", "pic_evaluate_electric_field", "pic_evaluate_magnetic_field",
@@ -51,7 +53,8 @@ class Config(C.Structure):
                 ("theta", C.c_double), ("eta", C.c_double), ("cfix", C.c_double),
                 ("solver", C.c_int), ("particle_real", C.c_int), ("field_real", C.c_int),
                 ("pressure_compat", C.c_int), ("sort_every", C.c_int), ("tile", C.c_int * 3),
-                ("max_species", C.c_int), ("smoothing_count", C.c_int), ("smoothing_parameter", C.c_double)]
+                ("max_species", C.c_int), ("smoothing_count", C.c_int), ("smoothing_parameter", C.c_double),
+                ("boundary_x", C.c_int), ("e_right", C.c_double * 3), ("b_right", C.c_double * 3)]
 
 
 class SolveOpts(C.Structure):
@@ -106,6 +109,7 @@ def load_library(path: str | None = None):
     L.pic_stream.restype = vp
     L.pic_add_species.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_long, _ip]
     L.pic_upload_particles.argtypes = [vp, C.c_int, C.c_long, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+    L.pic_append_particles.argtypes = [vp, C.c_int, C.c_long, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
     L.pic_download_particles.argtypes = [vp, C.c_int, C.POINTER(C.c_long), _ip, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
     L.pic_upload_fields.argtypes = [vp, _dp, _dp]
     L.pic_download_fields.argtypes = [vp, _dp, _dp, _dp]
@@ -177,7 +181,11 @@ class GpuSimulation:
     ``download_*``; each method mirrors the member function of that name."""
 
     def __init__(self, box, solver=BUNEMAN, particle_real=F32, field_real=None, pressure_compat=1,
-                 sort_every=1, tile=(8, 8, 8), max_species=8, smoothing_count=0, smoothing_parameter=0.5):
+                 sort_every=1, tile=(8, 8, 8), max_species=8, smoothing_count=0, smoothing_parameter=0.5,
+                 boundary_x=BOUNDARY_PERIODIC, e_right=(0.0, 0.0, 0.0), b_right=(0.0, 0.0, 0.0)):
+        """boundary_x = BOUNDARY_WALL_OPEN: conductor wall at x = 0 and open
+        boundary at x = (nx - 2) dx with the constant fields e_right, b_right
+        (include/picpp_gb300.h, pic_boundary_x)."""
         self.L = load_library()
         self.box = box
         cfg = Config()
@@ -193,6 +201,10 @@ class GpuSimulation:
         cfg.smoothing_parameter = smoothing_parameter
         cfg.tile[0], cfg.tile[1], cfg.tile[2] = tile
         cfg.max_species = max_species
+        cfg.boundary_x = boundary_x
+        for a in range(3):
+            cfg.e_right[a] = e_right[a]
+            cfg.b_right[a] = b_right[a]
         self.cfg = cfg
         self.ctx = C.c_void_p()
         st = self.L.pic_create(C.byref(cfg), C.byref(self.ctx))
@@ -241,6 +253,15 @@ class GpuSimulation:
         ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
         self._ck(self.L.pic_upload_particles(self.ctx, sid, n, _i(cell), *[_d(a) for a in arrs], _i(ids)))
 
+    def append_particles(self, sid, sp, ids=None):
+        """Adds the particles of sp after the species' current ones
+        (injection at an open boundary)."""
+        n = len(sp["cell"])
+        arrs = [np.ascontiguousarray(sp[k], dtype=np.float64) for k in ("ox", "oy", "oz", "px", "py", "pz")]
+        cell = np.ascontiguousarray(sp["cell"], dtype=np.int32)
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
+        self._ck(self.L.pic_append_particles(self.ctx, sid, n, _i(cell), *[_d(a) for a in arrs], _i(ids)))
+
     def download_particles(self, sid, with_ids=True):
         n = C.c_long()
         self._ck(self.L.pic_download_particles(self.ctx, sid, C.byref(n), None, None, None, None, None, None, None,
@@ -256,9 +277,11 @@ class GpuSimulation:
         return out
 
     def fill_species(self, sid, ppc, seed, theta, drift_gamma=1.0, alternate_drift=False):
-        """Device-side seeded loading (pic_fill_species)."""
-        self._ck(self.L.pic_fill_species(self.ctx, sid, int(ppc), int(seed), float(theta), float(drift_gamma),
-                                         1 if alternate_drift else 0))
+        """Device-side seeded loading (pic_fill_species).  alternate_drift:
+        False / 0 drift along +x, True / 1 every other particle along -x,
+        -1 every particle along -x."""
+        mode = int(alternate_drift) if not isinstance(alternate_drift, bool) else (1 if alternate_drift else 0)
+        self._ck(self.L.pic_fill_species(self.ctx, sid, int(ppc), int(seed), float(theta), float(drift_gamma), mode))
 
     def upload_state(self, state):
         """Species (adding them on first use) and fields of an initstate.State."""

@@ -29,6 +29,7 @@ struct Species {
     int* perm = nullptr;
     int* off = nullptr;     // nkeys + 1
     bool sorted = false;
+    long long next_id = 0;  // id of the next appended particle when the caller gives none
 };
 
 template <typename T>
@@ -71,6 +72,8 @@ struct pic_ctx {
     Net* net = nullptr;      // learned preconditioner, created by pic_nn_init / pic_nn_set_params
     double* smooth_tmp = nullptr;   // scratch of the smoothing passes (max(9N, rho-hat ext))
     bool fresh_sort = false;        // particles sorted and not moved since
+    bool pending_compact = false;   // escaped particles (cell -1) not yet erased (wall boxes)
+    double e_right[3] = {0, 0, 0}, b_right[3] = {0, 0, 0};   // open boundary fields (wall boxes)
     float* fields32 = nullptr;      // FP32 copies of E^n, B^n (6N) for the FP32 deposit
     // updateDensityParameters grids: per species conc, energy, velocity (5N), charge density (N)
     double* dens = nullptr;
@@ -185,11 +188,22 @@ pic_status sort_species(pic_ctx* ctx, Species& sp) {
     CK(cudaMemcpyAsync(ctx->cursor, ctx->counts, sizeof(int) * (size_t)ctx->nkeys, cudaMemcpyDeviceToDevice, s));
     launch_scatter_atomic(s, ctx->key, n, ctx->cursor, ctx->tmp);
     launch_segsort(s, sp.off, ctx->nkeys, ctx->tmp, sp.perm, ctx->long_count, ctx->long_list);
-    PK<T>::gather_payload(s, sp.perm, n, view<T>(sp), view_alt<T>(sp));
+    long long kept = n;
+    if (ctx->g.wall) {
+        // particles that escaped (cell -1) have no key: the keyed ones, in
+        // key order, are the species from now on (eraseEscapedPaticles,
+        // mover.cpp:167-192)
+        int total = 0;
+        CK(cudaMemcpyAsync(&total, sp.off + ctx->nkeys, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        kept = total;
+    }
+    PK<T>::gather_payload(s, sp.perm, kept, view<T>(sp), view_alt<T>(sp));
     CKL(ctx, "sort");
     std::swap(sp.cell, sp.cell2);
     std::swap(sp.id, sp.id2);
     for (int q = 0; q < 6; ++q) std::swap(sp.a[q], sp.b[q]);
+    sp.n = kept;
     sp.sorted = true;
     return PIC_OK;
 }
@@ -200,7 +214,15 @@ pic_status sort_all(pic_ctx* ctx) {
         if (st != PIC_OK) return st;
     }
     ctx->fresh_sort = true;
+    ctx->pending_compact = false;
     return PIC_OK;
+}
+
+// Erases the particles that left a wall box since the last sort, before any
+// call that reads the particle arrays.
+pic_status settle(pic_ctx* ctx) {
+    if (!ctx->pending_compact) return PIC_OK;
+    return sort_all(ctx);
 }
 
 bool all_sorted(const pic_ctx* ctx) {
@@ -358,8 +380,10 @@ pic_status implicit_moments(pic_ctx* ctx) {
             PK<T>::implicit_deposit(s, g, view<T>(sp), sp.q, sp.m, sp.w, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu,
                                     ctx->rho, ctx->Pi, compat, ctx->ga);
     }
+    if (g.wall) launch_wall_moments(s, g, ctx->Jh, ctx->mu, ctx->rho, ctx->Pi, compat ? 0 : 1);
     if (compat) {
-        for (int ax = 0; ax < 3; ++ax) launch_pi_fold_reference(s, ctx->Pi, ctx->ga, ax);
+        // one rank next to a wall folds nothing along x (momentum_exchange.cpp:1643-1670)
+        for (int ax = g.wall ? 1 : 0; ax < 3; ++ax) launch_pi_fold_reference(s, ctx->Pi, ctx->ga, ax);
         launch_jg_build(s, g, ctx->ga, ctx->Jh, ctx->Pi, ctx->Jg, ctx->nex, ctx->ney, ctx->nez);
         launch_rho_ext_reference(s, g, ctx->Jg, ctx->nex, ctx->ney, ctx->nez, ctx->rho, ctx->rho_ext, ctx->ex, ctx->ey,
                                  ctx->ez);
@@ -367,11 +391,13 @@ pic_status implicit_moments(pic_ctx* ctx) {
     } else {
         launch_j_minus_divpi(s, g, ctx->Pi, ctx->Jh, ctx->Jg);
         CK(cudaMemcpyAsync(ctx->Jh, ctx->Jg, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+        if (g.wall) launch_wall_zero_j(s, g, ctx->Jh);
         launch_rho_ext_periodic(s, g, ctx->Jh, ctx->rho, ctx->rho_ext, ctx->ex, ctx->ey, ctx->ez);
         pic_status st = smooth_moments(ctx);
         if (st != PIC_OK) return st;
     }
     launch_maxwell_rhs(s, g, ctx->Ei, ctx->Bi, ctx->Jh, ctx->rho_ext, ctx->ex, ctx->ey, ctx->rhs);
+    if (g.wall) launch_wall_rhs(s, g, ctx->rho_ext, ctx->ex, ctx->ey, ctx->e_right, ctx->rhs);
     CKL(ctx, "implicit moments");
     ctx->moments_ready = true;
     ctx->mu_valid = true;
@@ -451,6 +477,13 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     // the reference smooths J-hat and rho-hat including its own ghost values,
     // which only the periodic pressure placement represents as periodic images
     if (c.smoothing_count > 0 && c.solver == PIC_SOLVER_IMPLICIT && c.pressure_compat) return PIC_ERR_ARG;
+    // conductor wall / open boundary along x: implicit runs of 3-D boxes, no
+    // smoothing (the reference's own 2-D boundary rows are all fake,
+    // fields.cpp:528-530)
+    if (c.boundary_x != PIC_BOUNDARY_PERIODIC &&
+        (c.boundary_x != PIC_BOUNDARY_WALL_OPEN || c.solver != PIC_SOLVER_IMPLICIT || c.smoothing_count > 0 ||
+         c.nx < 4 || c.ny < 2 || c.nz < 2))
+        return PIC_ERR_ARG;
     long long N = (long long)c.nx * c.ny * c.nz;
     if (N >= (1LL << 31)) return PIC_ERR_ARG;
     int tile[3];
@@ -478,6 +511,8 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     g.y3 = c.ny > 1; g.z3 = c.nz > 1;
     g.divx = FastDiv((unsigned)c.nx);
     g.divy = FastDiv((unsigned)c.ny);
+    g.wall = c.boundary_x == PIC_BOUNDARY_WALL_OPEN ? 1 : 0;
+    for (int a = 0; a < 3; ++a) { ctx->e_right[a] = c.e_right[a]; ctx->b_right[a] = c.b_right[a]; }
     ctx->preal = c.particle_real;
     ctx->rsz = ctx->preal ? sizeof(double) : sizeof(float);
     TileGeom& t = ctx->tg;
@@ -610,20 +645,23 @@ pic_status pic_add_species(pic_ctx* ctx, double q, double m, double w, long capa
     return sync(ctx, "add species");
 }
 
-pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, const double* ox, const double* oy,
-                                const double* oz, const double* px, const double* py, const double* pz,
-                                const int* ids) {
-    if (!ctx) return PIC_ERR_ARG;
-    if (pic_status st = check_species(ctx, sid)) return st;
+namespace {
+
+// Host particles into slots [at, at + n) of a species (upload: at = 0, the
+// species then holds n; append: at = its count), validated on the device.
+pic_status put_particles(pic_ctx* ctx, int sid, long long at, long n, const int* cell, const double* ox,
+                         const double* oy, const double* oz, const double* px, const double* py, const double* pz,
+                         const int* ids) {
     Species& sp = ctx->sp[sid];
-    if (n < 0 || n > sp.cap) return fail(ctx, PIC_ERR_NOMEM, "particle count exceeds species capacity");
+    if (n < 0 || at + n > sp.cap) return fail(ctx, PIC_ERR_NOMEM, "particle count exceeds species capacity");
     if (n > 0 && (!cell || !ox || !oy || !oz || !px || !py || !pz)) return fail(ctx, PIC_ERR_ARG, "null array");
+    const long long n0 = sp.n;
     cudaStream_t s = ctx->s;
-    CK(cudaMemcpyAsync(sp.cell, cell, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sp.cell + at, cell, sizeof(int) * n, cudaMemcpyHostToDevice, s));
     if (ids) {
-        CK(cudaMemcpyAsync(sp.id, ids, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(sp.id + at, ids, sizeof(int) * n, cudaMemcpyHostToDevice, s));
     } else {
-        PK<float>::iota(s, sp.id, n);
+        PK<float>::iota(s, sp.id + at, n, at == 0 ? 0 : sp.next_id);
     }
     const double* src[6] = {ox, oy, oz, px, py, pz};
     const long long chunk = std::min<long long>(kStageChunk, ctx->stage_len);
@@ -632,34 +670,58 @@ pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, 
     CK(cudaMemsetAsync(ctx->flag, 0, sizeof(int), s));
     for (int q = 0; q < 6; ++q) {
         if (ctx->preal) {
-            CK(cudaMemcpyAsync(sp.a[q], src[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync((double*)sp.a[q] + at, src[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
             continue;
         }
         if (device_addressable(src[q])) {
-            PK<float>::to_real_checked(s, src[q], sp.a[q], n, q < 3 ? 0 : 1, ctx->flag);
+            PK<float>::to_real_checked(s, src[q], (float*)sp.a[q] + at, n, q < 3 ? 0 : 1, ctx->flag);
             continue;
         }
         for (long long b = 0; b < n; b += chunk) {
             long long len = std::min<long long>(chunk, n - b);
             CK(cudaMemcpyAsync(ctx->stage, src[q] + b, sizeof(double) * len, cudaMemcpyHostToDevice, s));
-            PK<float>::to_real_checked(s, ctx->stage, (float*)sp.a[q] + b, len, q < 3 ? 0 : 1, ctx->flag);
+            PK<float>::to_real_checked(s, ctx->stage, (float*)sp.a[q] + at + b, len, q < 3 ? 0 : 1, ctx->flag);
         }
     }
-    sp.n = n;
-    if (ctx->preal) PK<double>::validate(s, ctx->g, view<double>(sp), ctx->flag);
-    else PK<float>::validate(s, ctx->g, view<float>(sp), ctx->flag);
+    // validate the new slots only
+    Species part = sp;
+    for (int q = 0; q < 6; ++q) part.a[q] = (char*)sp.a[q] + ctx->rsz * at;
+    part.cell = sp.cell + at;
+    part.n = n;
+    if (ctx->preal) PK<double>::validate(s, ctx->g, view<double>(part), ctx->flag);
+    else PK<float>::validate(s, ctx->g, view<float>(part), ctx->flag);
     int bad = 0;
     CK(cudaMemcpyAsync(&bad, ctx->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (bad) {
-        sp.n = 0;
+        sp.n = at == 0 ? 0 : n0;
         if (bad & 4) return fail(ctx, PIC_ERR_NUMERIC, "non-finite particle momentum");
         return fail(ctx, PIC_ERR_ARG, (bad & 1) ? "cell index out of range" : "offset outside [0,1)");
     }
-    sp.n = n;
+    sp.n = at + n;
+    sp.next_id = at == 0 ? n : sp.next_id + n;
     sp.sorted = false;
     ctx->moments_ready = false;
-    return sync(ctx, "upload particles");
+    return sync(ctx, "put particles");
+}
+
+}  // namespace
+
+pic_status pic_upload_particles(pic_ctx* ctx, int sid, long n, const int* cell, const double* ox, const double* oy,
+                                const double* oz, const double* px, const double* py, const double* pz,
+                                const int* ids) {
+    if (!ctx) return PIC_ERR_ARG;
+    if (pic_status st = check_species(ctx, sid)) return st;
+    return put_particles(ctx, sid, 0, n, cell, ox, oy, oz, px, py, pz, ids);
+}
+
+pic_status pic_append_particles(pic_ctx* ctx, int sid, long n, const int* cell, const double* ox, const double* oy,
+                                const double* oz, const double* px, const double* py, const double* pz,
+                                const int* ids) {
+    if (!ctx) return PIC_ERR_ARG;
+    if (pic_status st = check_species(ctx, sid)) return st;
+    if (pic_status st = settle(ctx)) return st;
+    return put_particles(ctx, sid, ctx->sp[sid].n, n, cell, ox, oy, oz, px, py, pz, ids);
 }
 
 pic_status pic_fill_species(pic_ctx* ctx, int sid, int ppc, unsigned long long seed, double theta, double drift_gamma,
@@ -668,7 +730,9 @@ pic_status pic_fill_species(pic_ctx* ctx, int sid, int ppc, unsigned long long s
     if (pic_status st = check_species(ctx, sid)) return st;
     Species& sp = ctx->sp[sid];
     if (ppc < 0 || !(theta >= 0) || !(drift_gamma >= 1.0)) return fail(ctx, PIC_ERR_ARG, "bad fill parameters");
-    const long long n = (long long)ppc * ctx->g.N;
+    // a wall box leaves its two ghost columns empty
+    const int rowx = ctx->g.wall ? ctx->g.nx - 2 : ctx->g.nx;
+    const long long n = (long long)ppc * (ctx->g.N / ctx->g.nx) * rowx;
     if (n > sp.cap) return fail(ctx, PIC_ERR_NOMEM, "particle count exceeds species capacity");
     const int ntab = 4096;
     std::vector<double> us, cdf;
@@ -682,10 +746,11 @@ pic_status pic_fill_species(pic_ctx* ctx, int sid, int ppc, unsigned long long s
     sp.n = n;
     const unsigned long long sseed = seed * 0x100000001B3ull + (unsigned long long)sid * 0x9E3779B97F4A7C15ull;
     if (ctx->preal) launch_fill<double>(ctx->s, view<double>(sp), ppc, sseed, du, dc, theta > 0 ? ntab : 0, sp.m,
-                                        drift_gamma, alternate_drift);
+                                        drift_gamma, alternate_drift, rowx, ctx->g.nx);
     else launch_fill<float>(ctx->s, view<float>(sp), ppc, sseed, du, dc, theta > 0 ? ntab : 0, sp.m, drift_gamma,
-                            alternate_drift);
+                            alternate_drift, rowx, ctx->g.nx);
     CKL(ctx, "fill species");
+    sp.next_id = n;
     sp.sorted = false;
     ctx->moments_ready = false;
     return sync(ctx, "fill species");
@@ -695,6 +760,7 @@ pic_status pic_download_particles(pic_ctx* ctx, int sid, long* n_out, int* cell,
                                   double* px, double* py, double* pz, int* ids) {
     if (!ctx) return PIC_ERR_ARG;
     if (pic_status st = check_species(ctx, sid)) return st;
+    if (pic_status st0 = settle(ctx)) return st0;
     Species& sp = ctx->sp[sid];
     const long long n = sp.n;
     if (n_out) *n_out = (long)n;
@@ -798,6 +864,7 @@ pic_status pic_move_particles(pic_ctx* ctx) {
     if (!ctx->efield_ready) return fail(ctx, PIC_ERR_STATE, "evaluate the electric field first");
     pic_status st = ctx->preal ? implicit_move<double>(ctx) : implicit_move<float>(ctx);
     if (st != PIC_OK) return st;
+    if (ctx->g.wall) ctx->pending_compact = true;   // escaped particles are erased by the next sort
     return sync(ctx, "move particles");
 }
 
@@ -834,7 +901,8 @@ pic_status pic_buneman_step(pic_ctx* ctx, int nsteps) {
 pic_status pic_update_electromagnetic_parameters(pic_ctx* ctx) {
     if (!ctx) return PIC_ERR_ARG;
     if (is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not an implicit run");
-    if (ctx->cfg.sort_every > 0 && (!all_sorted(ctx) || ctx->step % ctx->cfg.sort_every == 0)) {
+    if (ctx->pending_compact ||
+        (ctx->cfg.sort_every > 0 && (!all_sorted(ctx) || ctx->step % ctx->cfg.sort_every == 0))) {
         pic_status st = sort_all(ctx);
         if (st != PIC_OK) return st;
     }
@@ -878,6 +946,7 @@ pic_status pic_evaluate_magnetic_field(pic_ctx* ctx) {
     {
         Phase ph(ctx, PIC_PHASE_FIELDS, 1);
         launch_field_update(ctx->s, ctx->g, ctx->Et, ctx->Ei, ctx->Bi, ctx->En, ctx->Bn, 0, 1);
+        if (ctx->g.wall) launch_wall_b(ctx->s, ctx->g, ctx->Bn, ctx->b_right);
     }
     return sync(ctx, "evaluate magnetic field");
 }
@@ -938,6 +1007,7 @@ pic_status pic_maxwell_apply(pic_ctx* ctx, const double* mu, const double* x, do
 pic_status pic_maxwell_apply_transpose(pic_ctx* ctx, const double* mu, const double* y, double* out) {
     if (!ctx || !mu || !y || !out) return PIC_ERR_ARG;
     if (is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not an implicit run");
+    if (ctx->g.wall) return fail(ctx, PIC_ERR_STATE, "the transpose covers periodic boxes only");
     const long long N = ctx->g.N;
     cudaStream_t s = ctx->s;
     CK(cudaMemcpyAsync(ctx->mu, mu, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, s));
@@ -987,6 +1057,7 @@ pic_status pic_download_permutation(pic_ctx* ctx, int sid, long* n, int* perm) {
 
 pic_status pic_energy(pic_ctx* ctx, double out[6]) {
     if (!ctx || !out) return PIC_ERR_ARG;
+    if (pic_status st0 = settle(ctx)) return st0;
     cudaStream_t s = ctx->s;
     const long long L = 3 * ctx->g.N;
     const double vol = ctx->g.dx * ctx->g.dy * ctx->g.dz;
@@ -1075,6 +1146,7 @@ struct FileCloser {
 
 pic_status pic_save_checkpoint(pic_ctx* ctx, const char* path) {
     if (!ctx || !path) return PIC_ERR_ARG;
+    if (pic_status st0 = settle(ctx)) return st0;
     FILE* f = fopen(path, "wb");
     if (!f) return fail(ctx, PIC_ERR_ARG, std::string("cannot open ") + path);
     FileCloser fc{f};
@@ -1186,6 +1258,7 @@ pic_status pic_load_checkpoint(pic_ctx* ctx, const char* path) {
 // ---------------------------------------------------------------- density diagnostics
 pic_status pic_update_density_parameters(pic_ctx* ctx) {
     if (!ctx) return PIC_ERR_ARG;
+    if (pic_status st0 = settle(ctx)) return st0;
     const long long N = ctx->g.N;
     const int ns = (int)ctx->sp.size();
     cudaStream_t s = ctx->s;
@@ -1263,6 +1336,7 @@ pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info
     pic_status st = net_of(ctx, true);
     if (st != PIC_OK) return st;
     if (!ctx->mu_valid) return fail(ctx, PIC_ERR_STATE, "no operator: update the electromagnetic parameters first");
+    if (ctx->g.wall) return fail(ctx, PIC_ERR_STATE, "train on a periodic box (the network is convolutional)");
     st = ctx->net->train(ctx->s, ctx->g, ctx->mu, *opts, info, ctx->partials, &ctx->err);
     if (st != PIC_OK) return st;
     return sync(ctx, "nn train");

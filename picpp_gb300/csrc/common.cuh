@@ -29,6 +29,7 @@ struct GridP {
     double theta, eta, cfix;
     int y3, z3;           // ny > 1, nz > 1
     FastDiv divx, divy;   // by nx, by ny
+    int wall;             // 1: conductor wall at x = 0, open boundary at x = (nx - 2) dx (wall.cuh)
 };
 
 __device__ __forceinline__ int fast_div(int n, const FastDiv& f) {

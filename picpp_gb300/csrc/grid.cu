@@ -4,6 +4,7 @@
 #include "kernels.hpp"
 #include "krylov.cuh"
 #include "sort.cuh"
+#include "wall.cuh"
 #include <algorithm>
 
 namespace pic {
@@ -82,6 +83,25 @@ void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, cons
                           double* y, double* wmu) {
     k_mu_times<<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
     k_maxwell_stencil<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
+    if (g.wall) k_wall_rows<<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
+}
+
+void launch_wall_moments(cudaStream_t s, const GridP& g, double* J, double* mu, double* rho, double* Pi,
+                         int pi_mirror) {
+    k_wall_moments<<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, J, mu, rho, Pi, pi_mirror);
+}
+
+void launch_wall_zero_j(cudaStream_t s, const GridP& g, double* J) {
+    k_wall_zero_j<<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, J);
+}
+
+void launch_wall_rhs(cudaStream_t s, const GridP& g, const double* rho_ext, int ex, int ey, const double er[3],
+                     double* rhs) {
+    k_wall_rhs<<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, rho_ext, ex, ey, er[0], er[1], er[2], rhs);
+}
+
+void launch_wall_b(cudaStream_t s, const GridP& g, double* B, const double br[3]) {
+    k_wall_b<<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, B, br[0], br[1], br[2]);
 }
 
 void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* y,

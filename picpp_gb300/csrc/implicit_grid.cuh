@@ -100,6 +100,8 @@ __global__ void k_jg_build(GridP g, GhostAxes ga, const double* __restrict__ J, 
             div_pi(g, i, j, k, PT, out);
         }
         for (int d = 0; d < 3; ++d) Jg[d * JN + t] = J[d * g.N + src] - out[d] * g.eta * g.dt;
+        if (g.wall && i <= ga.gx)   // the wall node and the ghosts left of it (momentum_collecting.cpp:638-646)
+            for (int d = 0; d < 3; ++d) Jg[d * JN + t] = 0.0;
     }
 }
 

@@ -3,6 +3,7 @@
 #pragma once
 #include "common.cuh"
 #include "types.cuh"
+#include "wall_particles.cuh"
 
 namespace pic {
 
@@ -190,7 +191,10 @@ __global__ void __launch_bounds__(128) k_implicit_deposit(GridP g, PartView<T> p
                     atomicAdd(&rho[id], qw * corr);
                     long long pid;
                     if (compat) {
-                        int rx = g.nx > 1 ? xl + a + ga.gx : 0;
+                        // a wall box mirrors the ghost cell left of the wall
+                        // onto the first cell (momentum_collecting.cpp:560-568)
+                        const int ux = xl + a;
+                        int rx = g.nx > 1 ? ((g.wall && ux < 0) ? -ux - 1 : ux) + ga.gx : 0;
                         int ry = g.ny > 1 ? bb : 0;
                         int rz = g.nz > 1 ? c : 0;
                         pid = ((long long)rz * ga.cey + ry) * ga.cex + rx;
@@ -235,8 +239,10 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
     const T id[3] = {T(1.0 / g.dx), T(1.0 / g.dy), T(1.0 / g.dz)};
     const int nn[3] = {g.nx, g.ny, g.nz};
     const T dxT = T(g.dx);
+    const T redt = T((1.0 - g.eta) * g.dt);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n;
          n += (long long)gridDim.x * blockDim.x) {
+        if (p.cell[n] < 0) continue;   // escaped, erased by the next sort
         int ci[3];
         decode(g, p.cell[n], ci[0], ci[1], ci[2]);
         T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
@@ -258,6 +264,13 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
         T mv[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
+        if (g.wall && wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
+            wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+            p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+            p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+            p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+            continue;
+        }
         T vh[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -270,6 +283,7 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
         T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
         T prevDisp[3];
         int it = 0;
+        bool reflected = false;
         while (picard_continue<T>(err, momNorm, cerr, dxN, it)) {
             ++it;
             T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
@@ -282,6 +296,11 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
             for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
 #pragma unroll
             for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
+            if (g.wall && wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
+                wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                reflected = true;
+                break;
+            }
             int tc[3];
             T tu[3];
 #pragma unroll
@@ -300,9 +319,19 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
                             (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
                             (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
         }
-        p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+        if (!reflected) {
+            if (g.wall) {
+                const int o = wall_final_x<T>(g, ci[0], u0[0], (mv[0] * dt) * id[0]);
+                if (o == 2) { p.cell[n] = -1; continue; }   // escaped through the open boundary
+                if (o == 1) pnew[0] = -pnew[0];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+                for (int d = 1; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+            } else {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+            }
+        }
+        p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
         p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
         p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
     }

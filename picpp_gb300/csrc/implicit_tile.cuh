@@ -600,6 +600,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
     const T id[3] = {T(1.0 / g.dx), T(1.0 / g.dy), T(1.0 / g.dz)};
     const int nn[3] = {g.nx, g.ny, g.nz};
     const T dxT = T(g.dx);
+    const T redt = T((1.0 - g.eta) * g.dt);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
         const int x0 = ti * t.tx, y0 = tj * t.ty, z0 = tk * t.tz;
@@ -698,6 +699,13 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T mv[3];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
+                if (g.wall && wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
+                    wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                    p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+                    p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+                    p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+                    continue;
+                }
                 T vh[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
@@ -710,6 +718,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
                 T prevDisp[3];
                 int it = 0;
+                bool reflected = false;
                 while (picard_continue<T>(err, momNorm, cerr, dxN, it)) {
                     ++it;
                     const T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
@@ -722,6 +731,11 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
 #pragma unroll
                     for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
+                    if (g.wall && wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
+                        wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                        reflected = true;
+                        break;
+                    }
                     int tc[3];
                     T tu[3];
 #pragma unroll
@@ -743,9 +757,19 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                                     (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
                                     (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
                 }
-                p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+                if (!reflected) {
+                    if (g.wall) {
+                        const int o = wall_final_x<T>(g, ci[0], u0[0], (mv[0] * dt) * id[0]);
+                        if (o == 2) { p.cell[n] = -1; continue; }   // escaped through the open boundary
+                        if (o == 1) pnew[0] = -pnew[0];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+                        for (int d = 1; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+                    } else {
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+                    }
+                }
+                p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
                 p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
                 p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
             }

@@ -69,14 +69,14 @@ struct PK {
     static void to_real_checked(cudaStream_t s, const double* src, void* dst, long long n, int mode, int* flag);
     static void from_real(cudaStream_t s, const void* src, double* dst, long long n);
     static void validate(cudaStream_t s, const GridP& g, PartView<T> p, int* flag);
-    static void iota(cudaStream_t s, int* a, long long n);
+    static void iota(cudaStream_t s, int* a, long long n, long long start = 0);
 };
 
 // init.cu
 std::vector<double> juttner_table(double theta, int n, std::vector<double>& us);
 template <typename T>
 void launch_fill(cudaStream_t s, PartView<T> p, long long ppc, unsigned long long seed, const double* u, const double* c,
-                 int ntab, double mass, double drift_gamma, int alternate);
+                 int ntab, double mass, double drift_gamma, int alternate, int rowx, int nx);
 
 // grid.cu
 void launch_keys_hist(cudaStream_t s, const GridP& g, const TileGeom& t, const int* cell, long long n, int* key,
@@ -100,6 +100,13 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
 // y = A(mu) x; wmu: scratch of 3N doubles (mu x)
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
                           double* y, double* wmu);
+// conductor wall at x = 0 / open boundary at x = (nx - 2) dx (wall.cuh)
+void launch_wall_moments(cudaStream_t s, const GridP& g, double* J, double* mu, double* rho, double* Pi,
+                         int pi_mirror);
+void launch_wall_zero_j(cudaStream_t s, const GridP& g, double* J);
+void launch_wall_rhs(cudaStream_t s, const GridP& g, const double* rho_ext, int ex, int ey, const double er[3],
+                     double* rhs);
+void launch_wall_b(cudaStream_t s, const GridP& g, double* B, const double br[3]);
 void launch_maxwell_apply_t(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* y,
                             double* out);
 void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,

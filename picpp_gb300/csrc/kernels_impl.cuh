@@ -120,6 +120,7 @@ __global__ void k_validate(GridP g, PartView<T> p, int* __restrict__ flag) {
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n; n += (long long)gridDim.x * blockDim.x) {
         int c = p.cell[n];
         if (c < 0 || c >= g.N) bad |= 1;
+        else if (g.wall && c % g.nx >= g.nx - 2) bad |= 1;   // wall box: the two ghost columns hold no particles
         T o[3] = {p.ox[n], p.oy[n], p.oz[n]};
         for (int a = 0; a < 3; ++a)
             if (!(o[a] >= T(0) && o[a] < T(1))) bad |= 2;
@@ -131,9 +132,9 @@ __global__ void k_validate(GridP g, PartView<T> p, int* __restrict__ flag) {
 }
 
 template <typename T>
-__global__ void k_iota(int* __restrict__ a, long long n) {
+__global__ void k_iota(int* __restrict__ a, long long n, long long start) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        a[i] = (int)i;
+        a[i] = (int)(start + i);
 }
 
 template <typename T>
@@ -143,9 +144,9 @@ void PK<T>::validate(cudaStream_t s, const GridP& g, PartView<T> p, int* flag) {
 }
 
 template <typename T>
-void PK<T>::iota(cudaStream_t s, int* a, long long n) {
+void PK<T>::iota(cudaStream_t s, int* a, long long n, long long start) {
     if (n == 0) return;
-    k_iota<T><<<grid_for(n, 256, 16), 256, 0, s>>>(a, n);
+    k_iota<T><<<grid_for(n, 256, 16), 256, 0, s>>>(a, n, start);
 }
 
 template <typename T>

@@ -106,7 +106,8 @@ pic_status gmres_reference(SolveCtx& c, const OpCoef& oc, const double* rhs, dou
     launch_dot(c.s, Vp(0), Vp(0), L, k.part, P, k.scal, 1);
     const double normR = read1(c, k.scal, &st);
     if (st != PIC_OK) return st;
-    const long long dim = L;
+    // matrixDimension of the reference: 3 x its cells (the physical ones of a wall box)
+    const long long dim = g.wall ? 3LL * (g.nx - 2) * g.ny * g.nz : L;
     double tolRel = o.tol / (double)dim;
     if (tolRel < 1e-15) tolRel = 1e-15;
     const int cap = maxIter + 2;

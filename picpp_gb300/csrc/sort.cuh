@@ -37,7 +37,8 @@ __global__ void k_keys_hist(GridP g, TileGeom t, const int* __restrict__ cell, l
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
         const long long a = base + lane;
-        const int kk = a < n ? sort_key(g, t, cell[a]) : -1;
+        const int ca = a < n ? cell[a] : -1;   // escaped particles (cell -1) get no key and drop out
+        const int kk = ca >= 0 ? sort_key(g, t, ca) : -1;
         if (a < n) key[a] = kk;
         const unsigned m = __match_any_sync(0xffffffffu, kk);
         if (kk >= 0 && lane == __ffs(m) - 1) atomicAdd(&counts[kk], __popc(m));

@@ -179,40 +179,34 @@ class FlowState(State):
     ppc: tuple = ()
 
 
-def shock_plasma(nx, ny, nz, dx=0.5, dt=0.4, ppc=(32, 32, 8), flow_gamma=1.5, theta_e=1e-3, sigma=0.04,
-                 angle_deg=60.0, mass_ratio=64.0, he_mass=256.0, he_fraction=0.1, theta=0.5, seed=5) -> FlowState:
-    """The reflecting-wall shock setup: a plasma of electrons, protons
-    (mass_ratio) and fully ionised helium (charge 2, mass he_mass, number
-    density he_fraction of the protons'), charge neutral, flowing towards
-    -x with Lorentz factor flow_gamma into a conductor wall at x = 0; every
-    species at the electron temperature (theta_e m_e / m_s); B0 at angle_deg
-    to x in the x-y plane with sigma = B0^2 / (4 pi flow_gamma sum_s n_s m_s);
+def shock_parameters(dx=0.5, ppc=(32, 32, 8), flow_gamma=1.5, theta_e=1e-3, sigma=0.04, angle_deg=60.0,
+                     mass_ratio=64.0, he_mass=256.0, he_fraction=0.1):
+    """Species and fields of the reflecting-wall shock setup: a plasma of
+    electrons, protons (mass_ratio) and fully ionised helium (charge 2, mass
+    he_mass, number density he_fraction of the protons'), charge neutral,
+    flowing towards -x with Lorentz factor flow_gamma; every species at the
+    electron temperature (theta = theta_e m_e / m_s); B0 at angle_deg to x
+    in the x-y plane with sigma = B0^2 / (4 pi flow_gamma sum_s n_s m_s);
     E0 = -V0 x B0 (initializeFluxFromRight, PIC++/initialization.cpp:
-    5201-5207), Ey = Ez = 0 on the wall node.  Particles fill the nx - 2
-    physical cells; electron density 1 / (4 pi) (omega_pe = 1)."""
-    box = Box(nx, ny, nz, dx, dx, dx, dt, theta=theta)
-    rng = np.random.default_rng(seed)
+    5201-5207).  Electron density 1 / (4 pi) (omega_pe = 1).  Returns
+    (species [(q, m, density, ppc, theta)], E0, B0, v0)."""
     n_e = 1.0 / FOUR_PI
     n_p = n_e / (1.0 + 2.0 * he_fraction)
     n_he = he_fraction * n_p
-    specs = ((-1.0, 1.0, n_e, ppc[0]), (1.0, mass_ratio, n_p, ppc[1]), (2.0, he_mass, n_he, ppc[2]))
+    specs = [(-1.0, 1.0, n_e, ppc[0], theta_e), (1.0, mass_ratio, n_p, ppc[1], theta_e / mass_ratio),
+             (2.0, he_mass, n_he, ppc[2], theta_e / he_mass)]
     v0 = math.sqrt(1.0 - 1.0 / (flow_gamma * flow_gamma))
-    phys = Box(nx - 2, ny, nz, dx, dx, dx, dt, theta=theta)
-    species, temps = [], []
-    for q, m, n, c in specs:
-        th = theta_e / m
-        sp = uniform_species(rng, phys, c, q, m, density_weight(box, n, c), th, flow_gamma, -1.0)
-        i = sp["cell"] % phys.nx
-        rest = sp["cell"] // phys.nx
-        sp["cell"] = (rest * nx + i).astype(np.int32)   # physical cells in the storage layout
-        species.append(sp)
-        temps.append(th)
-    rho_m = sum(n * m for _, m, n, _ in specs)
+    rho_m = sum(n * m for _, m, n, _, _ in specs)
     b0 = math.sqrt(sigma * FOUR_PI * flow_gamma * rho_m)
     a = math.radians(angle_deg)
     B0 = np.array([b0 * math.cos(a), b0 * math.sin(a), 0.0])
-    V0 = np.array([-v0, 0.0, 0.0])
-    E0 = -np.cross(V0, B0)
+    E0 = -np.cross(np.array([-v0, 0.0, 0.0]), B0)
+    return specs, E0, B0, v0
+
+
+def wall_fields(nx, ny, nz, E0, B0):
+    """Initial fields of a wall box: E0 and B0 everywhere, Ey = Ez = 0 on
+    the wall node (initializeFluxFromRight)."""
     E = np.zeros((3, nz, ny, nx))
     B = np.zeros((3, nz, ny, nx))
     for d in range(3):
@@ -220,7 +214,70 @@ def shock_plasma(nx, ny, nz, dx=0.5, dt=0.4, ppc=(32, 32, 8), flow_gamma=1.5, th
         B[d] = B0[d]
     E[1, :, :, 0] = 0.0
     E[2, :, :, 0] = 0.0
+    return E, B
+
+
+def shock_plasma(nx, ny, nz, dx=0.5, dt=0.4, ppc=(32, 32, 8), flow_gamma=1.5, theta_e=1e-3, sigma=0.04,
+                 angle_deg=60.0, mass_ratio=64.0, he_mass=256.0, he_fraction=0.1, theta=0.5, seed=5) -> FlowState:
+    """The reflecting-wall shock setup (shock_parameters) on a wall box of
+    nx x ny x nz storage cells: the flow fills the nx - 2 physical cells of
+    every x row."""
+    box = Box(nx, ny, nz, dx, dx, dx, dt, theta=theta)
+    rng = np.random.default_rng(seed)
+    specs, E0, B0, v0 = shock_parameters(dx, ppc, flow_gamma, theta_e, sigma, angle_deg, mass_ratio, he_mass,
+                                         he_fraction)
+    phys = Box(nx - 2, ny, nz, dx, dx, dx, dt, theta=theta)
+    species, temps = [], []
+    for q, m, n, c, th in specs:
+        sp = uniform_species(rng, phys, c, q, m, density_weight(box, n, c), th, flow_gamma, -1.0)
+        i = sp["cell"] % phys.nx
+        rest = sp["cell"] // phys.nx
+        sp["cell"] = (rest * nx + i).astype(np.int32)   # physical cells in the storage layout
+        species.append(sp)
+        temps.append(th)
+    E, B = wall_fields(nx, ny, nz, E0, B0)
     return FlowState(box, species, E, B, tuple(E0), tuple(B0), flow_gamma, tuple(temps), tuple(ppc))
+
+
+class Injector:
+    """The open boundary's particle source with the bookkeeping of
+    Simulation::simulate and injectNewParticles (PIC++/simulation.cpp:126,
+    281-285; PIC++/mover.cpp:910-1000): per species an injection length
+    that grows by |V0| dt every step; while ppc * length >= dx it shrinks by
+    dx / ppc and one particle enters every (y, z) cell column at
+    x = (nx - 2) dx - length.  Offsets along y and z are uniform per
+    particle (the reference draws one pair per call) and momenta are the
+    species' drifting Maxwell-Juttner law."""
+
+    def __init__(self, box: Box, species, flow_gamma: float, seed: int = 0):
+        self.box = box
+        self.species = species          # [(q, m, density, ppc, theta)]
+        self.gamma = flow_gamma
+        self.v0 = math.sqrt(1.0 - 1.0 / (flow_gamma * flow_gamma))
+        self.length = [box.dx / c - 1e-4 * box.dx for _, _, _, c, _ in species]
+        self.rng = np.random.default_rng(seed)
+
+    def step(self):
+        """The particles of one step, one dict per species (cell, ox, oy, oz,
+        px, py, pz)."""
+        b = self.box
+        cols = b.ny * b.nz
+        out = []
+        for s, (q, m, n, ppc, th) in enumerate(self.species):
+            self.length[s] += abs(self.v0 * b.dt)
+            lengths = []
+            while self.length[s] * ppc >= b.dx:
+                self.length[s] -= b.dx / ppc
+                lengths.append(self.length[s])
+            k = len(lengths)
+            x = ((b.nx - 2) * b.dx - np.repeat(np.array(lengths, dtype=np.float64), cols)) / b.dx
+            ci = np.floor(x)
+            jk = np.tile(np.arange(cols), k)
+            cell = ((jk // b.ny) * b.ny + jk % b.ny) * b.nx + ci.astype(np.int64)
+            px, py, pz = sample_juttner(self.rng, k * cols, th, m, self.gamma, -1.0)
+            out.append(dict(cell=cell.astype(np.int32), ox=x - ci, oy=self.rng.random(k * cols),
+                            oz=self.rng.random(k * cols), px=px, py=py, pz=pz))
+        return out
 
 def positions(box: Box, sp: dict):
     """Physical positions in [0, L) from cell + offset (float64)."""

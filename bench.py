@@ -56,7 +56,8 @@ def _args():
     p.add_argument("--no-shock", action="store_true")
     p.add_argument("--only-shock", action="store_true", help="run and print only the reflecting-wall shock section")
     p.add_argument("--nn-steps", type=int, default=4000, help="training steps of the learned preconditioner")
-    p.add_argument("--nn-batch", type=int, default=4, help="random fields per training step (Adam, lr 1e-3)")
+    p.add_argument("--nn-batch", type=int, default=4, help="triples per training step (Adam, lr 1e-3)")
+    p.add_argument("--nn-triples", type=int, default=2000, help="recorded plain-solve triples to train on")
     p.add_argument("--no-implicit", action="store_true")
     p.add_argument("--only-implicit", action="store_true",
                    help="run and print only the implicit section (profiling the implicit step, solver and network)")
@@ -440,54 +441,88 @@ NET_LAYERS = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (
 
 
 def learned_solve(a, sim, box, w, opts):
-    """Trains the learned preconditioner on a 64x64x16 box of the same
-    plasma (the network is convolutional: its parameters carry over), then
-    solves the full box's next implicit system to an FP64 relative residual
-    of 1e-8 with plain GMRES(30) and with FGMRES(30) + the network."""
+    """The learned preconditioner's protocol: the first a.nn_triples
+    (right-hand side, mu, FP64 solution) triples that plain GMRES(30)
+    produces on runs of seeds 10-19 of the same plasma (a 64x64x16 box, 200
+    steps per run; the network is convolutional, its parameters carry over
+    to the full box), Adam at lr 1e-3, batch a.nn_batch, a.nn_steps steps on
+    the supervised and residual losses; then, on held-out seeds 20-24 of the
+    full box, the system of the step after the first is solved to an FP64
+    relative residual of 1e-8 with plain GMRES(30) and with FGMRES(30) + the
+    network: iterations and device time, mean and spread over the seeds."""
     import math
     import numpy as np
     import picpp_gb300 as P
     from picpp_gb300 import initstate as I
-    tb = I.Box(64, 64, 16, box.dx, box.dy, box.dz, box.dt, theta=box.theta)
     ppc = a.implicit_ppc
-    tsim = P.GpuSimulation(tb, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=1)
-    N = tb.ncells
-    tsim.add_species(-1.0, 1.0, w, N * ppc)
-    tsim.add_species(1.0, 25.0, w, N * ppc)
-    tsim.fill_species(0, ppc, 13, 0.01, 10.0, True)
-    tsim.fill_species(1, ppc, 14, 0.01 / 25.0, 10.0, True)
-    E = np.zeros((3, tb.nz, tb.ny, tb.nx))
-    B = np.zeros((3, tb.nz, tb.ny, tb.nx))
-    B[2] = math.sqrt(4 * math.pi * 0.01 * (1.0 / (4 * math.pi)) * 26.0 * 10.0)
-    tsim.upload_fields(E, B)
-    tsim.implicit_step(opts)
-    tsim.updateElectroMagneticParameters()
+    tb = I.Box(64, 64, 16, box.dx, box.dy, box.dz, box.dt, theta=box.theta)
+    tsim = _beams(tb, ppc, w, (20, 21))
+    tsim.nn_record(a.nn_triples)
+    runs = 0
+    for seed in range(10, 20):
+        if tsim.nn_record_count() >= a.nn_triples:
+            break
+        tsim.fill_species(0, ppc, 2 * seed, 0.01, 10.0, True)
+        tsim.fill_species(1, ppc, 2 * seed + 1, 0.01 / 25.0, 10.0, True)
+        E, B = I.zero_fields(tb)
+        B[2] = math.sqrt(4 * math.pi * 0.01 * (1.0 / (4 * math.pi)) * 26.0 * 10.0)
+        tsim.upload_fields(E, B)
+        runs += 1
+        for _ in range(200):
+            tsim.implicit_step(opts)
+            if tsim.nn_record_count() >= a.nn_triples:
+                break
+    triples = tsim.nn_record_count()
     tsim.nn_init(1)
-    tr = tsim.nn_train(steps=a.nn_steps, batch=a.nn_batch, lr=1e-3, seed=3, smooth_max=2)
+    tr = tsim.nn_train(steps=a.nn_steps, batch=a.nn_batch, lr=1e-3, seed=3, source=1, supervised_weight=0.5)
     params = tsim.nn_get_params()
     tsim.close()
     sim.nn_set_params(params)
-    sim.updateElectroMagneticParameters()
-    _, mu, _, rhs = sim.download_moments()
     plain_opts = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=600, tol=1e-8)
     learned_opts = P.solve_opts(P.FGMRES_LEARNED, restart=30, max_iter=600, tol=1e-8)
-    sim.maxwell_solve(mu, rhs, plain_opts)   # warm-up of both paths
-    sim.maxwell_solve(mu, rhs, learned_opts)
-    _, ip = sim.maxwell_solve(mu, rhs, plain_opts)
-    _, il = sim.maxwell_solve(mu, rhs, learned_opts)
+    rows = []
+    for seed in range(20, 25):
+        sim.fill_species(0, ppc, 2 * seed, 0.01, 10.0, True)
+        sim.fill_species(1, ppc, 2 * seed + 1, 0.01 / 25.0, 10.0, True)
+        E, B = I.zero_fields(box)
+        B[2] = math.sqrt(4 * math.pi * 0.01 * (1.0 / (4 * math.pi)) * 26.0 * 10.0)
+        sim.upload_fields(E, B)
+        sim.implicit_step(opts)
+        sim.updateElectroMagneticParameters()
+        _, mu, _, rhs = sim.download_moments()
+        if not rows:   # warm-up of both paths
+            sim.maxwell_solve(mu, rhs, plain_opts)
+            sim.maxwell_solve(mu, rhs, learned_opts)
+        _, ip = sim.maxwell_solve(mu, rhs, plain_opts)
+        _, il = sim.maxwell_solve(mu, rhs, learned_opts)
+        rows.append((seed, ip, il))
     n = box.ncells
     flop = sum(2 * 27 * ci * co * n / 8 ** lv for ci, co, lv in NET_LAYERS)
-    per_it = ip["seconds"] / max(ip["iterations"], 1)
-    apply_s = max(il["seconds"] - il["iterations"] * per_it, 0.0) / max(il["iterations"], 1)
-    return {"system": "next implicit step of the full box", "tol": 1e-8,
-            "plain": {k: ip[k] for k in ("iterations", "restarts", "rel_residual", "seconds")},
-            "learned": {k: il[k] for k in ("iterations", "restarts", "used_fallback", "rel_residual", "seconds")},
-            "speedup": ip["seconds"] / il["seconds"] if il["seconds"] > 0 else None,
-            "network": {"flop_per_apply": flop, "apply_ms_est": apply_s * 1e3,
-                        "tflops_est": flop / apply_s / 1e12 if apply_s > 0 else None,
-                        "train": {"box": [64, 64, 16], "steps": tr["steps"], "seconds": tr["seconds"],
-                                  "first_loss": tr["first_loss"], "last_loss": tr["last_loss"]}}}
 
+    def stats(vals):
+        return {"mean": statistics.fmean(vals), "min": min(vals), "max": max(vals),
+                "stdev": statistics.pstdev(vals)}
+
+    pit = [r[1]["iterations"] for r in rows]
+    lit = [r[2]["iterations"] for r in rows]
+    pms = [r[1]["seconds"] * 1e3 for r in rows]
+    lms = [r[2]["seconds"] * 1e3 for r in rows]
+    per_it = statistics.fmean(p / max(i, 1) for p, i in zip(pms, pit))
+    apply_ms = statistics.fmean(max(l - i * per_it, 0.0) / max(i, 1) for l, i in zip(lms, lit))
+    return {"system": "step 2 of held-out seeds 20-24 of the full box", "tol": 1e-8,
+            "plain": {"iterations": stats(pit), "ms": stats(pms)},
+            "learned": {"iterations": stats(lit), "ms": stats(lms),
+                        "fallbacks": sum(r[2]["used_fallback"] for r in rows)},
+            "speedup": statistics.fmean(pms) / statistics.fmean(lms),
+            "per_seed": [{"seed": sd, "plain_iterations": ip["iterations"], "plain_ms": ip["seconds"] * 1e3,
+                          "learned_iterations": il["iterations"], "learned_ms": il["seconds"] * 1e3}
+                         for sd, ip, il in rows],
+            "network": {"flop_per_apply": flop, "apply_ms_est": apply_ms,
+                        "tflops_est": flop / (apply_ms * 1e-3) / 1e12 if apply_ms > 0 else None,
+                        "train": {"box": [64, 64, 16], "triples": triples, "runs": runs, "seeds": "10-19",
+                                  "steps": tr["steps"], "batch": a.nn_batch, "seconds": tr["seconds"],
+                                  "first_loss": tr["first_loss"], "last_loss": tr["last_loss"],
+                                  "loss": "0.5 |z - x|^2/|x|^2 + 0.5 |A z - b|^2/|b|^2"}}}
 
 def _dist():
     rank = int(os.environ.get("RANK", "0"))

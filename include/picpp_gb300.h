@@ -246,6 +246,10 @@ typedef struct {
     double lr;                    /* Adam step size                               */
     unsigned long long seed;      /* random fields                                */
     int smooth_max;               /* fields get 0..smooth_max binomial passes     */
+    int source;                   /* 0: random fields on the context's operator;
+                                     1: the triples recorded by pic_nn_record      */
+    double supervised_weight;     /* source 1: weight w of |z - x|^2 / |x|^2 against
+                                     (1 - w) |A z - b|^2 / |b|^2                    */
 } pic_train_opts;
 typedef struct {
     double first_loss, last_loss; /* relative residual loss of the first step / of the
@@ -260,12 +264,24 @@ long pic_nn_param_count(void);
 pic_status pic_nn_init(pic_ctx* ctx, unsigned long long seed);
 pic_status pic_nn_set_params(pic_ctx* ctx, const float* params);
 pic_status pic_nn_get_params(pic_ctx* ctx, float* params);
-/* Trains on the operator of the last pic_update_electromagnetic_parameters
- * (or the mu of the last pic_maxwell_apply / pic_maxwell_solve): random
- * fields r of unit rms on the whole box, loss |A(mu) z - r|^2 / |r|^2 for
- * z = network(r, mu diagonal), back-propagated through A^T.  Box axes must
- * be multiples of 4. */
+/* source 0: trains on the operator of the last
+ * pic_update_electromagnetic_parameters (or the mu of the last
+ * pic_maxwell_apply / pic_maxwell_solve): random fields r of unit rms on the
+ * whole box, loss |A(mu) z - r|^2 / |r|^2 for z = network(r, mu diagonal),
+ * back-propagated through A^T.  source 1: trains on the recorded triples
+ * (b, mu, x) (pic_nn_record), each scaled to a unit-rms b, loss
+ * w |z - x|^2 / |x|^2 + (1 - w) |A(mu) z - b|^2 / |b|^2 with
+ * z = network(b, mu diagonal).  Box axes must be multiples of 4; periodic
+ * boxes only. */
 pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info* info);
+/* Starts keeping, for training, the (right-hand side, mu, FP64 solution)
+ * triples that the next plain field solves of pic_evaluate_electric_field
+ * (PIC_GMRES_REFERENCE / PIC_GMRES_RESTARTED) produce: the first capacity of
+ * them, in FP32 on the device (60 bytes per cell each), over any number of
+ * steps and reloaded species (runs); capacity 0 stops and frees them.  No
+ * reference counterpart.  count (may be NULL) receives the number kept. */
+pic_status pic_nn_record(pic_ctx* ctx, int capacity);
+pic_status pic_nn_record_count(pic_ctx* ctx, int* count);
 /* Forward pass on host input x0[n][d][h][w][16] (FP32, rounded to BF16),
  * out[n][d][h][w][16] FP32.  d, h, w multiples of 4. */
 pic_status pic_nn_forward(pic_ctx* ctx, int n, int d, int h, int w, const float* x0, float* out);

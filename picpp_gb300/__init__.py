@@ -35,7 +35,7 @@ EXPORTS = [
     "pic_maxwell_apply_transpose", "pic_maxwell_solve",
     "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile", "pic_energy_noalloc",
     "pic_fill_species", "pic_nn_param_count", "pic_nn_init", "pic_nn_set_params", "pic_nn_get_params",
-    "pic_nn_train", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
+    "pic_nn_train", "pic_nn_record", "pic_nn_record_count", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
     "pic_save_checkpoint", "pic_load_checkpoint",
 ]
 PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover", "deposit"]
@@ -71,7 +71,7 @@ class SolveInfo(C.Structure):
 
 class TrainOpts(C.Structure):
     _fields_ = [("steps", C.c_int), ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_ulonglong),
-                ("smooth_max", C.c_int)]
+                ("smooth_max", C.c_int), ("source", C.c_int), ("supervised_weight", C.c_double)]
 
 
 class TrainInfo(C.Structure):
@@ -141,6 +141,8 @@ def load_library(path: str | None = None):
     L.pic_nn_set_params.argtypes = [vp, _fp]
     L.pic_nn_get_params.argtypes = [vp, _fp]
     L.pic_nn_train.argtypes = [vp, C.POINTER(TrainOpts), C.POINTER(TrainInfo)]
+    L.pic_nn_record.argtypes = [vp, C.c_int]
+    L.pic_nn_record_count.argtypes = [vp, C.POINTER(C.c_int)]
     L.pic_nn_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp]
     L.pic_nn_loss_grad.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _dp, _fp]
     for name in EXPORTS:
@@ -409,11 +411,24 @@ class GpuSimulation:
         self._ck(self.L.pic_nn_get_params(self.ctx, _f(p)))
         return p
 
-    def nn_train(self, steps=200, batch=1, lr=1e-3, seed=1, smooth_max=4):
+    def nn_train(self, steps=200, batch=1, lr=1e-3, seed=1, smooth_max=4, source=0, supervised_weight=0.5):
+        """source 0: random fields on the current operator; 1: the recorded
+        (b, mu, x) triples (nn_record), loss weight supervised_weight on
+        |z - x|^2 / |x|^2 against the residual |A z - b|^2 / |b|^2."""
         info = TrainInfo()
-        self._ck(self.L.pic_nn_train(self.ctx, C.byref(TrainOpts(steps, batch, lr, seed, smooth_max)),
-                                     C.byref(info)))
+        opts = TrainOpts(steps, batch, lr, seed, smooth_max, source, supervised_weight)
+        self._ck(self.L.pic_nn_train(self.ctx, C.byref(opts), C.byref(info)))
         return info.as_dict()
+
+    def nn_record(self, capacity):
+        """Keep the (b, mu, x) triples of the next plain field solves, the
+        first `capacity` of them (0 stops and frees them)."""
+        self._ck(self.L.pic_nn_record(self.ctx, int(capacity)))
+
+    def nn_record_count(self) -> int:
+        n = C.c_int()
+        self._ck(self.L.pic_nn_record_count(self.ctx, C.byref(n)))
+        return n.value
 
     def nn_forward(self, x0):
         x0 = np.ascontiguousarray(x0, dtype=np.float32)

@@ -70,6 +70,7 @@ struct pic_ctx {
     bool moments_ready = false, efield_ready = false;
     bool mu_valid = false;   // ctx->mu holds an operator (moments or an uploaded mu)
     Net* net = nullptr;      // learned preconditioner, created by pic_nn_init / pic_nn_set_params
+    TripleStore trip;        // recorded (b, mu, x) triples of plain solves (pic_nn_record)
     double* smooth_tmp = nullptr;   // scratch of the smoothing passes (max(9N, rho-hat ext))
     bool fresh_sort = false;        // particles sorted and not moved since
     bool pending_compact = false;   // escaped particles (cell -1) not yet erased (wall boxes)
@@ -930,6 +931,12 @@ pic_status pic_evaluate_electric_field(pic_ctx* ctx, const pic_solve_opts* opts,
         if (ctx->prof_on && info) ctx->launches += 6L * info->iterations + 8;
     }
     if (st != PIC_OK && st != PIC_ERR_NOT_CONVERGED) return st;
+    const int method = opts ? opts->method : PIC_GMRES_REFERENCE;
+    if (st == PIC_OK && ctx->trip.data && method != PIC_FGMRES_LEARNED) {
+        pic_status rs = ctx->trip.add(ctx->s, ctx->rhs, ctx->mu, ctx->Et, ctx->partials + 7 * 1024, ctx->partials,
+                                      &ctx->err);
+        if (rs != PIC_OK) return rs;
+    }
     {
         Phase ph(ctx, PIC_PHASE_FIELDS, 1);
         launch_field_update(ctx->s, ctx->g, ctx->Et, ctx->Ei, ctx->Bi, ctx->En, ctx->Bn, 1, 0);
@@ -1335,11 +1342,33 @@ pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info
     if (!opts) return PIC_ERR_ARG;
     pic_status st = net_of(ctx, true);
     if (st != PIC_OK) return st;
-    if (!ctx->mu_valid) return fail(ctx, PIC_ERR_STATE, "no operator: update the electromagnetic parameters first");
+    if (!ctx->mu_valid && opts->source != 1)
+        return fail(ctx, PIC_ERR_STATE, "no operator: update the electromagnetic parameters first");
     if (ctx->g.wall) return fail(ctx, PIC_ERR_STATE, "train on a periodic box (the network is convolutional)");
-    st = ctx->net->train(ctx->s, ctx->g, ctx->mu, *opts, info, ctx->partials, &ctx->err);
+    if (opts->source == 1)
+        st = ctx->net->train_triples(ctx->s, ctx->g, ctx->trip, *opts, info, ctx->partials, &ctx->err);
+    else
+        st = ctx->net->train(ctx->s, ctx->g, ctx->mu, *opts, info, ctx->partials, &ctx->err);
     if (st != PIC_OK) return st;
     return sync(ctx, "nn train");
+}
+
+pic_status pic_nn_record(pic_ctx* ctx, int capacity) {
+    if (!ctx || capacity < 0) return PIC_ERR_ARG;
+    if (is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not an implicit run");
+    if (capacity == 0) {
+        ctx->trip.release();
+        return PIC_OK;
+    }
+    pic_status st = ctx->trip.reserve(capacity, ctx->g.N, &ctx->err);
+    if (st != PIC_OK) return st == PIC_ERR_CUDA ? fail(ctx, PIC_ERR_NOMEM, "no room for the triples") : st;
+    return PIC_OK;
+}
+
+pic_status pic_nn_record_count(pic_ctx* ctx, int* count) {
+    if (!ctx || !count) return PIC_ERR_ARG;
+    *count = ctx->trip.count;
+    return PIC_OK;
 }
 
 pic_status pic_nn_forward(pic_ctx* ctx, int n, int d, int h, int w, const float* x0, float* out) {

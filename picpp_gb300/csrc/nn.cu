@@ -173,6 +173,22 @@ __global__ void k_noise(double* __restrict__ x, long long n, unsigned long long 
         x[e] = 2.0 * ((nn_mix(seed * 0x100000001B3ull + (unsigned long long)e) >> 11) * 0x1.0p-53) - 1.0;
 }
 
+__global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+__global__ void k_f2d(const float* __restrict__ a, double* __restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
+// y = a y + b x
+__global__ void k_axpby(double* __restrict__ y, const double* __restrict__ x, double a, double b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = a * y[i] + b * x[i];
+}
+
 // One periodic binomial (1 2 1) / 4 pass along every active axis of a
 // 3-component field, src -> dst.
 __global__ void k_smooth(GridP g, const double* __restrict__ src, double* __restrict__ dst) {
@@ -612,6 +628,184 @@ pic_status Net::train(cudaStream_t s, const GridP& g, const double* mu, const pi
                 best = lv;
                 // the loss was measured before this step's update: keep the
                 // parameters that produced it
+                cudaMemcpyAsync(best_p, prev_p, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
+            }
+        }
+    }
+    if (!(last <= best) && std::isfinite(best)) {
+        cudaMemcpyAsync(p_, best_p, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
+        refresh_bf16(s);
+        last = best;
+    }
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t ce = cudaGetLastError();
+    cleanup();
+    NCK(ce);
+    if (info) {
+        info->first_loss = first;
+        info->last_loss = last;
+        info->seconds = ms * 1e-3;
+        info->steps = steps;
+    }
+    if (!std::isfinite(last)) {
+        if (err) *err = "training diverged";
+        return PIC_ERR_NUMERIC;
+    }
+    return check_tc(s, err);
+}
+
+// ---- recorded triples ---------------------------------------------------
+TripleStore::~TripleStore() { release(); }
+
+void TripleStore::release() {
+    cudaFree(data);
+    data = nullptr;
+    cap = count = 0;
+    N = 0;
+    xx.clear();
+}
+
+pic_status TripleStore::reserve(int capacity, long long n, std::string* err) {
+    release();
+    if (capacity <= 0) return PIC_OK;
+    NCK(cudaMalloc(&data, sizeof(float) * 15 * (size_t)n * (size_t)capacity));
+    cap = capacity;
+    N = n;
+    return PIC_OK;
+}
+
+pic_status TripleStore::add(cudaStream_t s, const double* b, const double* mu, const double* x, double* scal,
+                            double* partials, std::string* err) {
+    if (!data || count >= cap) return PIC_OK;
+    float* dst = data + (size_t)count * 15 * (size_t)N;
+    const long long L = 3 * N;
+    k_d2f<<<gs(L), 256, 0, s>>>(b, dst, L);
+    k_d2f<<<gs(3 * L), 256, 0, s>>>(mu, dst + L, 3 * L);
+    k_d2f<<<gs(L), 256, 0, s>>>(x, dst + 4 * L, L);
+    launch_dot(s, b, b, L, partials, red_blocks(L), scal, 0);
+    launch_dot(s, x, x, L, partials, red_blocks(L), scal + 1, 0);
+    double h[2] = {0, 0};
+    NCK(cudaMemcpyAsync(h, scal, sizeof(h), cudaMemcpyDeviceToHost, s));
+    NCK(cudaStreamSynchronize(s));
+    xx.push_back(h[0] > 0 ? h[1] / h[0] : 0.0);
+    ++count;
+    return PIC_OK;
+}
+
+pic_status Net::train_triples(cudaStream_t s, const GridP& g, const TripleStore& ts, const pic_train_opts& o,
+                              pic_train_info* info, double* partials, std::string* err) {
+    if (!ready_) { if (err) *err = "network not initialised"; return PIC_ERR_STATE; }
+    if (ts.count < 1 || ts.N != g.N) { if (err) *err = "no recorded triples of this box"; return PIC_ERR_STATE; }
+    const int nb = o.batch > 0 ? o.batch : 1;
+    if (g.nx % 4 || g.ny % 4 || g.nz % 4) {
+        if (err) *err = "box axes must be multiples of 4";
+        return PIC_ERR_ARG;
+    }
+    NetBuffers* b = nullptr;
+    pic_status st = buffers(s, nb, g.nz, g.ny, g.nx, true, &b, err);
+    if (st != PIC_OK) return st;
+    const long long L = 3 * g.N, V = g.N;
+    std::vector<void*> tmp;
+    auto cleanup = [&]() { for (void* p : tmp) cudaFree(p); };
+    auto al = [&](void** p, size_t bytes) -> bool {
+        if (cudaMalloc(p, bytes) != cudaSuccess) return false;
+        tmp.push_back(*p);
+        return true;
+    };
+    double *bb = nullptr, *xb = nullptr, *mb = nullptr, *z = nullptr, *e = nullptr, *es = nullptr, *t = nullptr,
+           *wm = nullptr, *scal = nullptr;
+    float *best_p = nullptr, *prev_p = nullptr;
+    const size_t d8 = sizeof(double);
+    if (!al((void**)&bb, d8 * L * nb) || !al((void**)&xb, d8 * L * nb) || !al((void**)&mb, d8 * 3 * L * nb) ||
+        !al((void**)&z, d8 * L) || !al((void**)&e, d8 * L) || !al((void**)&es, d8 * L) || !al((void**)&t, d8 * L) ||
+        !al((void**)&wm, d8 * L) || !al((void**)&scal, d8 * (4 + (size_t)nb)) ||
+        !al((void**)&best_p, sizeof(float) * param_count()) || !al((void**)&prev_p, sizeof(float) * param_count())) {
+        cleanup();
+        if (err) *err = "out of device memory for training";
+        return PIC_ERR_NOMEM;
+    }
+    const OpCoef oc = make_opcoef(g);
+    const double ws = std::min(std::max(o.supervised_weight, 0.0), 1.0), wr = 1.0 - ws;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    unsigned long long rng = o.seed * 0x9E3779B97F4A7C15ull + 777;
+    auto next = [&]() {
+        rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17;   // xorshift64
+        return rng;
+    };
+    if (gate_pending_) {   // the recorded solutions decide nothing here: start from the identity
+        const float g1 = 1.0f;
+        cudaMemcpyAsync(p_ + param_count() - 1, &g1, sizeof(float), cudaMemcpyHostToDevice, s);
+        gate_pending_ = false;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    double first = 0, last = 0, best = INFINITY;
+    constexpr int kCheck = 50;
+    const int steps = o.steps > 0 ? o.steps : 1;
+    std::vector<int> pick(nb);
+    const float* gate = p_ + param_count() - 1;
+    for (int it = 0; it < steps; ++it) {
+        for (int q = 0; q < nb; ++q) {
+            pick[q] = (int)(next() % (unsigned long long)ts.count);
+            const float* src = ts.data + (size_t)pick[q] * 15 * (size_t)ts.N;
+            double* bq = bb + (size_t)q * L;
+            double* xq = xb + (size_t)q * L;
+            double* mq = mb + (size_t)q * 3 * L;
+            k_f2d<<<gs(L), 256, 0, s>>>(src, bq, L);
+            k_f2d<<<gs(3 * L), 256, 0, s>>>(src + L, mq, 3 * L);
+            k_f2d<<<gs(L), 256, 0, s>>>(src + 4 * L, xq, L);
+            // b to unit rms, x by the same factor (A x = b is linear)
+            launch_dot(s, bq, bq, L, partials, red_blocks(L), scal, 1);
+            k_rescale_by_norm<<<gs(L), 256, 0, s>>>(bq, L, scal);
+            k_rescale_by_norm<<<gs(L), 256, 0, s>>>(xq, L, scal);
+            k_pack_box<<<gs(V), 256, 0, s>>>(bq, 1.0, mq, b->x0 + (size_t)q * V * 16, V);
+        }
+        forward(s, *b);
+        cudaMemsetAsync(loss_, 0, sizeof(double), s);
+        for (int q = 0; q < nb; ++q) {
+            const double* bq = bb + (size_t)q * L;
+            const double* xq = xb + (size_t)q * L;
+            const double* mq = mb + (size_t)q * 3 * L;
+            const double xx = ts.xx[pick[q]] > 0 ? ts.xx[pick[q]] : 1.0;   // |x|^2 / |b|^2, |b|^2 = L now
+            k_unpack_box<<<gs(V), 256, 0, s>>>(b->out + (size_t)q * V * 16, 1.0, bq, gate, z, V);
+            // residual part: e = A z - b, t = A^T e
+            launch_maxwell_apply(s, g, oc, mq, z, e, wm);
+            k_sub_loss<<<gs(L), 256, 0, s>>>(e, bq, L, wr / ((double)L * nb), loss_);
+            launch_maxwell_apply_t(s, g, oc, mq, e, t);
+            // supervised part: es = z - x
+            cudaMemcpyAsync(es, z, sizeof(double) * L, cudaMemcpyDeviceToDevice, s);
+            k_sub_loss<<<gs(L), 256, 0, s>>>(es, xq, L, ws / (xx * (double)L * nb), loss_);
+            // dL/dz = 2 (1 - w) A^T e / (L nb) + 2 w (z - x) / (|x|^2 nb)
+            k_axpby<<<gs(L), 256, 0, s>>>(t, es, 2.0 * wr / ((double)L * nb), 2.0 * ws / (xx * (double)L * nb), L);
+            k_pack_grad<<<gs(V), 256, 0, s>>>(t, 1.0, b->A0 + (size_t)q * V * 16, V);
+            launch_dot(s, t, bq, L, partials, red_blocks(L), scal + 4 + q, 0);
+        }
+        cudaMemsetAsync(g_, 0, sizeof(float) * param_count(), s);
+        backward(s, *b);
+        k_gate_grad<<<1, 1, 0, s>>>(scal + 4, nb, 1.0, g_ + param_count() - 1);
+        const bool check = it == 0 || it == steps - 1 || it % kCheck == kCheck - 1;
+        if (check) cudaMemcpyAsync(prev_p, p_, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
+        ++adam_t_;
+        const float c1 = (float)(o.lr / (1.0 - std::pow((double)b1, adam_t_)));
+        const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, adam_t_)));
+        nn::k_adam<<<gs(param_count()), 256, 0, s>>>(p_, g_, m_, v_, param_count(), b1, b2, eps, c1, c2);
+        refresh_bf16(s);
+        if (check) {
+            double lv = 0;
+            cudaMemcpyAsync(&lv, loss_, sizeof(double), cudaMemcpyDeviceToHost, s);
+            cudaError_t ce = cudaStreamSynchronize(s);
+            if (ce != cudaSuccess) { cleanup(); NCK(ce); }
+            if (it == 0) first = lv;
+            last = lv;
+            if (std::isfinite(lv) && lv < best) {
+                best = lv;
                 cudaMemcpyAsync(best_p, prev_p, sizeof(float) * param_count(), cudaMemcpyDeviceToDevice, s);
             }
         }

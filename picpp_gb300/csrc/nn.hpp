@@ -26,6 +26,21 @@ struct NetLayer {
 
 struct NetBuffers;   // activations and gradients of one shape (nn.cu)
 
+// (right-hand side b, mu, solution x) triples of plain field solves, kept in
+// FP32 on the device for training the network: the first `cap` recorded.
+struct TripleStore {
+    int cap = 0, count = 0;
+    long long N = 0;             // cells of the box they come from
+    float* data = nullptr;       // per triple: b [3N], mu [9N], x [3N]
+    std::vector<double> xx;      // |x|^2 / |b|^2 of each triple
+    ~TripleStore();
+    void release();
+    pic_status reserve(int capacity, long long n, std::string* err);
+    // stores one more triple unless full; scal, partials: reduction scratch
+    pic_status add(cudaStream_t s, const double* b, const double* mu, const double* x, double* scal,
+                   double* partials, std::string* err);
+};
+
 
 
 class Net {
@@ -58,6 +73,12 @@ public:
     // and, dotted with r, gives the gate's.
     pic_status train(cudaStream_t s, const GridP& g, const double* mu, const pic_train_opts& o, pic_train_info* info,
                      double* partials, std::string* err);
+    // Training on recorded triples (b, mu, x) of the box g: batches of
+    // o.batch triples, loss w |z - x|^2 / |x|^2 + (1 - w) |A(mu) z - b|^2 / |b|^2
+    // with z = g b + net(b, mu diagonal) and w = o.supervised_weight, every
+    // triple scaled to a unit-rms right-hand side.
+    pic_status train_triples(cudaStream_t s, const GridP& g, const TripleStore& ts, const pic_train_opts& o,
+                             pic_train_info* info, double* partials, std::string* err);
 
 private:
     pic_status buffers(cudaStream_t s, int n, int d, int h, int w, bool grads, NetBuffers** out, std::string* err);

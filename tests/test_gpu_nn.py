@@ -185,3 +185,42 @@ def test_learned_solver_needs_a_network_and_a_box_of_fours(pg):
     with pytest.raises(pg.PicError) as e:
         sim6.maxwell_solve(np.zeros(9 * N), np.ones(3 * N), pg.solve_opts(pg.FGMRES_LEARNED))
     assert e.value.status == 1
+
+
+def test_training_on_recorded_solve_triples(pg):
+    """The plain field solves of a few implicit steps of two runs (species
+    reloaded) are recorded as (b, mu, x) triples, the first `capacity` kept;
+    training on them lowers the combined supervised and residual loss, and
+    FGMRES with the trained network reaches the tolerance on the next system
+    of a third run."""
+    box = I.Box(16, 16, 8, 0.5, 0.5, 0.5, 0.5, theta=0.5)
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=0, pressure_compat=0, sort_every=1)
+    w = I.density_weight(box, 1.0 / (4 * np.pi), 8)
+    sim.add_species(-1.0, 1.0, w, 8 * box.ncells)
+    sim.add_species(1.0, 25.0, w, 8 * box.ncells)
+    E, B = I.zero_fields(box)
+    B[2] = 0.5
+    opts = pg.solve_opts(pg.GMRES_RESTARTED, restart=30, max_iter=600, tol=1e-8)
+    sim.nn_record(5)
+    for run in range(2):
+        sim.fill_species(0, 8, 10 + 2 * run, 0.01, 10.0, True)
+        sim.fill_species(1, 8, 11 + 2 * run, 0.01 / 25, 10.0, True)
+        sim.upload_fields(E, B)
+        for _ in range(3):
+            sim.implicit_step(opts)
+    assert sim.nn_record_count() == 5
+    sim.nn_init(3)
+    info = sim.nn_train(steps=300, batch=2, lr=1e-3, seed=4, source=1, supervised_weight=0.5)
+    assert info["last_loss"] < info["first_loss"]
+    sim.fill_species(0, 8, 30, 0.01, 10.0, True)
+    sim.fill_species(1, 8, 31, 0.01 / 25, 10.0, True)
+    sim.upload_fields(E, B)
+    sim.implicit_step(opts)
+    sim.updateElectroMagneticParameters()
+    _, mu, _, rhs = sim.download_moments()
+    x, learned = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.FGMRES_LEARNED, restart=30, max_iter=600, tol=1e-8))
+    r = O.maxwell_apply(O.make_grid(box), mu, x) - rhs
+    assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1.01e-8
+    sim.nn_record(0)
+    assert sim.nn_record_count() == 0
+    sim.close()

@@ -35,7 +35,7 @@ EXPORTS = [
     "pic_maxwell_apply_transpose", "pic_maxwell_solve",
     "pic_sort_particles", "pic_download_permutation", "pic_energy", "pic_profile", "pic_energy_noalloc",
     "pic_fill_species", "pic_nn_param_count", "pic_nn_init", "pic_nn_set_params", "pic_nn_get_params",
-    "pic_nn_train", "pic_nn_record", "pic_nn_record_count", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
+    "pic_nn_train", "pic_nn_record", "pic_nn_record_count", "pic_nn_wait_limit", "pic_nn_forward", "pic_nn_loss_grad", "pic_update_density_parameters", "pic_download_density",
     "pic_save_checkpoint", "pic_load_checkpoint",
 ]
 PHASES = ["sort", "fields", "push_deposit", "assemble", "moments", "solve", "mover", "deposit"]
@@ -142,6 +142,7 @@ def load_library(path: str | None = None):
     L.pic_nn_get_params.argtypes = [vp, _fp]
     L.pic_nn_train.argtypes = [vp, C.POINTER(TrainOpts), C.POINTER(TrainInfo)]
     L.pic_nn_record.argtypes = [vp, C.c_int]
+    L.pic_nn_wait_limit.argtypes = [vp, C.c_uint]
     L.pic_nn_record_count.argtypes = [vp, C.POINTER(C.c_int)]
     L.pic_nn_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp]
     L.pic_nn_loss_grad.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _dp, _fp]
@@ -419,6 +420,10 @@ class GpuSimulation:
         opts = TrainOpts(steps, batch, lr, seed, smooth_max, source, supervised_weight)
         self._ck(self.L.pic_nn_train(self.ctx, C.byref(opts), C.byref(info)))
         return info.as_dict()
+
+    def nn_wait_limit(self, polls):
+        """Bound of the convolutions' MMA-completion wait (0: built-in)."""
+        self._ck(self.L.pic_nn_wait_limit(self.ctx, int(polls)))
 
     def nn_record(self, capacity):
         """Keep the (b, mu, x) triples of the next plain field solves, the

@@ -1353,6 +1353,13 @@ pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info
     return sync(ctx, "nn train");
 }
 
+pic_status pic_nn_wait_limit(pic_ctx* ctx, unsigned polls) {
+    pic_status st = net_of(ctx, true);
+    if (st != PIC_OK) return st;
+    ctx->net->set_wait_limit(polls);
+    return PIC_OK;
+}
+
 pic_status pic_nn_record(pic_ctx* ctx, int capacity) {
     if (!ctx || capacity < 0) return PIC_ERR_ARG;
     if (is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not an implicit run");

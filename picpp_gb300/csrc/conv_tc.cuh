@@ -67,8 +67,8 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                  : "memory");
 }
 
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
-    for (unsigned it = 0; it < kTcWaitLimit; ++it) {
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, unsigned limit = kTcWaitLimit) {
+    for (unsigned it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred P1;\n mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __nv_bfloat16* __
                                                          const float* __restrict__ bias,
                                                          __nv_bfloat16* __restrict__ y16, float* __restrict__ y32,
                                                          int dN, int dD, int dH, int dW, int relu,
-                                                         int* __restrict__ err) {
+                                                         int* __restrict__ err, unsigned wait_limit) {
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 128, "channel counts");
     constexpr int C8 = CIN / 8;
     constexpr bool kAll = tc_all_taps(CIN, COUT);
@@ -195,8 +195,10 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __nv_bfloat16* __
         }
         __syncwarp();
         // every thread waits: the next stage overwrites the weights, the
-        // epilogue reads TMEM; the outcome is made CTA-uniform
-        const bool done = tc_wait(mbar, (uint32_t)(st & 1));
+        // epilogue reads TMEM; the outcome is made CTA-uniform.  wait_limit
+        // bounds this completion wait (0: kTcWaitLimit polls); the wait before
+        // the tensor memory is released below always takes the full bound
+        const bool done = tc_wait(mbar, (uint32_t)(st & 1), wait_limit ? wait_limit : kTcWaitLimit);
         ok = __syncthreads_and(done) != 0;
         tc_fence_after();
         if (!ok) {

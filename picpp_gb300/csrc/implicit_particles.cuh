@@ -100,19 +100,17 @@ template <typename T> __device__ __forceinline__ T picard_bound(T tol, T ref) { 
 }
 
 // The loop test itself: go on while both changes exceed their thresholds
-// and fewer than three iterations ran.  The FP32 push applies the
-// displacement test from the second iteration on: the first iteration's
-// displacement differs from the predictor's only through quantities taken
-// at the old position, so its change can fall below FP32 resolution while
-// the fields at the mid point, which the second iteration brings in, still
-// move the particle (measured: 2e-5-cell position errors of gamma = 10 ions
-// that stopped after one iteration).  FP64 keeps the reference's test.
+// and fewer than three iterations ran.  The displacement change after the
+// first iteration measures the predictor against an iterate that still
+// uses the fields at the old position; where FP64 finds it just below
+// 1e-8 dx and stops there, FP32 resolves it only to about 3e-8 dx and may
+// take the second iteration, whose velocity includes the fields at the mid
+// point (measured: up to 2e-5 cells, 3e-7 of the box, for a few hundred of
+// 4.2 million gamma = 10 ions of a 64x64x16 box).
 template <typename T>
 __device__ __forceinline__ bool picard_continue(T err, T momNorm, T cerr, T dxN, int it) {
-    const bool mom = err > picard_bound<T>(picard_mom_tol<T>(), momNorm);
-    bool pos = cerr > picard_bound<T>(picard_pos_tol<T>(), dxN);
-    if constexpr (sizeof(T) == sizeof(float)) pos = pos || it < 2;
-    return mom && pos && it < 3;
+    return err > picard_bound<T>(picard_mom_tol<T>(), momNorm) && cerr > picard_bound<T>(picard_pos_tol<T>(), dxN) &&
+           it < 3;
 }
 
 template <typename T>

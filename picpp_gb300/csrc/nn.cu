@@ -47,7 +47,7 @@ int gs(long long n) { return grid_for(n, 256, 16); }
 
 template <int CI, int CO>
 void conv_t(cudaStream_t s, const bf16* x, const bf16* W, const float* b, bf16* y16, float* y32, Dims d, int relu,
-            int* err) {
+            int* err, unsigned wait_limit) {
     static bool attr = false;
     const size_t sm = nn::tc_conv_smem_bytes(CI, CO);
     if (!attr) {
@@ -55,15 +55,16 @@ void conv_t(cudaStream_t s, const bf16* x, const bf16* W, const float* b, bf16* 
         attr = true;
     }
     dim3 grid((d.W + nn::kTcW - 1) / nn::kTcW, (d.H + nn::kTcH - 1) / nn::kTcH, d.N * d.D);
-    nn::k_conv3_tc<CI, CO><<<grid, nn::kTcThreads, sm, s>>>(x, W, b, y16, y32, d.N, d.D, d.H, d.W, relu, err);
+    nn::k_conv3_tc<CI, CO><<<grid, nn::kTcThreads, sm, s>>>(x, W, b, y16, y32, d.N, d.D, d.H, d.W, relu, err,
+                                                              wait_limit);
 }
 
 // Every (cin, cout) pair of the forward layers and of their input-gradient
 // (transposed) convolutions.
 void conv(cudaStream_t s, int ci, int co, const bf16* x, const bf16* W, const float* b, bf16* y16, float* y32, Dims d,
-          int relu, int* err) {
+          int relu, int* err, unsigned wait_limit) {
 #define PIC_CONV(A, B) \
-    if (ci == A && co == B) return conv_t<A, B>(s, x, W, b, y16, y32, d, relu, err)
+    if (ci == A && co == B) return conv_t<A, B>(s, x, W, b, y16, y32, d, relu, err, wait_limit)
     PIC_CONV(16, 16); PIC_CONV(16, 32); PIC_CONV(32, 16); PIC_CONV(32, 32); PIC_CONV(32, 64); PIC_CONV(64, 32);
     PIC_CONV(64, 64); PIC_CONV(96, 32); PIC_CONV(32, 96); PIC_CONV(48, 16); PIC_CONV(16, 48);
 #undef PIC_CONV
@@ -392,7 +393,7 @@ void Net::forward(cudaStream_t s, NetBuffers& b) {
     const bf16* wk = (const bf16*)wk_;
     auto cv = [&](int li, const bf16* x, bf16* y16, float* y32, Dims d) {
         const NetLayer& l = L[li];
-        conv(s, l.cin, l.cout, x, wk + l.woff, p_ + l.boff, y16, y32, d, l.relu, tc_err_);
+        conv(s, l.cin, l.cout, x, wk + l.woff, p_ + l.boff, y16, y32, d, l.relu, tc_err_, wait_limit_);
     };
     cv(E0A, b.x0, b.e0a, nullptr, b.dm0);
     cv(E0B, b.e0a, b.e0, nullptr, b.dm0);
@@ -422,7 +423,7 @@ void Net::backward(cudaStream_t s, NetBuffers& b) {
         const long long n = d.vox() * l.cout;
         nn::k_relu_bwd<<<gs(n), 256, 0, s>>>(gy, l.relu ? y : nullptr, b.g16, n);
         wgrad(s, l.cin, l.cout, x, b.g16, d, g_ + l.woff, g_ + l.boff);
-        if (gx) conv(s, l.cout, l.cin, b.g16, wt + l.woff, nullptr, nullptr, gx, d, 0, tc_err_);
+        if (gx) conv(s, l.cout, l.cin, b.g16, wt + l.woff, nullptr, nullptr, gx, d, 0, tc_err_, wait_limit_);
     };
     back(HEAD, b.A0, nullptr, b.d0, b.B0, b.dm0);
     back(D0B, b.B0, b.d0, b.d0a, b.A0, b.dm0);

@@ -54,6 +54,9 @@ public:
     pic_status set_params(cudaStream_t s, const float* host, std::string* err);
     pic_status get_params(cudaStream_t s, float* host, std::string* err);
     bool ready() const { return ready_; }
+    // polls of the convolutions' MMA-completion wait before it gives up and
+    // reports an error (0: the built-in bound)
+    void set_wait_limit(unsigned polls) { wait_limit_ = polls; }
     // waits for the stream; an error if a convolution reported a timed-out wait
     pic_status check_tc(cudaStream_t s, std::string* err);
 
@@ -91,6 +94,7 @@ private:
     double* loss_ = nullptr;
     int* tc_err_ = nullptr;   // set by a convolution whose MMA completion wait ran out
     int adam_t_ = 0;
+    unsigned wait_limit_ = 0;
     bool gate_pending_ = false;   // fresh network: training picks the gate's start
     bool ready_ = false;
     std::vector<NetBuffers*> bufs_;

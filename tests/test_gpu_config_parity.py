@@ -9,8 +9,8 @@ largest difference in cells is reported beside it.  On the FP32 push a few
 gamma = 10 ions move up to 2e-5 cells away from the FP64 result: where the
 FP64 mover's displacement change after the first Picard iteration falls
 just below the reference's 1e-8 dx threshold (mover.cpp:222-223), the FP64
-run stops there, while that change lies below FP32 resolution and the FP32
-run takes the second iteration, whose velocity includes the fields at the
+run stops there, while FP32 resolves that change only to about 3e-8 dx and
+may take the second iteration, whose velocity includes the fields at the
 mid point.  Every measured error is printed (pytest -rP shows it) so that
 the numbers behind the bounds can be read off a run.
 

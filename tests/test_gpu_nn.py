@@ -224,3 +224,25 @@ def test_training_on_recorded_solve_triples(pg):
     sim.nn_record(0)
     assert sim.nn_record_count() == 0
     sim.close()
+
+
+def test_convolution_wait_bound_reports_and_the_context_stays_usable(pg):
+    """A one-poll bound on the convolutions' MMA-completion wait makes the
+    wait run out: the forward pass returns PIC_ERR_CUDA, the CTAs still wait
+    for their MMAs (full bound) before releasing tensor memory, and with the
+    bound restored the same context computes the same output as before."""
+    box = I.Box(16, 16, 8, 0.5, 0.5, 0.5, 0.5)
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    sim.nn_set_params(NN.init_params(3))
+    rng = np.random.default_rng(21)
+    x0 = np.zeros((1, 8, 16, 16, 16), dtype=np.float32)
+    x0[..., :6] = rng.standard_normal((1, 8, 16, 16, 6))
+    before = sim.nn_forward(x0)
+    sim.nn_wait_limit(1)
+    with pytest.raises(pg.PicError) as e:
+        sim.nn_forward(x0)
+    assert e.value.status == 2
+    sim.nn_wait_limit(0)
+    after = sim.nn_forward(x0)
+    assert np.array_equal(after, before)
+    sim.close()

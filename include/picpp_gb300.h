@@ -274,12 +274,14 @@ pic_status pic_nn_get_params(pic_ctx* ctx, float* params);
  * z = network(b, mu diagonal).  Box axes must be multiples of 4; periodic
  * boxes only. */
 pic_status pic_nn_train(pic_ctx* ctx, const pic_train_opts* opts, pic_train_info* info);
-/* The number of mbarrier polls the network's tensor-core convolutions make
- * while waiting for their MMAs to complete before they give up: the calls
+/* The number of non-blocking mbarrier polls (test_wait) the network's
+ * tensor-core convolutions make while waiting for their MMAs to complete
+ * before they give up: the calls
  * that ran the network then return PIC_ERR_CUDA ("an MMA completion wait
  * ran out") and the context stays usable; the wait before a CTA releases
  * its tensor memory keeps the built-in bound, so no memory is released
- * under an MMA in flight.  0 restores the built-in bound (2^22 polls).  No
+ * under an MMA in flight.  0 restores the built-in bound (2^22 blocking
+ * try_wait polls).  No
  * reference counterpart (failure detection of the device waits). */
 pic_status pic_nn_wait_limit(pic_ctx* ctx, unsigned polls);
 /* Starts keeping, for training, the (right-hand side, mu, FP64 solution)

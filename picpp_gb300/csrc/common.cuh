@@ -23,14 +23,17 @@ struct FastDiv {
 
 struct GridP {
     int nx, ny, nz;
+    int wall;             // 1: conductor wall at x = 0, open boundary at x = (nx - 2) dx (wall.cuh)
     long long N;          // nx*ny*nz
     double dx, dy, dz, dt;
     double idx, idy, idz; // 1/dx ...
     double theta, eta, cfix;
     int y3, z3;           // ny > 1, nz > 1
     FastDiv divx, divy;   // by nx, by ny
-    int wall;             // 1: conductor wall at x = 0, open boundary at x = (nx - 2) dx (wall.cuh)
 };
+// 128 bytes: the size up to which the out-of-line gathers take it in
+// registers (a larger struct goes through a stack frame)
+static_assert(sizeof(GridP) == 128, "GridP layout");
 
 __device__ __forceinline__ int fast_div(int n, const FastDiv& f) {
     return (int)((__umulhi(f.m, (unsigned)n) + (unsigned)n) >> f.l);

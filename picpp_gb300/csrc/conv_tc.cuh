@@ -81,6 +81,22 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, unsigned
     return false;
 }
 
+// The same wait with a poll count that means polls: test_wait returns at
+// once, where one try_wait may itself block for a hardware-chosen time.
+__device__ __forceinline__ bool tc_poll(uint32_t mbar, uint32_t parity, unsigned polls) {
+    for (unsigned it = 0; it < polls; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred P1;\n mbarrier.test_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+            " selp.b32 %0, 1, 0, P1;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // 8 consecutive FP32 accumulator columns of this thread's TMEM lane.
 __device__ __forceinline__ void tc_ld8(uint32_t taddr, float v[8]) {
     uint32_t r[8];
@@ -195,10 +211,12 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __nv_bfloat16* __
         }
         __syncwarp();
         // every thread waits: the next stage overwrites the weights, the
-        // epilogue reads TMEM; the outcome is made CTA-uniform.  wait_limit
-        // bounds this completion wait (0: kTcWaitLimit polls); the wait before
-        // the tensor memory is released below always takes the full bound
-        const bool done = tc_wait(mbar, (uint32_t)(st & 1), wait_limit ? wait_limit : kTcWaitLimit);
+        // epilogue reads TMEM; the outcome is made CTA-uniform.  A nonzero
+        // wait_limit bounds this completion wait to that many non-blocking
+        // polls (0: kTcWaitLimit blocking polls); the wait before the tensor
+        // memory is released below always takes the full bound
+        const bool done = wait_limit ? tc_poll(mbar, (uint32_t)(st & 1), wait_limit)
+                                     : tc_wait(mbar, (uint32_t)(st & 1));
         ok = __syncthreads_and(done) != 0;
         tc_fence_after();
         if (!ok) {

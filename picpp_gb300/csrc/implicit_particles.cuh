@@ -225,7 +225,7 @@ __device__ __forceinline__ void evaluate_velocity(const T p[3], T m, T v[3]) {
 // three Picard iterations re-gathering E^{n+theta} (nodes) and B^n (cells).
 // alpha is recomputed from E^n, B^n at x^n (what evaluateParticlesRotationTensor
 // stored, mover.cpp:810-841).
-template <typename T>
+template <typename T, bool kWall>
 __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, double q, double m,
                                                        const double* __restrict__ E, const double* __restrict__ B,
                                                        const double* __restrict__ Et) {
@@ -262,12 +262,14 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
         T mv[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
-        if (g.wall && wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
-            wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
-            p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
-            p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
-            p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
-            continue;
+        if constexpr (kWall) {
+            if (wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
+                wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+                p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+                p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+                continue;
+            }
         }
         T vh[3];
 #pragma unroll
@@ -294,10 +296,12 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
             for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
 #pragma unroll
             for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
-            if (g.wall && wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
-                wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
-                reflected = true;
-                break;
+            if constexpr (kWall) {
+                if (wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
+                    wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                    reflected = true;
+                    break;
+                }
             }
             int tc[3];
             T tu[3];
@@ -318,7 +322,7 @@ __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, d
                             (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
         }
         if (!reflected) {
-            if (g.wall) {
+            if constexpr (kWall) {
                 const int o = wall_final_x<T>(g, ci[0], u0[0], (mv[0] * dt) * id[0]);
                 if (o == 2) { p.cell[n] = -1; continue; }   // escaped through the open boundary
                 if (o == 1) pnew[0] = -pnew[0];

@@ -582,7 +582,7 @@ __device__ __noinline__ Comp3<T> gather_global_1(const GridP g, int c0, int c1, 
 // precision, so the predictor and the up to three Picard gathers read
 // shared memory; a particle whose stencil leaves the block gathers from the
 // FP64 grids.  Same arithmetic as k_implicit_push.
-template <typename T>
+template <typename T, bool kWall>
 __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g, TileGeom t, MoverBlock mb, ImpSpecies<T> S,
                                                             const double* __restrict__ E, const double* __restrict__ B,
                                                             const double* __restrict__ Et) {
@@ -699,12 +699,14 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T mv[3];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
-                if (g.wall && wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
-                    wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
-                    p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
-                    p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
-                    p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
-                    continue;
+                if constexpr (kWall) {
+                    if (wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
+                        wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                        p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+                        p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+                        p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+                        continue;
+                    }
                 }
                 T vh[3];
 #pragma unroll
@@ -731,10 +733,12 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
 #pragma unroll
                     for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
-                    if (g.wall && wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
-                        wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
-                        reflected = true;
-                        break;
+                    if constexpr (kWall) {
+                        if (wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
+                            wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                            reflected = true;
+                            break;
+                        }
                     }
                     int tc[3];
                     T tu[3];
@@ -758,7 +762,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                                     (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
                 }
                 if (!reflected) {
-                    if (g.wall) {
+                    if constexpr (kWall) {
                         const int o = wall_final_x<T>(g, ci[0], u0[0], (mv[0] * dt) * id[0]);
                         if (o == 2) { p.cell[n] = -1; continue; }   // escaped through the open boundary
                         if (o == 1) pnew[0] = -pnew[0];

@@ -281,13 +281,19 @@ bool PK<T>::implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& 
     if (smem > 227 * 1024) return false;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_implicit_push_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_implicit_push_tile<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_implicit_push_tile<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr_set = true;
     }
     const int per_sm = (int)((228 * 1024) / (smem + 1024));
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int cap = kNumSM * (per_sm > 0 ? per_sm : 1);
-    k_implicit_push_tile<T><<<ntiles < cap ? ntiles : cap, kMoverThreads, smem, s>>>(g, t, mb, S, E, B, Et);
+    // the wall rules are a separate instantiation: the periodic mover keeps
+    // none of their code in its loop
+    if (g.wall)
+        k_implicit_push_tile<T, true><<<ntiles < cap ? ntiles : cap, kMoverThreads, smem, s>>>(g, t, mb, S, E, B, Et);
+    else
+        k_implicit_push_tile<T, false><<<ntiles < cap ? ntiles : cap, kMoverThreads, smem, s>>>(g, t, mb, S, E, B, Et);
     return true;
 }
 
@@ -295,7 +301,8 @@ template <typename T>
 void PK<T>::implicit_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const double* E,
                           const double* B, const double* Et) {
     if (p.n == 0) return;
-    k_implicit_push<T><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, E, B, Et);
+    if (g.wall) k_implicit_push<T, true><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, E, B, Et);
+    else k_implicit_push<T, false><<<grid_for(p.n, 128, 32), 128, 0, s>>>(g, p, q, m, E, B, Et);
 }
 
 template <typename T>

@@ -125,6 +125,11 @@ void orc_yee_b_half(const orc_grid* g, const double* E, double* B) {
         for (int j = 0; j < g->ny; ++j)
             for (int i = 0; i < g->nx; ++i) {
                 long c = IX(g, i, j, k);
+                /* conductor wall: the reference updates Bx on nodes
+                 * minI..maxI and By, Bz on cells minI..maxI-1 (fields.cpp
+                 * 44-70); the ghost columns keep their values */
+                if (g->wall_x && i == g->nx - 1) continue;
+                const int cells = !(g->wall_x && i == g->nx - 2);
                 double rx = 0.0;
                 if (y3) rx += (Ez[IX(g, i, j + 1, k)] - Ez[c]) / g->dy;
                 if (z3) rx -= (Ey[IX(g, i, j, k + 1)] - Ey[c]) / g->dz;
@@ -133,14 +138,18 @@ void orc_yee_b_half(const orc_grid* g, const double* E, double* B) {
                 double rz = (Ey[IX(g, i + 1, j, k)] - Ey[c]) / g->dx;
                 if (y3) rz -= (Ex[IX(g, i, j + 1, k)] - Ex[c]) / g->dy;
                 Bx[c] = Bx[c] - rx * cdtd2;
-                By[c] = By[c] - ry * cdtd2;
-                Bz[c] = Bz[c] - rz * cdtd2;
+                if (cells) {
+                    By[c] = By[c] - ry * cdtd2;
+                    Bz[c] = Bz[c] - rz * cdtd2;
+                }
             }
 }
 
 /* tristanEvaluateE (fields.cpp:81-150), curls evaluateBunemanRotB{x,y,z}
- * (fields.cpp:3306-3337).  Periodic box: the conductor/Dirichlet edge
- * assignments do not apply. */
+ * (fields.cpp:3306-3337).  Conductor wall (wall_x): Ex on cells
+ * minI..maxI-1, Ey and Ez on nodes minI..maxI, zero on the wall node and
+ * E_right on the open boundary node (fields.cpp:116-121, 136-141); the
+ * ghost columns keep their values. */
 void orc_yee_e(const orc_grid* g, double* E, const double* B, const double* J) {
     const long N = NC(g);
     double* Ex = E; double* Ey = E + N; double* Ez = E + 2 * N;
@@ -158,10 +167,30 @@ void orc_yee_e(const orc_grid* g, double* E, const double* B, const double* J) {
                 if (z3) ry += (Bx[c] - Bx[IX(g, i, j, k - 1)]) / g->dz;
                 double rz = (By[c] - By[IX(g, i - 1, j, k)]) / g->dx;
                 if (y3) rz -= (Bx[c] - Bx[IX(g, i, j - 1, k)]) / g->dy;
-                Ex[c] = Ex[c] + (g->cfix * rx - FOUR_PI * Jx[c]) * g->dt;
+                if (g->wall_x && i == g->nx - 1) continue;
+                if (!(g->wall_x && i == g->nx - 2)) Ex[c] = Ex[c] + (g->cfix * rx - FOUR_PI * Jx[c]) * g->dt;
                 Ey[c] = Ey[c] + (g->cfix * ry - FOUR_PI * Jy[c]) * g->dt;
                 Ez[c] = Ez[c] + (g->cfix * rz - FOUR_PI * Jz[c]) * g->dt;
+                if (g->wall_x && i == 0) { Ey[c] = 0.0; Ez[c] = 0.0; }
+                if (g->wall_x && i == g->nx - 2) { Ey[c] = g->e_right[1]; Ez[c] = g->e_right[2]; }
             }
+}
+
+/* The ghost columns of a conductor-wall box as the reference's one-rank
+ * exchanges leave them (exchangeBuneman{E,B}field, fields_exchange.cpp
+ * 2537-2661 and the y, z, B counterparts, non-periodic branch): the column
+ * left of the wall (storage column nx - 1) holds zero in the cell-centred
+ * components Ex, By, Bz and the wall node's value in Ey, Ez, Bx; the column
+ * beyond the open boundary keeps whatever it held. */
+void orc_wall_yee_ghosts(const orc_grid* g, double* E, double* B) {
+    if (!g->wall_x) return;
+    const long N = NC(g);
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j) {
+            const long c = IX(g, g->nx - 1, j, k), w = IX(g, 0, j, k);
+            E[c] = 0.0; E[N + c] = E[N + w]; E[2 * N + c] = E[2 * N + w];
+            B[c] = B[w]; B[N + c] = 0.0; B[2 * N + c] = 0.0;
+        }
 }
 
 /* correlationBunemanEBfieldsWithoutMaps (correlation.cpp:441-600): E and B
@@ -188,12 +217,38 @@ static void yee_gather(const orc_grid* g, int cell, double ox, double oy, double
             }
 }
 
+/* The x move of moveParticleTristan next to a conductor wall
+ * (mover.cpp:744-772): x = x^n + v_x dt without a periodic wrap; a
+ * position left of the reflecting wall (node ORC_TRISTAN_WALL_NODE) is
+ * mirrored there (bit 1 of the result: p_x is to be reversed,
+ * reflectMomentumX); a position beyond the open boundary x = (nx - 2) dx
+ * sets bit 2 (escaped: the particle still deposits its current this step
+ * and is erased after it).  Cell and offset of the result in c, u. */
+static int tristan_wall_x(const orc_grid* g, int* c, double* u, double disp) {
+    const int W = ORC_TRISTAN_WALL_NODE;
+    const double s = *u + disp;
+    const double fl = floor(s);
+    int cn = *c + (int)fl;
+    double un = s - fl;
+    if (un >= 1.0) { un -= 1.0; cn += 1; }
+    int r = 0;
+    if (cn < W) {   /* x' = 2 W - x */
+        if (un > 0.0) { cn = 2 * W - cn - 1; un = 1.0 - un; }
+        else cn = 2 * W - cn;
+        r = 1;
+    }
+    if (cn > g->nx - 2 || (cn == g->nx - 2 && un > 0.0)) r |= 2;
+    *c = cn; *u = un;
+    return r;
+}
+
 /* moveParticleTristan (mover.cpp:718-742): Boris push, then x += v*dt.
  * Periodic wrap replaces exchangeParticles (mover.cpp:1002-1210).  Note the
  * reference's rotation factor f = 2/sqrt(1 + t^2) (mover.cpp:738), kept. */
 void orc_boris_push(const orc_grid* g, orc_particles* p, const double* E, const double* B) {
     const double beta = p->q * g->dt / (2.0 * p->m);  /* Particle::beta, particle.cpp:47 */
     for (long n = 0; n < p->n; ++n) {
+        if (p->cell[n] < 0) continue;   /* escaped (wall_x), erased after the step */
         double e[3], b[3];
         yee_gather(g, p->cell[n], p->ox[n], p->oy[n], p->oz[n], E, B, e, b);
         double s = p->q * g->dt * 0.5;
@@ -214,7 +269,11 @@ void orc_boris_push(const orc_grid* g, orc_particles* p, const double* E, const 
         double v[3]; velocity_of(mom, p->m, v);
         int i, j, k; decode(g, p->cell[n], &i, &j, &k);
         double ux = p->ox[n], uy = p->oy[n], uz = p->oz[n];
-        advance_axis(&ux, &i, (v[0] * g->dt) * (1.0 / g->dx), g->nx);
+        if (g->wall_x) {
+            if (tristan_wall_x(g, &i, &ux, (v[0] * g->dt) * (1.0 / g->dx)) & 1) p->px[n] = -p->px[n];
+        } else {
+            advance_axis(&ux, &i, (v[0] * g->dt) * (1.0 / g->dx), g->nx);
+        }
         advance_axis(&uy, &j, (v[1] * g->dt) * (1.0 / g->dy), g->ny);
         advance_axis(&uz, &k, (v[2] * g->dt) * (1.0 / g->dz), g->nz);
         p->ox[n] = ux; p->oy[n] = uy; p->oz[n] = uz;
@@ -226,9 +285,13 @@ void orc_boris_push(const orc_grid* g, orc_particles* p, const double* E, const 
  * the new position X (length units from the new cell's lower face), the
  * old position P = X - v*dt, the relay point R and the cell shift of the
  * first segment. */
-static inline void zig_axis(double X, double v, double dt, double d, int n,
+static inline void zig_axis(double X, double v, double dt, double d, int n, int mirror,
                             double* P, double* R, int* sh) {
     double prev = X - v * dt;
+    /* the particle's cell is the one right of the reflecting wall and it
+     * moves away from it: an old position left of the wall is mirrored
+     * (momentum_collecting.cpp:93-99) */
+    if (mirror && v > 0 && prev < 0) prev = -prev;
     if (n == 1) { *P = prev; *R = (X + prev) / 2; *sh = 0; return; }
     int s = (int)floor(prev / d);
     double r = (X + prev) / 2;
@@ -245,14 +308,15 @@ void orc_zigzag(const orc_grid* g, const orc_particles* p, double* J) {
     const double fcd = p->q * p->w / vol;
     const int y3 = g->ny > 1, z3 = g->nz > 1;
     for (long n = 0; n < p->n; ++n) {
+        if (p->cell[n] < 0) continue;
         double mom[3] = {p->px[n], p->py[n], p->pz[n]};
         double v[3]; velocity_of(mom, p->m, v);
         int i, j, k; decode(g, p->cell[n], &i, &j, &k);
         double X = p->ox[n] * g->dx, Y = p->oy[n] * g->dy, Z = p->oz[n] * g->dz;
         double PX, PY, PZ, RX, RY, RZ; int si, sj, sk;
-        zig_axis(X, v[0], g->dt, g->dx, g->nx, &PX, &RX, &si);
-        zig_axis(Y, v[1], g->dt, g->dy, g->ny, &PY, &RY, &sj);
-        zig_axis(Z, v[2], g->dt, g->dz, g->nz, &PZ, &RZ, &sk);
+        zig_axis(X, v[0], g->dt, g->dx, g->nx, g->wall_x && i == ORC_TRISTAN_WALL_NODE, &PX, &RX, &si);
+        zig_axis(Y, v[1], g->dt, g->dy, g->ny, 0, &PY, &RY, &sj);
+        zig_axis(Z, v[2], g->dt, g->dz, g->nz, 0, &PZ, &RZ, &sk);
         double Fx1 = fcd * (RX - PX) / g->dt;
         double Fy1 = fcd * (RY - PY) / g->dt;
         double Fz1 = fcd * (RZ - PZ) / g->dt;
@@ -333,6 +397,7 @@ void orc_smooth(const orc_grid* g, double* a, int ncomp) {
  * simulation.cpp:186-188), E step. */
 void orc_buneman_step(const orc_grid* g, orc_particles* sp, int nspecies,
                       double* E, double* B, double* J) {
+    orc_wall_yee_ghosts(g, E, B);
     orc_yee_b_half(g, E, B);
     for (int s = 0; s < nspecies; ++s) orc_boris_push(g, &sp[s], E, B);
     orc_yee_b_half(g, E, B);
@@ -340,6 +405,16 @@ void orc_buneman_step(const orc_grid* g, orc_particles* sp, int nspecies,
     for (int s = 0; s < nspecies; ++s) orc_zigzag(g, &sp[s], J);
     for (int q = 0; q < g->smoothing_count; ++q) orc_smooth(g, J, 3);
     orc_yee_e(g, E, B, J);
+    if (!g->wall_x) return;
+    /* particles beyond the open boundary were marked escaped by the mover
+     * and deposited their current; eraseEscapedPaticles (mover.cpp:167-192)
+     * drops them now (cell -1 here; the caller compacts the arrays) */
+    for (int s = 0; s < nspecies; ++s)
+        for (long n = 0; n < sp[s].n; ++n) {
+            if (sp[s].cell[n] < 0) continue;
+            int i, j, k; decode(g, sp[s].cell[n], &i, &j, &k);
+            if (i > g->nx - 2 || (i == g->nx - 2 && sp[s].ox[n] > 0.0)) sp[s].cell[n] = -1;
+        }
 }
 
 /* ================================================================== */

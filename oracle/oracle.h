@@ -45,7 +45,10 @@ typedef struct {
                                at x = (nx - 2) dx (SUPER_CONDUCTOR_LEFT, one
                                rank); storage columns nx - 2 and nx - 1 are the
                                ghost cells beyond the open boundary and left of
-                               the wall (implicit path, 3-D boxes)           */
+                               the wall (3-D boxes).  The explicit path
+                               reflects particles at node
+                               ORC_TRISTAN_WALL_NODE, the implicit path at
+                               the field wall x = 0                          */
     double e_right[3], b_right[3]; /* the open boundary's constant E and B
                                (ConstantBoundaryFieldEvaluator)              */
 } orc_grid;
@@ -68,6 +71,11 @@ void orc_smooth(const orc_grid* g, double* a, int ncomp);
 void orc_smooth_moments(const orc_grid* g, double* J, double* mu, double* rho_ext);
 
 /* ---- explicit Buneman / Tristan path ---- */
+/* The reflecting wall of the explicit path: xgrid[reflectingWallPoint]
+ * (constants.h:64, reflectingWallPoint = 20 in the reference's ghosted
+ * index, two ghost layers left of node 0 here). */
+#define ORC_TRISTAN_WALL_NODE 18
+void orc_wall_yee_ghosts(const orc_grid* g, double* E, double* B);
 void orc_yee_b_half(const orc_grid* g, const double* E, double* B);
 void orc_yee_e(const orc_grid* g, double* E, const double* B, const double* J);
 void orc_boris_push(const orc_grid* g, orc_particles* p, const double* E, const double* B);

@@ -64,6 +64,7 @@ def lib():
         L.orc_boris_push.argtypes = [g, p, _dp, _dp]
         L.orc_zigzag.argtypes = [g, p, _dp]
         L.orc_buneman_step.argtypes = [g, p, C.c_int, _dp, _dp, _dp]
+        L.orc_wall_yee_ghosts.argtypes = [g, _dp, _dp]
         L.orc_sort_key.argtypes = [g, C.c_int]
         L.orc_sort_key.restype = C.c_long
         L.orc_counting_sort.argtypes = [g, C.c_long, _ip, _lp]
@@ -138,6 +139,8 @@ def buneman_step(grid: Grid, species, E, B, J=None):
         J = np.zeros_like(E)
     arr = _plist(species)
     lib().orc_buneman_step(C.byref(grid), arr, len(species), _d(E), _d(B), _d(J))
+    if grid.wall_x:
+        erase_escaped(species)
     return J
 
 

@@ -13,12 +13,14 @@
 //   int32[10]  solver (0 Buneman, 1 implicit), nx, ny, nz, nspecies, steps,
 //              dump_first_step_moments, density_pass, smoothing_count, wall_x
 //   float64[11] dx, dt, theta, eta, smoothing_parameter, E_right[3], B_right[3]
-// wall_x = 1 (implicit runs): SUPER_CONDUCTOR_LEFT with a constant field
-// E_right, B_right at the open right boundary (initializeFluxFromRight,
-// initialization.cpp:5201-5207); the reference box then has nx - 2 cells
-// along x, the two remaining storage columns being its ghost cells beyond
-// the open boundary and left of the wall.  Particles that escape are
-// written back with NaN coordinates; no particles are injected.
+// wall_x = 1: SUPER_CONDUCTOR_LEFT with a constant field E_right, B_right
+// at the open right boundary (initializeFluxFromRight,
+// initialization.cpp:5201-5207; for Buneman runs E_right is Simulation::E0,
+// which tristanEvaluateE writes on the boundary node); the reference box
+// then has nx - 2 cells along x, the two remaining storage columns being
+// its ghost cells beyond the open boundary and left of the wall.  Particles
+// that escape are written back with NaN coordinates; no particles are
+// injected.
 //   per species: float64 q, m, w; int64 n; float64 x[n], y[n], z[n] (in
 //              [0, L) of the periodic box), px[n], py[n], pz[n]
 //   float64 E[3][nz][ny][nx], B[3][nz][ny][nx] on our periodic layout
@@ -67,7 +69,8 @@ int main(int argc, char** argv) {
     double eright[3], bright[3];
     for (int a = 0; a < 3; ++a) eright[a] = rd<double>(f);
     for (int a = 0; a < 3; ++a) bright[a] = rd<double>(f);
-    if (wall && (solver != 1 || nx < 4 || ny < 2 || nz < 2)) die("wall_x needs an implicit 3-D box");
+    // Buneman runs reflect at xgrid[reflectingWallPoint = 20] (constants.h:64)
+    if (wall && (nx < (solver == 0 ? 24 : 4) || ny < 2 || nz < 2)) die("wall_x needs a 3-D box (nx >= 24 for Buneman)");
     Box bx{nx, ny, nz};
     const long N = (long)nx * ny * nz;
 
@@ -108,6 +111,7 @@ int main(int argc, char** argv) {
     S->createArrays();
     Vector3d Er(eright[0], eright[1], eright[2]), Br(bright[0], bright[1], bright[2]);
     if (wall) S->rightBoundaryFieldEvaluator = new ConstantBoundaryFieldEvaluator(Er, Br);
+    if (wall && solver == 0) S->E0 = Er;
     // grid coordinates as Simulation::initialize builds them (initialization.cpp:1989-2023)
     S->xgrid[0] = S->leftX;
     for (int i = 1; i <= S->xnumberAdded; ++i) S->xgrid[i] = S->xgrid[0] + i * S->deltaX;

@@ -217,20 +217,28 @@ def wall_fields(nx, ny, nz, E0, B0):
     return E, B
 
 
+# The explicit (Tristan) mover reflects at xgrid[reflectingWallPoint]
+# (PIC++/mover.cpp:746-750, constants.h:64): node 18 of the wall box, and
+# createParticles fills the box from there (initialization.cpp:8152-8155).
+TRISTAN_WALL_NODE = 18
+
+
 def shock_plasma(nx, ny, nz, dx=0.5, dt=0.4, ppc=(32, 32, 8), flow_gamma=1.5, theta_e=1e-3, sigma=0.04,
-                 angle_deg=60.0, mass_ratio=64.0, he_mass=256.0, he_fraction=0.1, theta=0.5, seed=5) -> FlowState:
+                 angle_deg=60.0, mass_ratio=64.0, he_mass=256.0, he_fraction=0.1, theta=0.5, seed=5,
+                 first_cell=0) -> FlowState:
     """The reflecting-wall shock setup (shock_parameters) on a wall box of
-    nx x ny x nz storage cells: the flow fills the nx - 2 physical cells of
-    every x row."""
+    nx x ny x nz storage cells: the flow fills the physical cells
+    first_cell .. nx - 3 of every x row (first_cell = TRISTAN_WALL_NODE for
+    the explicit path, whose particles reflect there)."""
     box = Box(nx, ny, nz, dx, dx, dx, dt, theta=theta)
     rng = np.random.default_rng(seed)
     specs, E0, B0, v0 = shock_parameters(dx, ppc, flow_gamma, theta_e, sigma, angle_deg, mass_ratio, he_mass,
                                          he_fraction)
-    phys = Box(nx - 2, ny, nz, dx, dx, dx, dt, theta=theta)
+    phys = Box(nx - 2 - first_cell, ny, nz, dx, dx, dx, dt, theta=theta)
     species, temps = [], []
     for q, m, n, c, th in specs:
         sp = uniform_species(rng, phys, c, q, m, density_weight(box, n, c), th, flow_gamma, -1.0)
-        i = sp["cell"] % phys.nx
+        i = sp["cell"] % phys.nx + first_cell
         rest = sp["cell"] // phys.nx
         sp["cell"] = (rest * nx + i).astype(np.int32)   # physical cells in the storage layout
         species.append(sp)

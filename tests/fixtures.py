@@ -67,3 +67,12 @@ def survivors(out):
     """Indices of the particles a reference run kept (escaped ones come back
     as NaN)."""
     return np.nonzero(~np.isnan(np.asarray(out["x"])))[0]
+
+
+def yee_physical(a, box, field):
+    """The physical part of a staggered Yee field ("E" or "B") of a wall box,
+    as one flat array: x-cell-centred components (Ex; By, Bz) on cells
+    0 .. nx - 3, x-node components (Ey, Ez; Bx) on nodes 0 .. nx - 2."""
+    a = np.asarray(a).reshape(3, box.nz, box.ny, box.nx)
+    cells = (0,) if field == "E" else (1, 2)
+    return np.concatenate([a[c, ..., : box.nx - (2 if c in cells else 1)].ravel() for c in range(3)])

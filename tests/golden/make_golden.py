@@ -78,6 +78,24 @@ def wall(name, nx, ny, nz, ppc, steps, seed, flow_gamma=3.0, theta_e=0.3):
     _save(name, 1, st, steps, out_sp, E, B, extra)
 
 
+def tristan_wall(name, nx, ny, nz, ppc, steps, seed, flow_gamma=3.0, theta_e=0.3, dx=0.5, courant=0.45):
+    """The explicit path in a reflecting-wall box: the flow fills the cells
+    from the reflecting wall (node 18) to the open boundary and a third of
+    every species is turned towards the open boundary, so that particles
+    both reflect and escape; E_right's y, z components are Simulation::E0
+    on the boundary node."""
+    st = I.shock_plasma(nx, ny, nz, dx=dx, dt=courant * dx, ppc=ppc, flow_gamma=flow_gamma, theta_e=theta_e,
+                        seed=seed, first_cell=I.TRISTAN_WALL_NODE)
+    rng = np.random.default_rng(seed + 100)
+    for sp in st.species:
+        sp["px"][::3] = -sp["px"][::3]
+    st.E = st.E + 0.02 * rng.standard_normal(st.E.shape)
+    out_sp, E, B, extra = O.run_reference(0, st.box, st.species, st.E, st.B, steps, wall_x=1,
+                                          e_right=st.e_right, b_right=st.b_right)
+    extra["wall"] = np.concatenate([np.asarray(st.e_right), np.asarray(st.b_right)])
+    _save(name, 0, st, steps, out_sp, E, B, extra)
+
+
 def density(name, nx, ny, nz, ppc, seed):
     """updateDensityParameters of a seeded state, one species per reference
     run (the harness gives every particle reference type 0)."""
@@ -95,6 +113,14 @@ def density(name, nx, ny, nz, ppc, seed):
 def main():
     if not O.reference_available():
         sys.exit("the PIC++ reference tree is not available here (set PICPP_REFERENCE_SRC)")
+    only = sys.argv[1:]   # optional name prefixes: regenerate just those cases
+    if only:
+        global _save
+        full_save = _save
+
+        def _save(name, *a, **k):   # noqa: F811
+            if any(name.startswith(p) for p in only):
+                full_save(name, *a, **k)
     buneman("buneman_8x8x8_3steps", 8, 8, 8, 2, 3, 11)
     buneman("buneman_12x6x5_2steps", 12, 6, 5, 3, 2, 12)
     buneman("buneman_2d_16x8x1_3steps", 16, 8, 1, 4, 3, 13)
@@ -105,6 +131,8 @@ def main():
     buneman("buneman_smooth_2d_12x8x1_2steps", 12, 8, 1, 3, 2, 15, smoothing=(1, 0.5))
     wall("wall_7x4x4_4steps", 7, 4, 4, (4, 4, 2), 4, 41)
     wall("wall_10x6x5_2steps", 10, 6, 5, (3, 3, 2), 2, 42)
+    tristan_wall("tristan_wall_26x4x4_4steps", 26, 4, 4, (3, 3, 2), 4, 51)
+    tristan_wall("tristan_wall_32x6x5_3steps", 32, 6, 5, (4, 3, 2), 3, 52)
     density("density_8x6x5", 8, 6, 5, 3, 31)
     density("density_2d_8x8x1", 8, 8, 1, 4, 32)
 

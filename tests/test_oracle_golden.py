@@ -4,7 +4,8 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of, survivors, wall_of
+from fixtures import (copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of, survivors, wall_of,
+                      yee_physical)
 from picpp_gb300 import initstate as I
 
 # The oracle keeps cell + offset where the reference keeps absolute FP64
@@ -174,3 +175,37 @@ def test_wall_steps_match_reference(name):
         for k in ("px", "py", "pz"):
             assert rel_err(s[k], o[k][keep]) < TOL
     assert escaped > 0
+
+
+@pytest.mark.parametrize("name", golden_names("tristan_wall"))
+def test_tristan_wall_matches_reference(name):
+    """The explicit path in a reflecting-wall box against the reference's
+    own SUPER_CONDUCTOR_LEFT Buneman runs: reflection at node 18 (the
+    zigzag current of a reflected particle mirrored there), E_y = E_z = 0 on
+    the wall node and E0 on the open boundary node, escape and erase."""
+    f = load(name)
+    st = f["state"]
+    w, er, br = wall_of(f)
+    g = O.make_grid(st.box, wall_x=w, e_right=er, b_right=br)
+    sp = copy_species(st.species)
+    for s in sp:
+        s["id"] = np.arange(len(s["cell"]))
+    E, B = st.E.copy(), st.B.copy()
+    for _ in range(f["steps"]):
+        J = O.buneman_step(g, sp, E, B)
+    b = st.box
+    assert rel_err(yee_physical(E, b, "E"), yee_physical(f["E"], b, "E")) < TOL
+    assert rel_err(yee_physical(B, b, "B"), yee_physical(f["B"], b, "B")) < TOL
+    assert rel_err(J, f["extra"]["J"]) < TOL
+    escaped = reflected = 0
+    for s, s0, o in zip(sp, st.species, f["out"]):
+        keep = survivors(o)
+        escaped += len(o["x"]) - len(keep)
+        reflected += int(np.sum(np.sign(s["px"]) != np.sign(s0["px"][keep])))
+        assert np.array_equal(s["id"], keep)
+        x, y, z = I.positions(b, s)
+        assert np.abs(x - o["x"][keep]).max() < 1e-12
+        assert x.min() >= I.TRISTAN_WALL_NODE * b.dx
+        for k in ("px", "py", "pz"):
+            assert rel_err(s[k], o[k][keep]) < TOL
+    assert escaped > 0 and reflected > 0

@@ -75,18 +75,26 @@ typedef struct {
 } pic_config;
 
 /* Boundary along x.  PIC_BOUNDARY_WALL_OPEN is boundaryConditionTypeX =
- * SUPER_CONDUCTOR_LEFT of one rank (implicit runs of 3-D boxes, no
- * smoothing): a conductor wall at x = 0 and an open
- * boundary at x = (nx - 2) dx.  The physical domain is nodes 0 .. nx - 2 and
- * cells 0 .. nx - 3 of the nx-cell storage; storage cell nx - 2 is the ghost
- * cell beyond the open boundary (boundary field), cell nx - 1 the ghost cell
- * left of the wall (the first cell's field), node nx - 1 the ghost node
- * beyond the open boundary.  Particles may not be placed in the two ghost
- * columns.  The mover reflects particles at the wall (mover.cpp:247-260,
- * 312-330, 435-445) and erases those that cross the open boundary
- * (mover.cpp:447-458, eraseEscapedPaticles mover.cpp:167-192); particles
- * are fed in with pic_append_particles (injectNewParticles,
- * mover.cpp:910-1000, with the caller's particles). */
+ * SUPER_CONDUCTOR_LEFT of one rank (3-D boxes, no smoothing): a conductor
+ * wall at x = 0 and an open boundary at x = (nx - 2) dx.  The physical
+ * domain is nodes 0 .. nx - 2 and cells 0 .. nx - 3 of the nx-cell storage;
+ * storage column nx - 2 holds the ghost cell beyond the open boundary,
+ * column nx - 1 the ghost cell left of the wall and the ghost node beyond
+ * the open boundary.  Particles may not be placed in the two ghost columns.
+ *   Implicit runs: the boundary field E_right, B_right in the ghost cells
+ * and boundary rows (fields.cpp:690-781, 2738-2756); the mover reflects
+ * particles at the wall x = 0 (mover.cpp:247-260, 312-330, 435-445).
+ *   Explicit runs (nx >= 24): E_y = E_z = 0 on the wall node and E_right's
+ * y, z components (Simulation::E0) on the open boundary node
+ * (fields.cpp:116-121, 136-141), the ghost column left of the wall as the
+ * reference's exchanges set it; the mover reflects particles at node 18
+ * (xgrid[reflectingWallPoint], mover.cpp:744-772) and the zigzag current
+ * mirrors the old position there (momentum_collecting.cpp:93-99).
+ * Both erase the particles that cross the open boundary after they
+ * deposited their current (mover.cpp:447-458, 760-770,
+ * eraseEscapedPaticles mover.cpp:167-192); particles are fed in with
+ * pic_append_particles (injectNewParticles, mover.cpp:910-1000, with the
+ * caller's particles). */
 typedef enum { PIC_BOUNDARY_PERIODIC = 0, PIC_BOUNDARY_WALL_OPEN = 1 } pic_boundary_x;
 
 /* Field-solve options for the implicit Maxwell system. */
@@ -149,7 +157,9 @@ pic_status pic_append_particles(pic_ctx* ctx, int species, long n, const int* ce
                                 const double* px, const double* py, const double* pz,
                                 const int* ids);
 /* Fills a species on the device with ppc particles per cell (the physical
- * cells of a wall box): uniform in-cell offsets, Maxwell-Juttner momenta of
+ * cells of a wall box, from the reflecting wall at node 18 on in explicit
+ * runs, as createParticles does, initialization.cpp:8152-8155): uniform
+ * in-cell offsets, Maxwell-Juttner momenta of
  * temperature theta (kT/mc^2), boosted along x with Lorentz factor
  * drift_gamma (> 1) -- towards +x with alternate_drift 0, every other
  * particle towards -x with 1, all towards -x with -1.  Seeded and

@@ -325,9 +325,10 @@ pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
             Phase ph(ctx, PIC_PHASE_FIELDS, 2 * ctx->cfg.smoothing_count + 1);
             pic_status st = smooth_current(ctx);
             if (st != PIC_OK) return st;
-            PK<T>::yee_e(s, g, ctx->E, ctx->B, ctx->J);
+            PK<T>::yee_e(s, g, ctx->E, ctx->B, ctx->J, ctx->e_right);
         }
         CKL(ctx, "buneman step");
+        if (g.wall) ctx->pending_compact = true;   // escaped particles (cell -1) until the next sort
         ctx->step++;
     }
     return PIC_OK;
@@ -478,12 +479,13 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     // the reference smooths J-hat and rho-hat including its own ghost values,
     // which only the periodic pressure placement represents as periodic images
     if (c.smoothing_count > 0 && c.solver == PIC_SOLVER_IMPLICIT && c.pressure_compat) return PIC_ERR_ARG;
-    // conductor wall / open boundary along x: implicit runs of 3-D boxes, no
-    // smoothing (the reference's own 2-D boundary rows are all fake,
-    // fields.cpp:528-530)
+    // conductor wall / open boundary along x: 3-D boxes, no smoothing (the
+    // reference's own 2-D boundary rows are all fake, fields.cpp:528-530);
+    // explicit runs reflect at node kTristanWallNode, so their box reaches
+    // at least four cells beyond it
     if (c.boundary_x != PIC_BOUNDARY_PERIODIC &&
-        (c.boundary_x != PIC_BOUNDARY_WALL_OPEN || c.solver != PIC_SOLVER_IMPLICIT || c.smoothing_count > 0 ||
-         c.nx < 4 || c.ny < 2 || c.nz < 2))
+        (c.boundary_x != PIC_BOUNDARY_WALL_OPEN || c.smoothing_count > 0 || c.ny < 2 || c.nz < 2 ||
+         c.nx < (c.solver == PIC_SOLVER_BUNEMAN ? kTristanWallNode + 6 : 4)))
         return PIC_ERR_ARG;
     long long N = (long long)c.nx * c.ny * c.nz;
     if (N >= (1LL << 31)) return PIC_ERR_ARG;
@@ -731,8 +733,11 @@ pic_status pic_fill_species(pic_ctx* ctx, int sid, int ppc, unsigned long long s
     if (pic_status st = check_species(ctx, sid)) return st;
     Species& sp = ctx->sp[sid];
     if (ppc < 0 || !(theta >= 0) || !(drift_gamma >= 1.0)) return fail(ctx, PIC_ERR_ARG, "bad fill parameters");
-    // a wall box leaves its two ghost columns empty
-    const int rowx = ctx->g.wall ? ctx->g.nx - 2 : ctx->g.nx;
+    // a wall box leaves its two ghost columns empty; the explicit path fills
+    // from its reflecting wall on (createParticles, initialization.cpp
+    // 8152-8155)
+    const int x0 = ctx->g.wall && is_buneman(ctx) ? kTristanWallNode : 0;
+    const int rowx = ctx->g.wall ? ctx->g.nx - 2 - x0 : ctx->g.nx;
     const long long n = (long long)ppc * (ctx->g.N / ctx->g.nx) * rowx;
     if (n > sp.cap) return fail(ctx, PIC_ERR_NOMEM, "particle count exceeds species capacity");
     const int ntab = 4096;
@@ -747,9 +752,9 @@ pic_status pic_fill_species(pic_ctx* ctx, int sid, int ppc, unsigned long long s
     sp.n = n;
     const unsigned long long sseed = seed * 0x100000001B3ull + (unsigned long long)sid * 0x9E3779B97F4A7C15ull;
     if (ctx->preal) launch_fill<double>(ctx->s, view<double>(sp), ppc, sseed, du, dc, theta > 0 ? ntab : 0, sp.m,
-                                        drift_gamma, alternate_drift, rowx, ctx->g.nx);
+                                        drift_gamma, alternate_drift, rowx, ctx->g.nx, x0);
     else launch_fill<float>(ctx->s, view<float>(sp), ppc, sseed, du, dc, theta > 0 ? ntab : 0, sp.m, drift_gamma,
-                            alternate_drift, rowx, ctx->g.nx);
+                            alternate_drift, rowx, ctx->g.nx, x0);
     CKL(ctx, "fill species");
     sp.next_id = n;
     sp.sorted = false;
@@ -860,6 +865,9 @@ pic_status pic_move_particles(pic_ctx* ctx) {
             else PK<float>::boris_push(ctx->s, ctx->g, view<float>(sp), sp.q, sp.m, ctx->E, ctx->B);
             sp.sorted = false;
         }
+        // escaped particles deposit their current (pic_tristan_update_flux),
+        // which marks them; the next sort erases them
+        if (ctx->g.wall) ctx->pending_compact = true;
         return sync(ctx, "move particles");
     }
     if (!ctx->efield_ready) return fail(ctx, PIC_ERR_STATE, "evaluate the electric field first");
@@ -885,8 +893,8 @@ pic_status pic_tristan_update_flux(pic_ctx* ctx) {
 pic_status pic_tristan_evaluate_e(pic_ctx* ctx) {
     if (!ctx) return PIC_ERR_ARG;
     if (!is_buneman(ctx)) return fail(ctx, PIC_ERR_STATE, "not a Buneman run");
-    if (ctx->preal) PK<double>::yee_e(ctx->s, ctx->g, ctx->E, ctx->B, ctx->J);
-    else PK<float>::yee_e(ctx->s, ctx->g, ctx->E, ctx->B, ctx->J);
+    if (ctx->preal) PK<double>::yee_e(ctx->s, ctx->g, ctx->E, ctx->B, ctx->J, ctx->e_right);
+    else PK<float>::yee_e(ctx->s, ctx->g, ctx->E, ctx->B, ctx->J, ctx->e_right);
     return sync(ctx, "evaluate E");
 }
 

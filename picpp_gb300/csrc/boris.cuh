@@ -9,6 +9,7 @@
 //     whole-step path.
 #pragma once
 #include "common.cuh"
+#include "wall_particles.cuh"
 
 namespace pic {
 
@@ -121,6 +122,7 @@ __global__ void __launch_bounds__(256) k_boris_push(GridP g, PartView<TP> p, TP 
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n;
          n += (long long)gridDim.x * blockDim.x) {
         int cell = p.cell[n];
+        if (cell < 0) continue;   // escaped through the open boundary, erased by the next sort
         TP ox = p.ox[n], oy = p.oy[n], oz = p.oz[n];
         TP e[3], b[3];
         yee_gather<TP, TF>(g, cell, ox, oy, oz, E, B, e, b);
@@ -131,7 +133,13 @@ __global__ void __launch_bounds__(256) k_boris_push(GridP g, PartView<TP> p, TP 
         velocity<TP>(mom, m, v);
         int i, j, k;
         decode(g, cell, i, j, k);
-        advance_axis<TP>(ox, i, (v[0] * dt) * idx, g.nx);
+        if (g.wall) {
+            // the escaped particle keeps its position beyond the open
+            // boundary: k_zigzag deposits its current, then marks it
+            if (tristan_wall_x<TP>(g, i, ox, (v[0] * dt) * idx) & 1) p.px[n] = -mom[0];
+        } else {
+            advance_axis<TP>(ox, i, (v[0] * dt) * idx, g.nx);
+        }
         advance_axis<TP>(oy, j, (v[1] * dt) * idy, g.ny);
         advance_axis<TP>(oz, k, (v[2] * dt) * idz, g.nz);
         p.ox[n] = ox; p.oy[n] = oy; p.oz[n] = oz;
@@ -142,8 +150,12 @@ __global__ void __launch_bounds__(256) k_boris_push(GridP g, PartView<TP> p, TP 
 // One axis of the zigzag split (PIC++/momentum_collecting.cpp:91-96,
 // 200-221): old position P = X - v dt, relay point R, first-segment shift.
 template <typename TP>
-__device__ __forceinline__ void zig_axis(TP X, TP v, TP dt, TP d, TP invd, int n, TP& P, TP& R, int& sh) {
+__device__ __forceinline__ void zig_axis(TP X, TP v, TP dt, TP d, TP invd, int n, TP& P, TP& R, int& sh,
+                                         bool mirror = false) {
     TP prev = X - v * dt;
+    // in the cell right of the reflecting wall, moving away from it: an old
+    // position left of the wall is mirrored (momentum_collecting.cpp:93-99)
+    if (mirror && v > TP(0) && prev < TP(0)) prev = -prev;
     TP r = (X + prev) / TP(2);
     if (n == 1) { P = prev; R = r; sh = 0; return; }
     int s = (int)dev_floor(divd<TP>(prev, d, invd));
@@ -156,13 +168,13 @@ __device__ __forceinline__ void zig_axis(TP X, TP v, TP dt, TP d, TP invd, int n
 // sink(component, di, dj, dk, value) with offsets relative to the new cell.
 template <typename TP, typename Sink>
 __device__ __forceinline__ void zigzag_terms(const GridP& g, TP fcd, TP ox, TP oy, TP oz,
-                                             const TP v[3], Sink&& sink) {
+                                             const TP v[3], Sink&& sink, bool wall_cell = false) {
     const TP dt = TP(g.dt), dx = TP(g.dx), dy = TP(g.dy), dz = TP(g.dz);
     const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
     TP X = ox * dx, Y = oy * dy, Z = oz * dz;
     TP PX, PY, PZ, RX, RY, RZ;
     int si, sj, sk;
-    zig_axis<TP>(X, v[0], dt, dx, idx, g.nx, PX, RX, si);
+    zig_axis<TP>(X, v[0], dt, dx, idx, g.nx, PX, RX, si, wall_cell);
     zig_axis<TP>(Y, v[1], dt, dy, idy, g.ny, PY, RY, sj);
     zig_axis<TP>(Z, v[2], dt, dz, idz, g.nz, PZ, RZ, sk);
     TP Fx1 = divd<TP>(fcd * (RX - PX), dt, TP(1.0 / g.dt));
@@ -215,15 +227,21 @@ __global__ void __launch_bounds__(256) k_zigzag(GridP g, PartView<TP> p, TP q, T
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n;
          n += (long long)gridDim.x * blockDim.x) {
         int cell = p.cell[n];
+        if (cell < 0) continue;
         TP mom[3] = {p.px[n], p.py[n], p.pz[n]};
         TP v[3];
         velocity<TP>(mom, m, v);
         int i, j, k;
         decode(g, cell, i, j, k);
-        zigzag_terms<TP>(g, fcd, p.ox[n], p.oy[n], p.oz[n], v,
+        const TP ox = p.ox[n];
+        zigzag_terms<TP>(g, fcd, ox, p.oy[n], p.oz[n], v,
                          [&](int comp, int di, int dj, int dk, TP val) {
                              atomicAdd(&J[comp * g.N + linw(g, i + di, j + dj, k + dk)], double(val));
-                         });
+                         },
+                         g.wall && i == kTristanWallNode);
+        // eraseEscapedPaticles (mover.cpp:167-192) after the deposit: the
+        // next sort drops the particle
+        if (g.wall && tristan_escaped<TP>(g, i, ox)) p.cell[n] = -1;
     }
 }
 

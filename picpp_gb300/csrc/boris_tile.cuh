@@ -73,7 +73,7 @@ __device__ __noinline__ void deposit_global(const GridP& g, TP fcd, TP ox, TP oy
     const TP v[3] = {vx, vy, vz};
     zigzag_terms<TP>(g, fcd, ox, oy, oz, v, [&](int comp, int di, int dj, int dk, TP val) {
         atomicAdd(&Jfix[comp * g.N + linw(g, ni + di, nj + dj, nk + dk)], double(val));
-    });
+    }, g.wall && ni == kTristanWallNode);
 }
 
 // One zigzag segment's 12 terms relative to its cell
@@ -174,8 +174,11 @@ __device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __r
 }
 
 // CT: compile-time tile extent of a cubic 3-D tile (8), or 0 for shapes read
-// from TileShape at run time.
-template <typename TP, typename TF, int CT>
+// from TileShape at run time.  kWall: conductor-wall box (GridP::wall), the
+// Tristan mover's reflection and escape and the zigzag wall term
+// (mover.cpp:744-772, momentum_collecting.cpp:93-99); a particle that
+// escaped deposits its current and is marked (cell -1) for the next sort.
+template <typename TP, typename TF, int CT, bool kWall>
 __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
                                                                        const TF* __restrict__ E, const TF* __restrict__ B,
                                                                        double* __restrict__ Jpart, double* __restrict__ Jfix,
@@ -233,8 +236,9 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                 TP aB[12];
                 TP s1[6] = {TP(0), TP(0), TP(0), TP(0), TP(0), TP(0)};   // F1 and W1 of the old-side segment
                 int keyA = -1 - lane, keyB = -1 - lane;   // lanes outside a reduction keep unique keys
-                if (n < pe) {
-                    const int cell = P.cell[n];
+                const int cell = n < pe ? P.cell[n] : -1;
+                // (an escaped particle of a wall box waits with cell -1 for the sort)
+                if (n < pe && (!kWall || cell >= 0)) {
                     TP ox = P.ox[n], oy = P.oy[n], oz = P.oz[n];
                     TP mom[3] = {P.px[n], P.py[n], P.pz[n]};
                     int i, j, k;
@@ -275,26 +279,40 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                     TP v[3];
                     velocity_t<TP>(mom, m, v);
                     int ni = i, nj = j, nk = k;
-                    advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
+                    int wall_r = 0;
+                    if constexpr (kWall) {
+                        wall_r = tristan_wall_x<TP>(g, ni, ox, (v[0] * dt) * idx);
+                        if (wall_r & 1) { mom[0] = -mom[0]; v[0] = -v[0]; }   // reflectMomentumX
+                    } else {
+                        advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
+                    }
                     advance_axis<TP>(oy, nj, (v[1] * dt) * idy, g.ny);
                     advance_axis<TP>(oz, nk, (v[2] * dt) * idz, g.nz);
                     P.px[n] = mom[0]; P.py[n] = mom[1]; P.pz[n] = mom[2];
                     P.ox[n] = ox; P.oy[n] = oy; P.oz[n] = oz;
-                    P.cell[n] = (int)lin(g, ni, nj, nk);
+                    P.cell[n] = (wall_r & 2) ? -1 : (int)lin(g, ni, nj, nk);
                     auto shift = [](int nw, int old, int nn) {
                         int d = nw - old;
                         if (d > 1) d -= nn;
                         if (d < -1) d += nn;
                         return d;
                     };
-                    // block cell of the new position
-                    const int bx = li + shift(ni, i, g.nx) + hx;
+                    // block cell of the new position (a wall box has no x
+                    // wrap; a particle reflected from left of the wall may
+                    // land far from its old cell and takes the global path)
+                    const int sxw = kWall ? ni - i : shift(ni, i, g.nx);
+                    const bool nearx = !kWall || (sxw >= -1 && sxw <= 1);
+                    const int bx = li + sxw + hx;
                     const int by = (ey ? lj + shift(nj, j, g.ny) : 0) + hy;
                     const int bz = (ez ? lk + shift(nk, k, g.nz) : 0) + hz;
                     // zigzag split (zig_axis, momentum_collecting.cpp:91-221) in the
                     // new cell's frame: old position P, relay R, relay shift r
                     const TP X = ox * dx, Y = oy * dy, Z = oz * dz;
-                    const TP PX = X - v[0] * dt, PY = Y - v[1] * dt, PZ = Z - v[2] * dt;
+                    TP PX = X - v[0] * dt;
+                    const TP PY = Y - v[1] * dt, PZ = Z - v[2] * dt;
+                    if constexpr (kWall) {
+                        if (ni == kTristanWallNode && v[0] > TP(0) && PX < TP(0)) PX = -PX;
+                    }
                     const int rx = (int)dev_floor(divd<TP>(PX, dx, idx));
                     const int ry = ey ? (int)dev_floor(divd<TP>(PY, dy, idy)) : 0;
                     const int rz = ez ? (int)dev_floor(divd<TP>(PZ, dz, idz)) : 0;
@@ -303,7 +321,7 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                     const TP RZ = rz == 0 ? (Z + PZ) / TP(2) : TP(rz > 0 ? rz : 0) * dz;
                     const int ax = bx + rx, ay = by + ry, az = bz + rz;   // block cell of the old-side segment
                     // unsigned compares: (unsigned)x < n is 0 <= x < n
-                    const bool inblock = fast && (unsigned)(rx + 1) <= 2u && (unsigned)(ry + 1) <= 2u &&
+                    const bool inblock = fast && nearx && (unsigned)(rx + 1) <= 2u && (unsigned)(ry + 1) <= 2u &&
                                          (unsigned)(rz + 1) <= 2u && (unsigned)ax < (unsigned)(jx - 1) &&
                                          (unsigned)bx < (unsigned)(jx - 1) && (unsigned)ay < (unsigned)(jy - ey) &&
                                          (unsigned)by < (unsigned)(jy - ey) && (unsigned)az < (unsigned)(jz - ez) &&

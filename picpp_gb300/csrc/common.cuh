@@ -31,6 +31,12 @@ struct GridP {
     int y3, z3;           // ny > 1, nz > 1
     FastDiv divx, divy;   // by nx, by ny
 };
+// The explicit (Tristan) mover of a wall box reflects at
+// xgrid[reflectingWallPoint] (mover.cpp:746-750; reflectingWallPoint = 20
+// in the reference's ghosted index, constants.h:64): node 18 here, two
+// ghost layers left of node 0.
+constexpr int kTristanWallNode = 18;
+
 // 128 bytes: the size up to which the out-of-line gathers take it in
 // registers (a larger struct goes through a stack frame)
 static_assert(sizeof(GridP) == 128, "GridP layout");

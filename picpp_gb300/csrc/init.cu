@@ -32,16 +32,17 @@ __device__ __forceinline__ double urand(unsigned long long seed, long long p, in
     return (double)(h >> 11) * (1.0 / 9007199254740992.0);   // [0, 1)
 }
 
-// rowx: cells per x row that receive particles (nx, or nx - 2 in a wall box
-// whose two ghost columns stay empty); nx: the storage row length.
+// rowx: cells per x row that receive particles, from cell x0 on (nx from
+// 0, or fewer in a wall box whose two ghost columns stay empty); nx: the
+// storage row length.
 template <typename T>
 __global__ void k_fill(pic::PartView<T> p, long long ppc, unsigned long long seed, const double* __restrict__ cdf_u,
                        const double* __restrict__ cdf, int ntab, double mass, double drift_gamma, int alternate,
-                       int rowx, int nx) {
+                       int rowx, int nx, int x0) {
     const double beta = drift_gamma > 1.0 ? sqrt(1.0 - 1.0 / (drift_gamma * drift_gamma)) : 0.0;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n; n += (long long)gridDim.x * blockDim.x) {
         const long long q = n / ppc;   // the q-th filled cell
-        p.cell[n] = (int)((q / rowx) * nx + q % rowx);
+        p.cell[n] = (int)((q / rowx) * nx + x0 + q % rowx);
         p.id[n] = (int)n;
         double o[3];
         for (int a = 0; a < 3; ++a) {
@@ -103,12 +104,12 @@ std::vector<double> juttner_table(double theta, int n, std::vector<double>& us) 
 
 template <typename T>
 void launch_fill(cudaStream_t s, PartView<T> p, long long ppc, unsigned long long seed, const double* u, const double* c,
-                 int ntab, double mass, double drift_gamma, int alternate, int rowx, int nx) {
-    k_fill<T><<<grid_for(p.n, 256, 32), 256, 0, s>>>(p, ppc, seed, u, c, ntab, mass, drift_gamma, alternate, rowx, nx);
+                 int ntab, double mass, double drift_gamma, int alternate, int rowx, int nx, int x0) {
+    k_fill<T><<<grid_for(p.n, 256, 32), 256, 0, s>>>(p, ppc, seed, u, c, ntab, mass, drift_gamma, alternate, rowx, nx, x0);
 }
 template void launch_fill<float>(cudaStream_t, PartView<float>, long long, unsigned long long, const double*,
-                                 const double*, int, double, double, int, int, int);
+                                 const double*, int, double, double, int, int, int, int);
 template void launch_fill<double>(cudaStream_t, PartView<double>, long long, unsigned long long, const double*,
-                                  const double*, int, double, double, int, int, int);
+                                  const double*, int, double, double, int, int, int, int);
 
 }  // namespace pic

@@ -30,8 +30,10 @@ inline int red_blocks(long long n) {
 
 template <typename T>
 struct PK {
-    static void yee_b_half(cudaStream_t s, const GridP& g, const void* E, void* B);
-    static void yee_e(cudaStream_t s, const GridP& g, void* E, const void* B, const double* J);
+    // with GridP::wall the B half step first sets the ghost column left of
+    // the wall, and the E step writes er[1], er[2] on the open boundary node
+    static void yee_b_half(cudaStream_t s, const GridP& g, void* E, void* B);
+    static void yee_e(cudaStream_t s, const GridP& g, void* E, const void* B, const double* J, const double er[3]);
     static void boris_push(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, const void* E,
                            const void* B);
     static void zigzag(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w, double* J);
@@ -76,7 +78,7 @@ struct PK {
 std::vector<double> juttner_table(double theta, int n, std::vector<double>& us);
 template <typename T>
 void launch_fill(cudaStream_t s, PartView<T> p, long long ppc, unsigned long long seed, const double* u, const double* c,
-                 int ntab, double mass, double drift_gamma, int alternate, int rowx, int nx);
+                 int ntab, double mass, double drift_gamma, int alternate, int rowx, int nx, int x0);
 
 // grid.cu
 void launch_keys_hist(cudaStream_t s, const GridP& g, const TileGeom& t, const int* cell, long long n, int* key,

@@ -150,16 +150,17 @@ void PK<T>::iota(cudaStream_t s, int* a, long long n, long long start) {
 }
 
 template <typename T>
-void PK<T>::yee_b_half(cudaStream_t s, const GridP& g, const void* E, void* B) {
+void PK<T>::yee_b_half(cudaStream_t s, const GridP& g, void* E, void* B) {
     const T cdtd2 = T(g.cfix * g.dt / 2.0);
+    if (g.wall) k_wall_yee_ghosts<T><<<grid_for((long long)g.ny * g.nz, 128), 128, 0, s>>>(g, (T*)E, (T*)B);
     k_yee_b_half<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, (const T*)E, (T*)B, cdtd2, T(g.dx), T(g.dy), T(g.dz),
                                                       T(g.idx), T(g.idy), T(g.idz));
 }
 
 template <typename T>
-void PK<T>::yee_e(cudaStream_t s, const GridP& g, void* E, const void* B, const double* J) {
+void PK<T>::yee_e(cudaStream_t s, const GridP& g, void* E, const void* B, const double* J, const double er[3]) {
     k_yee_e<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, (T*)E, (const T*)B, J, T(g.cfix), T(g.dt), T(g.dx), T(g.dy),
-                                                 T(g.dz), T(g.idx), T(g.idy), T(g.idz));
+                                                 T(g.dz), T(g.idx), T(g.idy), T(g.idz), T(er[1]), T(er[2]));
 }
 
 template <typename T>
@@ -187,8 +188,9 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
                                int grid, size_t smem) {
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_push_deposit_tile<T, T, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     const bool cube8 = t.tx == 8 && t.ty == 8 && t.tz == 8 && g.y3 && g.z3 && sh.fx == 12 && sh.fy == 12 &&
@@ -201,12 +203,16 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
     for (int q = 0; q < S.ns; ++q)
         fmax = std::max(fmax, std::fabs((double)S.q[q] * (double)S.w[q] / (g.dx * g.dy * g.dz)));
     const float fx_scale = fmax > 0 ? (float)std::ldexp(1.0, 35 - (int)std::ceil(std::log2(fmax))) : 1.0f;
-    if (cube8)
-        k_push_deposit_tile<T, T, 8><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix,
-                                                                     fx_scale);
+    // a wall box runs its own instantiation (run-time tile shape)
+    if (g.wall)
+        k_push_deposit_tile<T, T, 0, true><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
+                                                                           Jfix, fx_scale);
+    else if (cube8)
+        k_push_deposit_tile<T, T, 8, false><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
+                                                                            Jfix, fx_scale);
     else
-        k_push_deposit_tile<T, T, 0><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart, Jfix,
-                                                                     fx_scale);
+        k_push_deposit_tile<T, T, 0, false><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
+                                                                            Jfix, fx_scale);
 }
 
 template <typename T>

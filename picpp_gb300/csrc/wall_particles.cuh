@@ -75,4 +75,39 @@ __device__ __forceinline__ int wall_final_x(const GridP& g, int& c, T& u, T disp
     return 0;
 }
 
+// The x move of moveParticleTristan in a wall box (mover.cpp:744-772),
+// reflecting at node kTristanWallNode:
+// x^{n+1} = x^n + disp (disp in cells) without a periodic wrap; a position
+// left of the reflecting wall is mirrored there (bit 1 of the result: p_x
+// is to be reversed, reflectMomentumX); a position beyond the open boundary
+// x = (nx - 2) dx sets bit 2 (escaped: the particle deposits its current
+// this step, then leaves).  c, u: cell and offset of x^n on entry, of the
+// result on return.
+template <typename T>
+__device__ __forceinline__ int tristan_wall_x(const GridP& g, int& c, T& u, T disp) {
+    const int W = kTristanWallNode;
+    const T s = u + disp;
+    const T fl = dev_floor(s);
+    int cn = c + (int)fl;
+    T un = s - fl;
+    if (un >= T(1)) { un -= T(1); cn += 1; }
+    int r = 0;
+    if (cn < W) {   // x' = 2 W - x
+        if (un > T(0)) { cn = 2 * W - cn - 1; un = T(1) - un; }
+        else cn = 2 * W - cn;
+        r = 1;
+    }
+    if (cn > g.nx - 2 || (cn == g.nx - 2 && un > T(0))) r |= 2;
+    c = cn;
+    u = un;
+    return r;
+}
+
+// True for a particle that left a wall box through the open boundary: its
+// position lies beyond x = (nx - 2) dx (the ghost column).
+template <typename T>
+__device__ __forceinline__ bool tristan_escaped(const GridP& g, int i, T u) {
+    return i > g.nx - 2 || (i == g.nx - 2 && u > T(0));
+}
+
 }  // namespace pic

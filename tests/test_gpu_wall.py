@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from fixtures import copy_species, golden_names, load, rel_err, survivors, wall_of
+from fixtures import copy_species, golden_names, load, rel_err, survivors, wall_of, yee_physical
 from picpp_gb300 import initstate as I
 
 pytestmark = pytest.mark.gpu
@@ -168,8 +168,115 @@ def test_wall_rejects_particles_in_ghost_columns_and_other_setups(pg):
     with pytest.raises(pg.PicError):
         sim.upload_particles(sid, bad)
     sim.close()
-    with pytest.raises(pg.PicError):   # explicit runs have no wall
+    with pytest.raises(pg.PicError):   # explicit wall boxes reach 4 cells beyond the reflecting wall (nx >= 24)
         pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=1, boundary_x=pg.BOUNDARY_WALL_OPEN)
     flat = I.Box(12, 8, 1, 0.5, 0.5, 0.5, 0.4)
     with pytest.raises(pg.PicError):   # 3-D boxes only
         pg.GpuSimulation(flat, pg.IMPLICIT, particle_real=1, pressure_compat=0, boundary_x=pg.BOUNDARY_WALL_OPEN)
+
+
+# ------------------------------------------------------------------ explicit (Tristan) path
+def tristan_sim(pg, st, real, sort_every, er, br):
+    return pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real, sort_every=sort_every, tile=(0, 0, 0),
+                            boundary_x=pg.BOUNDARY_WALL_OPEN, e_right=er, b_right=br)
+
+
+@pytest.mark.parametrize("sort_every", [0, 1, 3])
+@pytest.mark.parametrize("name", golden_names("tristan_wall"))
+def test_tristan_wall_golden_vectors(pg, name, sort_every):
+    """The reference's own explicit wall runs on the FP64 path: the unfused
+    push and zigzag (sort_every 0) and the fused tile kernel (sorted
+    particles; escaped ones wait marked for the sort every third step)."""
+    f = load(name)
+    st = f["state"]
+    w, er, br = wall_of(f)
+    sim = tristan_sim(pg, st, 1, sort_every, er, br)
+    sim.upload_state(st)
+    sim.buneman_step(f["steps"])
+    E, B, J = sim.download_fields()
+    b = st.box
+    assert rel_err(yee_physical(E, b, "E"), yee_physical(f["E"], b, "E")) < TOL64
+    assert rel_err(yee_physical(B, b, "B"), yee_physical(f["B"], b, "B")) < TOL64
+    assert rel_err(J, f["extra"]["J"].reshape(J.shape)) < TOL64
+    escaped = 0
+    for s, o in enumerate(f["out"]):
+        keep = survivors(o)
+        escaped += len(o["x"]) - len(keep)
+        got = by_id(sim.download_particles(s))
+        assert np.array_equal(got["id"], keep)
+        xg, yg, zg = I.positions(b, got)
+        assert np.abs(xg - o["x"][keep]).max() < 1e-11
+        for k in ("px", "py", "pz"):
+            assert rel_err(got[k], o[k][keep]) < TOL64
+    assert escaped > 0
+    sim.close()
+
+
+def _tristan_state(seed=53):
+    st = I.shock_plasma(32, 8, 4, dx=0.5, dt=0.225, ppc=(4, 4, 2), flow_gamma=3.0, theta_e=0.3, seed=seed,
+                        first_cell=I.TRISTAN_WALL_NODE)
+    for sp in st.species:
+        sp["px"][::3] = -sp["px"][::3]
+    return st
+
+
+@pytest.mark.parametrize("real,sort_every", [(1, 1), (1, 0), (0, 1), (0, 2)])
+def test_tristan_wall_steps_with_injection_match_oracle(pg, real, sort_every):
+    """Reflection, escape and particles appended at the open boundary before
+    every explicit step, against the oracle on the same particles: FP64
+    1e-11, FP32 particles and fields 1e-5."""
+    st = _tristan_state()
+    er, br = st.e_right, st.b_right
+    sim = tristan_sim(pg, st, real, sort_every, er, br)
+    for sp in st.species:
+        sim.add_species(sp["q"], sp["m"], sp["w"], 4 * len(sp["cell"]))
+    for s, sp in enumerate(st.species):
+        sim.upload_particles(s, sp)
+    sim.upload_fields(st.E, st.B)
+    g = O.make_grid(st.box, wall_x=1, e_right=er, b_right=br)
+    spo = copy_species(st.species)
+    for sp in spo:
+        sp["id"] = np.arange(len(sp["cell"]), dtype=np.int32)
+    nxt = [len(sp["cell"]) for sp in spo]
+    E, B = st.E.copy(), st.B.copy()
+    rng = np.random.default_rng(9)
+    for step in range(5):
+        for s, new in enumerate(_inject(st, step, rng)):
+            sim.append_particles(s, new)
+            for k in ("cell", "ox", "oy", "oz", "px", "py", "pz"):
+                spo[s][k] = np.concatenate([spo[s][k], new[k]]).astype(spo[s][k].dtype)
+            spo[s]["id"] = np.concatenate([spo[s]["id"], np.arange(nxt[s], nxt[s] + len(new["cell"]), dtype=np.int32)])
+            nxt[s] += len(new["cell"])
+        sim.buneman_step(1)
+        J = O.buneman_step(g, spo, E, B)
+    tol = TOL64 if real else TOL32
+    Eg, Bg, Jg = sim.download_fields()
+    b = st.box
+    assert rel_err(yee_physical(Eg, b, "E"), yee_physical(E, b, "E")) < tol
+    assert rel_err(yee_physical(Bg, b, "B"), yee_physical(B, b, "B")) < tol
+    assert rel_err(Jg, J.reshape(Jg.shape)) < tol
+    escaped = 0
+    for s in range(len(spo)):
+        got = by_id(sim.download_particles(s))
+        ref = by_id({k: v for k, v in spo[s].items() if isinstance(v, np.ndarray)})
+        escaped += nxt[s] - len(ref["id"])
+        assert np.array_equal(got["id"], ref["id"])
+        xg, _, _ = I.positions(b, got)
+        xr, _, _ = I.positions(b, ref)
+        assert np.abs(xg - xr).max() < (1e-11 if real else 1e-5) * b.nx * b.dx
+        for k in ("px", "py", "pz"):
+            assert rel_err(got[k], ref[k]) < tol
+    assert escaped > 0
+    sim.close()
+
+
+def test_tristan_wall_fill_starts_at_the_reflecting_wall(pg):
+    st = _tristan_state()
+    sim = tristan_sim(pg, st, 0, 1, st.e_right, st.b_right)
+    sid = sim.add_species(-1.0, 1.0, 0.01, 8 * st.box.ncells)
+    sim.fill_species(sid, 2, seed=3, theta=0.01, drift_gamma=1.5, alternate_drift=-1)
+    d = sim.download_particles(sid)
+    i = d["cell"] % st.box.nx
+    assert i.min() == I.TRISTAN_WALL_NODE and i.max() == st.box.nx - 3
+    assert len(d["cell"]) == 2 * (st.box.nx - 2 - I.TRISTAN_WALL_NODE) * st.box.ny * st.box.nz
+    sim.close()

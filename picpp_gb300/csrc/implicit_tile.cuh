@@ -94,6 +94,22 @@ __device__ __forceinline__ T tri_block(const T* __restrict__ F, int base, int sx
                  wy * (ux * F[base + sz + sy] + wx * F[base + sz + sy + sx]));
 }
 
+// The same trilinear form on a block of float4 nodes or cells (x, y, z, unused):
+// one 16-byte load per corner for all three components, each component
+// evaluated in exactly tri_block's order.
+__device__ __forceinline__ void tri_block4(const float4* __restrict__ F, int base, int sx, int sy, int sz, float wx,
+                                           float wy, float wz, float out[3]) {
+    const float ux = 1.f - wx, uy = 1.f - wy, uz = 1.f - wz;
+    const float4 f000 = F[base], f100 = F[base + sx], f010 = F[base + sy], f110 = F[base + sy + sx];
+    const float4 f001 = F[base + sz], f101 = F[base + sz + sx], f011 = F[base + sz + sy], f111 = F[base + sz + sy + sx];
+    out[0] = uz * (uy * (ux * f000.x + wx * f100.x) + wy * (ux * f010.x + wx * f110.x)) +
+             wz * (uy * (ux * f001.x + wx * f101.x) + wy * (ux * f011.x + wx * f111.x));
+    out[1] = uz * (uy * (ux * f000.y + wx * f100.y) + wy * (ux * f010.y + wx * f110.y)) +
+             wz * (uy * (ux * f001.y + wx * f101.y) + wy * (ux * f011.y + wx * f111.y));
+    out[2] = uz * (uy * (ux * f000.z + wx * f100.z) + wy * (ux * f010.z + wx * f110.z)) +
+             wz * (uy * (ux * f001.z + wx * f101.z) + wy * (ux * f011.z + wx * f111.z));
+}
+
 // ---- tensor-core reduction of one run (FP32 accumulators) -------------------
 // The 96 node sums  N[q][c] = sum_p QN_p[q] wn_p[c]  and 189 cell sums
 // C[s][q] = sum_p wc_p[s] QC_p[q]  of a run of particles are small matrix
@@ -587,9 +603,15 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                                                             const double* __restrict__ E, const double* __restrict__ B,
                                                             const double* __restrict__ Et) {
     extern __shared__ __align__(16) unsigned char mv_smem[];
-    T* sE = reinterpret_cast<T*>(mv_smem);   // [3][NB]
-    T* sEt = sE + 3 * mb.NB;                 // [3][NB]
-    T* sB = sEt + 3 * mb.NB;                 // [3][CB]
+    // FP32: E^theta and B^n, gathered two or three times per particle, as
+    // float4 nodes / cells (one 16-byte load per corner); E^n, gathered
+    // once, as three scalar planes.  FP64: three scalar planes each.
+    constexpr bool kVec = sizeof(T) == sizeof(float);
+    float4* sEt4 = reinterpret_cast<float4*>(mv_smem);   // [NB] (FP32)
+    float4* sB4 = sEt4 + mb.NB;                           // [CB] (FP32)
+    T* sE = kVec ? reinterpret_cast<T*>(sB4 + mb.CB) : reinterpret_cast<T*>(mv_smem);   // [3][NB]
+    T* sEt = sE + 3 * mb.NB;                 // [3][NB] (FP64)
+    T* sB = sEt + 3 * mb.NB;                 // [3][CB] (FP64)
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int T3 = t.tx * t.ty * t.tz;
     const bool ax = g.nx > 1, ay = g.y3, az = g.z3;
@@ -609,17 +631,24 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
             const int lx = e % mb.nbx, ly = (e / mb.nbx) % mb.nby, lz = e / (mb.nbx * mb.nby);
             const long long gid = linw(g, x0 - hx + lx, y0 - hy + ly, z0 - hz + lz);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                sE[c * mb.NB + e] = T(E[c * g.N + gid]);
-                sEt[c * mb.NB + e] = T(Et[c * g.N + gid]);
+            for (int c = 0; c < 3; ++c) sE[c * mb.NB + e] = T(E[c * g.N + gid]);
+            if constexpr (kVec) {
+                sEt4[e] = make_float4(float(Et[gid]), float(Et[g.N + gid]), float(Et[2 * g.N + gid]), 0.f);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) sEt[c * mb.NB + e] = T(Et[c * g.N + gid]);
             }
         }
         for (int e = threadIdx.x; e < mb.CB; e += blockDim.x) {
             const int lx = e % mb.cbx, ly = (e / mb.cbx) % mb.cby, lz = e / (mb.cbx * mb.cby);
             const long long gid = linw(g, x0 - hx - (ax ? 1 : 0) + lx, y0 - hy - (ay ? 1 : 0) + ly,
                                        z0 - hz - (az ? 1 : 0) + lz);
+            if constexpr (kVec) {
+                sB4[e] = make_float4(float(B[gid]), float(B[g.N + gid]), float(B[2 * g.N + gid]), 0.f);
+            } else {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sB[c * mb.CB + e] = T(B[c * g.N + gid]);
+                for (int c = 0; c < 3; ++c) sB[c * mb.CB + e] = T(B[c * g.N + gid]);
+            }
         }
         __syncthreads();
         for (int s = 0; s < S.ns; ++s) {
@@ -679,6 +708,25 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                             out[q] = tri_block<T>(blkN + q * mb.CB, L.cbase, csx, csy, csz, L.wc[0], L.wc[1], L.wc[2]);
                     }
                 };
+                // E^theta (node) and B^n (cell): float4 blocks for FP32
+                auto gatEt = [&](const Loc& L, const int c[3], const T u[3], T out[3]) {
+                    if constexpr (kVec) {
+                        if (L.inb) {
+                            tri_block4(sEt4, L.nbase, nsx, nsy, nsz, L.wn[0], L.wn[1], L.wn[2], out);
+                            return;
+                        }
+                    }
+                    gat(L, c, u, sEt, Et, true, out);
+                };
+                auto gatB = [&](const Loc& L, const int c[3], const T u[3], T out[3]) {
+                    if constexpr (kVec) {
+                        if (L.inb) {
+                            tri_block4(sB4, L.cbase, csx, csy, csz, L.wc[0], L.wc[1], L.wc[2], out);
+                            return;
+                        }
+                    }
+                    gat(L, c, u, sB, B, false, out);
+                };
                 T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
                 T mom0[3] = {p.px[n], p.py[n], p.pz[n]};
                 T gam, v[3];
@@ -687,9 +735,9 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 Loc L0;
                 locate(ci, u0, L0);
                 gat(L0, ci, u0, sE, E, true, e);
-                gat(L0, ci, u0, sB, B, false, b);
+                gatB(L0, ci, u0, b);
                 alpha_tensor<T>(beta, v, gam, e, b, al);
-                gat(L0, ci, u0, sEt, Et, true, e);
+                gatEt(L0, ci, u0, e);
                 T vxb[3] = {v[1] * b[2] - v[2] * b[1], -v[0] * b[2] + v[2] * b[0], v[0] * b[1] - v[1] * b[0]};
                 T pnew[3];
 #pragma unroll
@@ -749,8 +797,8 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     }
                     Loc L1;
                     locate(tc, tu, L1);
-                    gat(L1, tc, tu, sEt, Et, true, e);
-                    gat(L1, tc, tu, sB, B, false, b);
+                    gatEt(L1, tc, tu, e);
+                    gatB(L1, tc, tu, b);
                     const T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
 #pragma unroll
                     for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;

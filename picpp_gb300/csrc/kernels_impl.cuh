@@ -283,7 +283,10 @@ bool PK<T>::implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& 
     mb.cbz = g.z3 ? t.tz + 2 * H + 2 : 1;
     mb.NB = mb.nbx * mb.nby * mb.nbz;
     mb.CB = mb.cbx * mb.cby * mb.cbz;
-    const size_t smem = (6 * (size_t)mb.NB + 3 * (size_t)mb.CB) * sizeof(T);
+    // FP32: E^theta and B^n as float4 nodes / cells, E^n as three planes
+    const size_t smem = sizeof(T) == sizeof(float)
+                            ? ((size_t)mb.NB + (size_t)mb.CB) * 16 + 3 * (size_t)mb.NB * sizeof(float)
+                            : (6 * (size_t)mb.NB + 3 * (size_t)mb.CB) * sizeof(T);
     if (smem > 227 * 1024) return false;
     static bool attr_set = false;
     if (!attr_set) {

@@ -148,23 +148,46 @@ __device__ __forceinline__ void mma_tf32x3(float d[4], const float a[4], const u
     mma_tf32(d, ah, bh);
 }
 
-// Sums of one run over the warp, added to dn and dc: mem = lanes in the run;
-// row = this lane's raw quantities (used only when the lane is in the run).
-// Lane (g = lane/4, t = lane%4) holds dn[i] = N[g + 8(i/2)][2t + i%2] and
-// dc[4k + i] = C[16k + g + 8(i/2)][2t + i%2].
-__device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, bool me, unsigned mem,
-                                            const float row[kScrRow], float dn[4], float dc[8]) {
-    const int g = lane >> 2, tq = lane & 3;
-    const int gx = g & 1, gy = (g >> 1) & 1, gz = g >> 2;
-    const int ia = g >= 1 && g <= 6 ? sym_a(g - 1) : 0, ib = g >= 1 && g <= 6 ? sym_b(g - 1) : 0;
-    // this lane's four cell slots g, g + 8, g + 16, g + 24: row offsets of their x, y, z weights
-    int sox[4], soy[4], soz[4];
+// The scratch-row columns a lane reads in tc_run_sums, which depend on the
+// lane only: byte k of sx / sy / sz is the column of the x / y / z weight
+// of cell slot g + 8k (g = lane / 4); bytes of nb: the node weight columns
+// 12 + gx, 14 + gy, 16 + gz and the rv columns ia, ib of pressure
+// component g - 1.  Built once per CTA into a shared table.
+struct TcLane {
+    unsigned sx, sy, sz, nb;
+};
+__device__ __forceinline__ TcLane tc_lane(int lane) {
+    const int g = lane >> 2;
+    TcLane t{0u, 0u, 0u, 0u};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int sl = g + 8 * k;
-        sox[k] = 18 + sl % 3;
-        soy[k] = 21 + (sl / 3) % 3;
-        soz[k] = sl < 27 ? 24 + sl / 9 : 24;
+        t.sx |= (unsigned)(18 + sl % 3) << (8 * k);
+        t.sy |= (unsigned)(21 + (sl / 3) % 3) << (8 * k);
+        t.sz |= (unsigned)(sl < 27 ? 24 + sl / 9 : 24) << (8 * k);
+    }
+    const int ia = g >= 1 && g <= 6 ? sym_a(g - 1) : 0, ib = g >= 1 && g <= 6 ? sym_b(g - 1) : 0;
+    t.nb = (unsigned)(12 + (g & 1)) | (unsigned)(14 + ((g >> 1) & 1)) << 8 | (unsigned)(16 + (g >> 2)) << 16 |
+           (unsigned)(ia | ib << 4) << 24;
+    return t;
+}
+__device__ __forceinline__ int tc_byte(unsigned w, int k) { return (int)((w >> (8 * k)) & 0xffu); }
+
+// Sums of one run over the warp, added to dn and dc: mem = lanes in the run;
+// row = this lane's raw quantities (used only when the lane is in the run);
+// tl = this lane's TcLane.  Lane (g = lane/4, t = lane%4) holds
+// dn[i] = N[g + 8(i/2)][2t + i%2] and dc[4k + i] = C[16k + g + 8(i/2)][2t + i%2].
+__device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, bool me, unsigned mem,
+                                            const float row[kScrRow], float dn[4], float dc[8], const TcLane tl) {
+    const int g = lane >> 2, tq = lane & 3;
+    const int cnx = tc_byte(tl.nb, 0), cny = tc_byte(tl.nb, 1), cnz = tc_byte(tl.nb, 2);
+    const int ia = tc_byte(tl.nb, 3) & 15, ib = tc_byte(tl.nb, 3) >> 4;
+    int sox[4], soy[4], soz[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        sox[k] = tc_byte(tl.sx, k);
+        soy[k] = tc_byte(tl.sy, k);
+        soz[k] = tc_byte(tl.sz, k);
     }
     {
         float* r = scr + lane * kScrRow;
@@ -180,8 +203,8 @@ __device__ __forceinline__ void tc_run_sums(float* __restrict__ scr, int lane, b
         unsigned bh[2], bl[2];
         float a[4];
         // nodes: A[q][p] = (rv, alpha)[q], q = g and g + 8 (< 12); B[p][c] = node weight of corner c = g
-        tf32_split(P0[12 + gx] * P0[14 + gy] * P0[16 + gz], bh[0], bl[0]);
-        tf32_split(P1[12 + gx] * P1[14 + gy] * P1[16 + gz], bh[1], bl[1]);
+        tf32_split(P0[cnx] * P0[cny] * P0[cnz], bh[0], bl[0]);
+        tf32_split(P1[cnx] * P1[cny] * P1[cnz], bh[1], bl[1]);
         a[0] = P0[g];
         a[1] = g < 4 ? P0[g + 8] : 0.f;
         a[2] = P1[g];
@@ -351,9 +374,12 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
     const int oxc = ax ? 1 : 0, oyc = ay ? csy : 0, ozc = az ? csz : 0;   // slot strides
     const int tot = 12 * bk.NB + 7 * bk.CB;
     constexpr bool kTc = sizeof(A) == sizeof(float);   // FP32 accumulators: tensor-core run sums
-    float* scr = reinterpret_cast<float*>(imp_smem + (size_t)tot * sizeof(A) +
-                                          (kStaged ? (size_t)3 * (bk.NB + bk.CB) * sizeof(T) : 0)) +
-                 warp * (kScrParticles * kScrRow);
+    float* scr0 = reinterpret_cast<float*>(imp_smem + (size_t)tot * sizeof(A) +
+                                           (kStaged ? (size_t)3 * (bk.NB + bk.CB) * sizeof(T) : 0));
+    float* scr = scr0 + warp * (kScrParticles * kScrRow);
+    // the lane table of tc_run_sums follows the scratch rows of all warps
+    TcLane* s_lane = reinterpret_cast<TcLane*>(scr0 + nwarps * (kScrParticles * kScrRow));
+    if (kTc && threadIdx.x < 32) s_lane[threadIdx.x] = tc_lane(threadIdx.x);
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int ti = tile % t.ntx, tj = (tile / t.ntx) % t.nty, tk = tile / (t.ntx * t.nty);
@@ -466,7 +492,7 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                         const bool mine = valid && inb && nb == nbK;
                         const unsigned mm = __ballot_sync(0xffffffffu, mine);
                         if (mm) {
-                            tc_run_sums(scr, lane, mine, mm, row, an, ac);
+                            tc_run_sums(scr, lane, mine, mm, row, an, ac, s_lane[lane]);
                             acc_any = true;
                         }
                         pending &= ~mm;
@@ -482,7 +508,7 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                             const int cbL = __shfl_sync(0xffffffffu, cb, leader);
                             if constexpr (kTc) {
                                 float dn[4] = {0.f, 0.f, 0.f, 0.f}, dc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                                tc_run_sums(scr, lane, me, mem, row, dn, dc);
+                                tc_run_sums(scr, lane, me, mem, row, dn, dc, s_lane[lane]);
                                 add_run_sums(sN, sC, bk.NB, bk.CB, nbL, cbL, oxn, oyn, ozn, oxc, oyc, ozc, lane, dn, dc,
                                              float(cq), float(cm));
                             } else {

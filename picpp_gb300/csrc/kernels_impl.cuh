@@ -247,7 +247,10 @@ ImpBlock PK<T>::implicit_block(const GridP& g, const TileGeom& t, int h) {
 template <typename T>
 size_t PK<T>::implicit_tile_smem(const ImpBlock& bk) {
     // FP32 accumulators add the per-warp rows of the tensor-core run sums
-    const size_t scratch = sizeof(T) == sizeof(float) ? (size_t)(imp_threads<T>() / 32) * kScrParticles * kScrRow * sizeof(float) : 0;
+    // and their 32-entry lane table
+    const size_t scratch = sizeof(T) == sizeof(float)
+                               ? (size_t)(imp_threads<T>() / 32) * kScrParticles * kScrRow * sizeof(float) + 32 * sizeof(TcLane)
+                               : 0;
     return (12 * (size_t)bk.NB + 7 * (size_t)bk.CB + (bk.stage ? 3 * ((size_t)bk.NB + bk.CB) : 0)) * sizeof(T) + scratch;
 }
 

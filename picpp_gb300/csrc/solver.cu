@@ -188,7 +188,9 @@ pic_status ensure_z(SolveCtx& c, int m, long long L) {
 }
 
 // Restarted GMRES(m): classical Gram-Schmidt with a second pass where the
-// first one cancels, Givens rotations on the host, FP64 true residual at every restart.  With
+// first one cancels, Givens rotations on the host (one stream
+// synchronisation per iteration, two with the second pass), FP64 true
+// residual at every restart.  With
 // a network (pc != nullptr) it is flexible GMRES (Saad 1993) with the right
 // preconditioner z_j = pc(v_j), x += Z y; a cycle that does not halve the
 // true residual, or a non-finite preconditioned direction, switches the
@@ -258,7 +260,8 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             CKS(cudaMemcpyAsync(&after, k.scal + 2, sizeof(double), cudaMemcpyDeviceToHost, c.s));
             CKS(cudaStreamSynchronize(c.s));
             const double before = std::sqrt(std::max(h1[j + 1], 0.0));
-            if (!(after >= 0.7071067811865476 * before)) {
+            const bool second = !(after >= 0.7071067811865476 * before);
+            if (second) {
                 launch_multi_dot(c.s, k.V, L, j + 1, w, L, k.part, P, k.hdev + (m + 2));
                 launch_multi_axpy_minus(c.s, w, k.V, L, j + 1, k.hdev + (m + 2), 1, L);
                 launch_dot(c.s, w, w, L, k.part, P, k.hdev + (j + 1), 1);
@@ -270,7 +273,9 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
                 CKS(cudaMemcpyAsync(k.hdev + (j + 1), k.scal + 2, sizeof(double), cudaMemcpyDeviceToDevice, c.s));
             }
             launch_scale_inv_dev(c.s, w, w, k.hdev + (j + 1), L);
-            CKS(cudaStreamSynchronize(c.s));
+            // only the second pass copies values back; otherwise the host's
+            // Givens update overlaps the normalisation and the next apply
+            if (second) CKS(cudaStreamSynchronize(c.s));
             if (pc) {
                 // a non-finite direction, or one already in the Krylov space
                 // (|h_{j+1,j}| below 1e-10 |A z_j|), ends the cycle

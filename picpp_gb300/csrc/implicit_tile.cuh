@@ -123,12 +123,12 @@ __device__ __forceinline__ void tri_block4(const float4* __restrict__ F, int bas
 constexpr int kScrRow = 27;         // scratch floats per particle
 constexpr int kScrParticles = 32;   // scratch rows per warp
 
-// Round to the 19-bit TF32 format (ties away from zero); low 13 bits zero.
-__device__ __forceinline__ unsigned tf32_round(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
-
+// x = hi + lo + e with hi, lo in the 19-bit TF32 format (low 13 bits zero),
+// both truncated: x - hi is exact in FP32 (at most 13 significant bits) and
+// |e| < 2^-21 |x|.  Three integer/FP32 operations per split.
 __device__ __forceinline__ void tf32_split(float x, unsigned& hi, unsigned& lo) {
-    hi = tf32_round(x);
-    lo = tf32_round(x - __uint_as_float(hi));
+    hi = __float_as_uint(x) & 0xffffe000u;
+    lo = __float_as_uint(x - __uint_as_float(hi)) & 0xffffe000u;
 }
 
 // D (16x8, FP32) += A (16x8, TF32, row) * B (8x8, TF32, col)

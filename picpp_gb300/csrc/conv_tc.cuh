@@ -194,18 +194,20 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __nv_bfloat16* __
         __syncthreads();
         tc_fence_after();
         if (threadIdx.x == 0 && ok) {
-#pragma unroll 1
-            for (int tp = 0; tp < kTapsPerStage; ++tp) {
-                const int tap = st * kTapsPerStage + tp;
-                const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
-                const uint32_t aTap = aBase + (uint32_t)(((kd * kTcBH + kh) * kTcBW + kw) * 16);
-                const uint32_t bTap = wBase + (uint32_t)(tp * C8 * COUT * 16);
+            // descriptor start fields count 16-byte units (one voxel of the
+            // A layout, one 8-channel row of B): base descriptors plus
+            // constants per tap
+            const uint64_t aD = tc_desc(aBase, kTcBV * 16, kTcBW * 16);
+            const uint64_t bD = tc_desc(wBase, COUT * 16, 128);
 #pragma unroll
-                for (int kc = 0; kc < CIN / 16; ++kc) {
-                    const uint64_t ad = tc_desc(aTap + (uint32_t)(2 * kc * kTcBV * 16), kTcBV * 16, kTcBW * 16);
-                    const uint64_t bd = tc_desc(bTap + (uint32_t)(2 * kc * COUT * 16), COUT * 16, 128);
-                    tc_mma(tmem, ad, bd, kIdesc, (tap | kc) != 0);
-                }
+            for (int tp = 0; tp < kTapsPerStage; ++tp) {
+                const int kd = kAll ? tp / 9 : st, kh = (tp / 3) % 3, kw = tp % 3;
+                const uint64_t aT = aD + (uint64_t)((kd * kTcBH + kh) * kTcBW + kw);
+                const uint64_t bT = bD + (uint64_t)(tp * C8 * COUT);
+#pragma unroll
+                for (int kc = 0; kc < CIN / 16; ++kc)
+                    tc_mma(tmem, aT + (uint64_t)(2 * kc * kTcBV), bT + (uint64_t)(2 * kc * COUT), kIdesc,
+                           ((st * kTapsPerStage + tp) | kc) != 0);
             }
             tc_commit(mbar);
         }

@@ -521,6 +521,11 @@ pic_status pic_create(const pic_config* cfg, pic_ctx** out) {
     TileGeom& t = ctx->tg;
     t.tx = tile[0]; t.ty = tile[1]; t.tz = tile[2];
     t.ntx = c.nx / t.tx; t.nty = c.ny / t.ty; t.ntz = c.nz / t.tz;
+    {
+        auto lg = [](int v) { int l = 0; while ((1 << l) < v) ++l; return (1 << l) == v ? l : -1; };
+        t.lx = lg(t.tx); t.ly = lg(t.ty); t.lz = lg(t.tz);
+        if (t.lx < 0 || t.ly < 0 || t.lz < 0) t.lx = t.ly = t.lz = -1;
+    }
     ctx->ntiles = t.ntx * t.nty * t.ntz;
     ctx->T3 = t.tx * t.ty * t.tz;
     ctx->nkeys = (int)N;

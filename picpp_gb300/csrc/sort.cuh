@@ -4,9 +4,10 @@
 // GPU keeps each species in SoA arrays ordered by a tile-major cell key so
 // that a tile's particles are contiguous.  The sort is bit-exact with the
 // oracle's stable counting sort:
-//   1. key per particle, histogram (integer atomics: exact counts)
+//   1. key per particle, histogram (integer atomics per run of equal keys
+//      in a warp: exact counts)
 //   2. exclusive scan of the counts (3-phase block scan)
-//   3. scatter of source indices with one atomic cursor per key
+//   3. scatter of source indices with one atomic cursor per key and run
 //      (arbitrary order inside a key), then
 //   4. per-key segment sort of the source indices by rank counting, which
 //      restores input order inside every key: stable and run-independent
@@ -21,16 +22,33 @@ namespace pic {
 __device__ __forceinline__ int sort_key(const GridP& g, const TileGeom& t, int cell) {
     int i, j, k;
     decode(g, cell, i, j, k);
-    int ti = i / t.tx, tj = j / t.ty, tk = k / t.tz;
+    int ti, tj, tk;
+    if (t.lx >= 0) {   // power-of-two tiles (the default): shifts, not divisions
+        ti = i >> t.lx; tj = j >> t.ly; tk = k >> t.lz;
+    } else {
+        ti = i / t.tx; tj = j / t.ty; tk = k / t.tz;
+    }
     int li = i - ti * t.tx, lj = j - tj * t.ty, lk = k - tk * t.tz;
     int tile = (tk * t.nty + tj) * t.ntx + ti;
     int local = (lk * t.ty + lj) * t.tx + li;
     return tile * (t.tx * t.ty * t.tz) + local;
 }
 
-// Sort key of every particle and the per-key counts, one atomic per distinct
-// key per warp (consecutive particles mostly share a key: the input is the
-// previous sort order).
+// Runs of equal keys within a warp: the head lane of each run and the run's
+// length (consecutive particles mostly share a key: the input is the
+// previous sort order; a key that recurs later in the warp starts another
+// run).
+__device__ __forceinline__ bool key_run(int kk, int lane, int& len) {
+    const int prev = __shfl_up_sync(0xffffffffu, kk, 1);
+    const bool head = lane == 0 || kk != prev;
+    const unsigned H = __ballot_sync(0xffffffffu, head);
+    const unsigned after = H & ~((2u << lane) - 1u);   // heads after this lane
+    len = (after ? __ffs(after) - 1 : 32) - lane;
+    return head;
+}
+
+// Sort key of every particle and the per-key counts, one atomic per run of
+// equal keys in a warp.
 __global__ void k_keys_hist(GridP g, TileGeom t, const int* __restrict__ cell, long long n, int* __restrict__ key,
                             int* __restrict__ counts) {
     const int lane = threadIdx.x & 31;
@@ -40,8 +58,8 @@ __global__ void k_keys_hist(GridP g, TileGeom t, const int* __restrict__ cell, l
         const int ca = a < n ? cell[a] : -1;   // escaped particles (cell -1) get no key and drop out
         const int kk = ca >= 0 ? sort_key(g, t, ca) : -1;
         if (a < n) key[a] = kk;
-        const unsigned m = __match_any_sync(0xffffffffu, kk);
-        if (kk >= 0 && lane == __ffs(m) - 1) atomicAdd(&counts[kk], __popc(m));
+        int len;
+        if (key_run(kk, lane, len) && kk >= 0) atomicAdd(&counts[kk], len);
     }
 }
 
@@ -119,21 +137,23 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(int* __restrict__ a, 
         if (base + q < n) a[base + q] += add;
 }
 
-// Source index a to tmp[cursor[key[a]]++], one atomic per distinct key per
-// warp (consecutive particles mostly share a key: the input is the previous
-// sort order); the order inside a key is restored by the segment sort.
+// Source index a to tmp[cursor[key[a]]++], one atomic per run of equal keys
+// in a warp; the order inside a key is restored by the segment sort.
 __global__ void k_scatter_atomic(const int* __restrict__ key, long long n, int* __restrict__ cursor, int* __restrict__ tmp) {
     const int lane = threadIdx.x & 31;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long base = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
         const long long a = base + lane;
         const int kk = a < n ? key[a] : -1;
-        const unsigned m = __match_any_sync(0xffffffffu, kk);
-        const int leader = __ffs(m) - 1;
+        int len;
+        const bool head = key_run(kk, lane, len);
         int pos = 0;
-        if (kk >= 0 && lane == leader) pos = atomicAdd(&cursor[kk], __popc(m));
-        pos = __shfl_sync(0xffffffffu, pos, leader);
-        if (kk >= 0) tmp[pos + __popc(m & ((1u << lane) - 1u))] = (int)a;
+        if (head && kk >= 0) pos = atomicAdd(&cursor[kk], len);
+        // each lane takes its run head's position plus its place in the run
+        const unsigned H = __ballot_sync(0xffffffffu, head);
+        const int hl = 31 - __clz(H & ((2u << lane) - 1u));   // this lane's head
+        pos = __shfl_sync(0xffffffffu, pos, hl);
+        if (kk >= 0) tmp[pos + (lane - hl)] = (int)a;
     }
 }
 

@@ -18,6 +18,7 @@ struct GhostAxes {
 struct TileGeom {
     int tx, ty, tz;      // tile extents
     int ntx, nty, ntz;   // tiles per axis
+    int lx, ly, lz;      // log2 of the extents when all three are powers of two, else -1
 };
 
 // Shared-memory blocks of the fused explicit kernel (boris_tile.cuh).

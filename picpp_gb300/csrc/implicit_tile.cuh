@@ -696,19 +696,19 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     int nbase, cbase;
                     T wn[3], wc[3];
                 };
-                auto locate = [&](const int c[3], const T u[3], Loc& L) {
-                    int l[3];
-                    L.inb = local_axis(c[0], x0, t.tx, hx, g.nx, l[0]) && local_axis(c[1], y0, t.ty, hy, g.ny, l[1]) &&
-                            local_axis(c[2], z0, t.tz, hz, g.nz, l[2]);
+                // from tile-local cells l (the block holds l in [-h, t - 1 + h])
+                auto locate_l = [&](const int l[3], const T u[3], Loc& L) {
+                    L.inb = l[0] >= -hx && l[0] <= t.tx - 1 + hx && l[1] >= -hy && l[1] <= t.ty - 1 + hy &&
+                            l[2] >= -hz && l[2] <= t.tz - 1 + hz;
                     if (!L.inb) return;
                     int lo[3];
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
                         T w2[2];
                         int idx[2];
-                        node_w<T>(u[a], c[a], nn[a], idx, w2);
+                        node_w<T>(u[a], l[a], nn[a], idx, w2);
                         L.wn[a] = w2[1];
-                        cell_w<T>(u[a], c[a], nn[a], idx, w2);
+                        cell_w<T>(u[a], l[a], nn[a], idx, w2);
                         L.wc[a] = w2[1];
                         // lower cell of the pair: c - 1 below the centre, c above
                         lo[a] = (nn[a] > 1 && u[a] < T(0.5)) ? l[a] - 1 : l[a];
@@ -716,6 +716,15 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     L.nbase = (l[2] + hz) * nsz + (l[1] + hy) * nsy + (l[0] + hx) * nsx;
                     const int ex = ax ? 1 : 0, ey = ay ? 1 : 0, ez = az ? 1 : 0;
                     L.cbase = (lo[2] + hz + ez) * csz + (lo[1] + hy + ey) * csy + (lo[0] + hx + ex) * csx;
+                };
+                // from global cells c: the periodic image inside the block, if any
+                auto locate = [&](const int c[3], const T u[3], Loc& L, int l[3]) {
+                    if (!(local_axis(c[0], x0, t.tx, hx, g.nx, l[0]) && local_axis(c[1], y0, t.ty, hy, g.ny, l[1]) &&
+                          local_axis(c[2], z0, t.tz, hz, g.nz, l[2]))) {
+                        L.inb = false;
+                        return;
+                    }
+                    locate_l(l, u, L);
                 };
                 auto gat = [&](const Loc& L, const int c[3], const T u[3], const T* __restrict__ blkN,
                                const double* __restrict__ glbN, bool node, T out[3]) {
@@ -759,7 +768,8 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 gamma_vel<T>(mom0, mm, gam, v);
                 T e[3], b[3], al[9];
                 Loc L0;
-                locate(ci, u0, L0);
+                int l0[3];
+                locate(ci, u0, L0, l0);
                 gat(L0, ci, u0, sE, E, true, e);
                 gatB(L0, ci, u0, b);
                 alpha_tensor<T>(beta, v, gam, e, b, al);
@@ -814,15 +824,39 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                             break;
                         }
                     }
-                    int tc[3];
+                    // the trial position x^n + newDisp: the offsets as advance_axis
+                    // forms them; the cell in tile-local terms (no periodic wrap),
+                    // the global cell only for a position outside the block
+                    int tc[3] = {0, 0, 0};
                     T tu[3];
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        tc[d] = ci[d]; tu[d] = u0[d];
-                        advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
-                    }
                     Loc L1;
-                    locate(tc, tu, L1);
+                    if (L0.inb) {
+                        int tl[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            const T sd = u0[d] + newDisp[d] * id[d];
+                            const T fd = dev_floor(sd);
+                            T ud = sd - fd;
+                            int cd = l0[d] + (int)fd;
+                            if (ud >= T(1)) { ud -= T(1); cd += 1; }
+                            tl[d] = nn[d] > 1 ? cd : 0;
+                            tu[d] = ud;
+                        }
+                        locate_l(tl, tu, L1);
+                        if (!L1.inb) {
+                            const int org[3] = {x0, y0, z0};
+#pragma unroll
+                            for (int d = 0; d < 3; ++d) tc[d] = nn[d] > 1 ? wrap_any(org[d] + tl[d], nn[d]) : 0;
+                        }
+                    } else {
+                        int tl[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            tc[d] = ci[d]; tu[d] = u0[d];
+                            advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
+                        }
+                        locate(tc, tu, L1, tl);
+                    }
                     gatEt(L1, tc, tu, e);
                     gatB(L1, tc, tu, b);
                     const T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};

@@ -52,6 +52,18 @@ public:
         check(pic_download_particles(ctx_, species, &n, cell, ox, oy, oz, px, py, pz, ids));
         return n;
     }
+    // injectNewParticles (PIC++/mover.cpp:910-1000) with the caller's new
+    // particles, appended after the species' own
+    void injectNewParticles(int species, long n, const int* cell, const double* ox, const double* oy,
+                            const double* oz, const double* px, const double* py, const double* pz,
+                            const int* ids = nullptr) {
+        check(pic_append_particles(ctx_, species, n, cell, ox, oy, oz, px, py, pz, ids));
+    }
+    // device loading of a drifting Maxwell-Juttner species (no reference counterpart)
+    void fillSpecies(int species, int ppc, unsigned long long seed, double theta, double drift_gamma,
+                     int alternate_drift) {
+        check(pic_fill_species(ctx_, species, ppc, seed, theta, drift_gamma, alternate_drift));
+    }
     void uploadFields(const double* E, const double* B) { check(pic_upload_fields(ctx_, E, B)); }
     void downloadFields(double* E, double* B, double* J) { check(pic_download_fields(ctx_, E, B, J)); }
 
@@ -75,6 +87,16 @@ public:
     }
     void evaluateMagneticField() { check(pic_evaluate_magnetic_field(ctx_)); }
     void updateFields() { check(pic_update_fields(ctx_)); }
+    // the whole implicit branch of one step
+    pic_solve_info implicitStep(const pic_solve_opts& opts = defaultSolve()) {
+        pic_solve_info info{};
+        pic_status s = pic_implicit_step(ctx_, &opts, &info);
+        if (s != PIC_OK && s != PIC_ERR_NOT_CONVERGED) check(s);
+        return info;
+    }
+    // escaped particles of a wall box are erased inside the step calls
+    // (the next sort, before any call that reads particles)
+    void eraseEscapedPaticles() {}
     // correlation maps and the periodic particle exchange are folded into
     // the kernels (cell index + offset, wrap on every move)
     void updateParticleCorrelationMaps() {}
@@ -111,6 +133,21 @@ public:
         pic_train_info info{};
         check(pic_nn_train(ctx_, &opts, &info));
         return info;
+    }
+    // record up to capacity (right part, mu, solution) triples of the plain
+    // solves that follow (pic_train_opts.source = 1 trains on them)
+    void recordSolves(int capacity) { check(pic_nn_record(ctx_, capacity)); }
+    int recordedSolves() {
+        int n = 0;
+        check(pic_nn_record_count(ctx_, &n));
+        return n;
+    }
+    // bound of the convolutions' MMA-completion waits (0: the built-in one)
+    void convolutionWaitLimit(unsigned polls) { check(pic_nn_wait_limit(ctx_, polls)); }
+
+    // per-phase device time (the reference's timing prints)
+    void profile(bool enable, double* phase_ms = nullptr, long* launches = nullptr) {
+        check(pic_profile(ctx_, enable ? 1 : 0, phase_ms, launches));
     }
 
     static pic_solve_opts defaultSolve() { return pic_solve_opts{PIC_GMRES_REFERENCE, 30, 50, 1e-8}; }

@@ -1398,6 +1398,25 @@ void orc_density_moments(const orc_grid* g, const orc_particles* sp, int nspecie
                         vs[2 * N + id] += mom[2] * p->w * corr;
                     }
         }
+        if (g->wall_x) {
+            /* conductor wall: deposits in the ghost cell left of the wall go
+             * to the first cell with p_x reflected (momentum_collecting.cpp
+             * 945-960), those beyond the open boundary to the last physical
+             * cell; both ghost columns end empty (sumCellParametersX and
+             * sumCellVectorParametersX, one rank, momentum_exchange.cpp
+             * 968-988, 1351-1361) */
+            for (int k = 0; k < g->nz; ++k)
+                for (int j = 0; j < g->ny; ++j) {
+                    const long gl = IX(g, g->nx - 1, j, k), f = IX(g, 0, j, k);
+                    const long gr = IX(g, g->nx - 2, j, k), l = IX(g, g->nx - 3, j, k);
+                    cs[f] += cs[gl]; es[f] += es[gl];
+                    vs[f] -= vs[gl]; vs[N + f] += vs[N + gl]; vs[2 * N + f] += vs[2 * N + gl];
+                    cs[l] += cs[gr]; es[l] += es[gr];
+                    for (int d = 0; d < 3; ++d) vs[d * N + l] += vs[d * N + gr];
+                    cs[gl] = es[gl] = cs[gr] = es[gr] = 0.0;
+                    for (int d = 0; d < 3; ++d) vs[d * N + gl] = vs[d * N + gr] = 0.0;
+                }
+        }
         for (long c = 0; c < N; ++c) {
             rho[c] += p->q * cs[c];
             if (es[c] > 0) {

@@ -1297,6 +1297,7 @@ pic_status pic_update_density_parameters(pic_ctx* ctx) {
         double* base = ctx->dens + 5 * N * q;
         if (ctx->preal) PK<double>::density_deposit(s, ctx->g, view<double>(sp), sp.m, sp.w, base, base + N, base + 2 * N);
         else PK<float>::density_deposit(s, ctx->g, view<float>(sp), sp.m, sp.w, base, base + N, base + 2 * N);
+        if (ctx->g.wall) launch_density_wall_fold(s, ctx->g, base, base + N, base + 2 * N);
         launch_density_finish(s, N, sp.q, base, base + N, base + 2 * N, ctx->dens_rho);
     }
     return sync(ctx, "density parameters");

@@ -198,6 +198,38 @@ void launch_density_finish(cudaStream_t s, long long N, double q, const double* 
     k_density_finish<<<grid_for(N, 256), 256, 0, s>>>(N, q, conc, energy, mom_to_vel, rho);
 }
 
+// Wall box (SUPER_CONDUCTOR_LEFT, one rank): the deposits in the ghost cell
+// left of the wall (storage column nx - 1) go to cell 0 with the momentum's
+// x component reflected (momentum_collecting.cpp:945-960); those beyond the
+// open boundary (column nx - 2) go to the last physical cell nx - 3
+// (sumCellParametersX, momentum_exchange.cpp:968-988, and
+// sumCellVectorParametersX, 1351-1361); both ghost columns end empty.  One
+// thread per (y, z) row: each touches four cells of its own row.
+__global__ void k_density_wall_fold(GridP g, double* __restrict__ conc, double* __restrict__ energy,
+                                    double* __restrict__ mom) {
+    const int rows = g.ny * g.nz;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const int j = r % g.ny, k = r / g.ny;
+        const long long gl = lin(g, g.nx - 1, j, k), f = lin(g, 0, j, k);
+        const long long gr = lin(g, g.nx - 2, j, k), l = lin(g, g.nx - 3, j, k);
+        conc[f] += conc[gl];
+        energy[f] += energy[gl];
+        conc[l] += conc[gr];
+        energy[l] += energy[gr];
+        conc[gl] = energy[gl] = conc[gr] = energy[gr] = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double* m = mom + d * g.N;
+            m[f] += d == 0 ? -m[gl] : m[gl];
+            m[l] += m[gr];
+            m[gl] = m[gr] = 0.0;
+        }
+    }
+}
+
+void launch_density_wall_fold(cudaStream_t s, const GridP& g, double* conc, double* energy, double* mom) {
+    k_density_wall_fold<<<grid_for((long long)g.ny * g.nz, 128), 128, 0, s>>>(g, conc, energy, mom);
+}
+
 void launch_field_update(cudaStream_t s, const GridP& g, const double* Et, const double* E, const double* B,
                          double* En, double* Bn, int doE, int doB) {
     k_field_update<<<grid_for(g.N, 256), 256, 0, s>>>(g, Et, E, B, En, Bn, doE, doB);

@@ -118,6 +118,7 @@ void launch_smooth_rho_ext(cudaStream_t s, const GridP& g, const double* src, do
                            double sp);
 void launch_density_finish(cudaStream_t s, long long N, double q, const double* conc, const double* energy,
                            double* mom_to_vel, double* rho);
+void launch_density_wall_fold(cudaStream_t s, const GridP& g, double* conc, double* energy, double* mom);
 // Krylov
 void launch_dot(cudaStream_t s, const double* a, const double* b, long long n, double* partials, int P, double* out,
                 int take_sqrt);

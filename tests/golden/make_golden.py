@@ -110,6 +110,25 @@ def density(name, nx, ny, nz, ppc, seed):
                            for sp in st.species], st.E, st.B, extra)
 
 
+def wall_density(name, nx, ny, nz, ppc, seed):
+    """updateDensityParameters in the reflecting-wall box (SUPER_CONDUCTOR_LEFT,
+    one rank): particles fill every physical cell and a third move towards
+    the wall, so that both ghost-column folds carry mass and momentum."""
+    st = I.shock_plasma(nx, ny, nz, ppc=ppc, flow_gamma=3.0, theta_e=0.3, seed=seed)
+    for sp in st.species:
+        sp["px"][::3] = -sp["px"][::3]
+    conc, en, vel, rho = [], [], [], 0.0
+    for sp in st.species:
+        _, _, _, extra = O.run_reference(1, st.box, [dict(sp)], st.E, st.B, 0, density=True, wall_x=1,
+                                         e_right=st.e_right, b_right=st.b_right)
+        c, e, v, r = extra["density"]
+        conc.append(c[0]); en.append(e[0]); vel.append(v[0]); rho = rho + r
+    extra = dict(conc=np.array(conc), energy=np.array(en), vel=np.array(vel), rho=rho,
+                 wall=np.concatenate([np.asarray(st.e_right), np.asarray(st.b_right)]))
+    _save(name, 1, st, 0, [dict(x=sp["ox"], y=sp["oy"], z=sp["oz"], px=sp["px"], py=sp["py"], pz=sp["pz"])
+                           for sp in st.species], st.E, st.B, extra)
+
+
 def main():
     if not O.reference_available():
         sys.exit("the PIC++ reference tree is not available here (set PICPP_REFERENCE_SRC)")
@@ -135,6 +154,8 @@ def main():
     tristan_wall("tristan_wall_32x6x5_3steps", 32, 6, 5, (4, 3, 2), 3, 52)
     density("density_8x6x5", 8, 6, 5, 3, 31)
     density("density_2d_8x8x1", 8, 8, 1, 4, 32)
+    wall_density("density_wall_12x6x5", 12, 6, 5, (3, 3, 2), 61)
+    wall_density("density_wall_9x5x4", 9, 5, 4, (4, 3, 2), 62)
 
 
 if __name__ == "__main__":

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import pyoracle as O
-from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of
+from fixtures import copy_species, golden_names, load, periodic_dist, rel_err, smoothing_of, wall_of
 from picpp_gb300 import initstate as I
 
 pytestmark = pytest.mark.gpu
@@ -595,10 +595,14 @@ def test_implicit_solver_rejects_nonfinite_rhs(pg):
 @pytest.mark.parametrize("name", golden_names("density"))
 @pytest.mark.parametrize("real", [1, 0])
 def test_density_parameters_match_reference(pg, name, real):
-    """updateDensityParameters on the device against the reference's grids."""
+    """updateDensityParameters on the device against the reference's grids
+    (the density_wall cases in a reflecting-wall box, whose ghost columns
+    fold into the first and the last physical cell)."""
     f = load(name)
     st = f["state"]
-    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, sort_every=0)
+    wall, er, br = wall_of(f)
+    kw = dict(boundary_x=pg.BOUNDARY_WALL_OPEN, e_right=er, b_right=br, tile=(0, 0, 0)) if wall else {}
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, sort_every=0, **kw)
     sim.upload_state(st)
     sim.updateDensityParameters()
     x = f["extra"]

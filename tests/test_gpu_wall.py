@@ -267,6 +267,16 @@ def test_tristan_wall_steps_with_injection_match_oracle(pg, real, sort_every):
         for k in ("px", "py", "pz"):
             assert rel_err(got[k], ref[k]) < tol
     assert escaped > 0
+    # the density pass of the same wall box (reflected fold at the wall,
+    # open-boundary fold into the last cell)
+    sim.updateDensityParameters()
+    conc, en, vel, rho = O.density_moments(g, spo)
+    for s in range(len(spo)):
+        c, e, v, r = sim.download_density(s)
+        assert rel_err(c, conc[s]) < tol
+        assert rel_err(e, en[s]) < tol
+        assert rel_err(v, vel[s]) < tol
+    assert rel_err(r, rho) < tol
     sim.close()
 
 

@@ -173,6 +173,53 @@ __device__ __forceinline__ void add_slots_fx(unsigned* __restrict__ lo, int* __r
         if (use[q]) fx_add(lo, hi, off[q], a[q] * sc);
 }
 
+// Run heads whose totals one warp spreads over its lanes, and the per-warp
+// shared scratch that holds them (12 totals and the block cell of each head,
+// 16-byte aligned).
+constexpr int kSpreadHeads = 10;
+constexpr int kSpreadBytes = (kSpreadHeads * 12 * 4 + kSpreadHeads * 4 + 15) & ~15;
+
+// The fixed-point adds of one reduced segment: the run heads (head, key >= 0)
+// hold 12 totals each.  With at most kSpreadHeads heads in the warp (the
+// usual case: particles sorted by cell make runs of about the cell's
+// particle count) the heads park their scaled totals in the warp's scratch
+// and every lane adds about 12 heads / 32 of them, so that the conversion
+// and the two atomics of each add run on all lanes instead of on the heads
+// alone; with more heads each head adds its own.  Exact either way: the
+// fixed-point sums do not depend on the order of the adds.
+__device__ __forceinline__ void add_runs_fx(unsigned* __restrict__ lo, int* __restrict__ hi, int JC, int X0, int XY,
+                                            int ey, int ez, bool head, int key, const float a[12], float sc,
+                                            float* __restrict__ wv) {
+    const int lane = threadIdx.x & 31;
+    const bool mine = head && key >= 0;
+    const unsigned H = __ballot_sync(0xffffffffu, mine);
+    const int nh = __popc(H);
+    if (nh > kSpreadHeads) {
+        if (mine) add_slots_fx(lo, hi, JC, key, X0, XY, ey, ez, a, sc);
+        return;
+    }
+    int* wk = reinterpret_cast<int*>(wv + kSpreadHeads * 12);
+    if (mine) {
+        const int o = __popc(H & ((1u << lane) - 1u));
+        float4* d = reinterpret_cast<float4*>(wv + 12 * o);
+        d[0] = make_float4(a[0] * sc, a[1] * sc, a[2] * sc, a[3] * sc);
+        d[1] = make_float4(a[4] * sc, a[5] * sc, a[6] * sc, a[7] * sc);
+        d[2] = make_float4(a[8] * sc, a[9] * sc, a[10] * sc, a[11] * sc);
+        wk[o] = key;
+    }
+    __syncwarp();
+    // value v = 12 o + q: head o, slot q of segment_slots (component q / 4;
+    // bit 0 of q % 4 the first upper neighbour, bit 1 the second)
+    for (int v = lane; v < 12 * nh; v += 32) {
+        const int o = v / 12, q = v - 12 * o;
+        const int comp = q >> 2, sub = q & 3;
+        const int s1 = comp == 0 ? X0 : 1, s2 = comp == 2 ? X0 : XY;
+        const bool use = ((sub & 1) == 0 || comp != 0 || ey) && ((sub & 2) == 0 || (comp == 2 ? ey : ez));
+        if (use) fx_add(lo, hi, comp * JC + wk[o] + (sub & 1) * s1 + (sub >> 1) * s2, wv[v]);
+    }
+    __syncwarp();
+}
+
 // CT: compile-time tile extent of a cubic 3-D tile (8), or 0 for shapes read
 // from TileShape at run time.  kWall: conductor-wall box (GridP::wall), the
 // Tristan mover's reflection and escape and the zigzag wall term
@@ -195,6 +242,9 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
     TP* sJ = reinterpret_cast<TP*>(smem_raw + ((6 * F * sizeof(TF) + 15) & ~size_t(15)));   // 3 * JC (FP64)
     unsigned* sLo = reinterpret_cast<unsigned*>(sJ);                                        // 3 * JC (FP32)
     int* sHi = reinterpret_cast<int*>(sLo + 3 * JC);                                        // 3 * JC (FP32)
+    // FP32: the warps' spread scratch after the block
+    float* sW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(sJ) + ((24 * JC + 15) & ~15ll) +
+                                         (threadIdx.x >> 5) * kSpreadBytes);
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int T3 = tx * ty * tz;
     const long long N = g.N;
@@ -364,8 +414,8 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                 }
                 const bool crossed = __any_sync(0xffffffffu, keyA >= 0);
                 if constexpr (kFixed) {
-                    if (run_sum<TP>(keyB, aB) && keyB >= 0)
-                        add_slots_fx(sLo, sHi, (int)JC, keyB, jx, jx * jy, ey, ez, (const float*)aB, fx_scale);
+                    const bool hb = run_sum<TP>(keyB, aB);
+                    add_runs_fx(sLo, sHi, (int)JC, jx, jx * jy, ey, ez, hb, keyB, (const float*)aB, fx_scale, sW);
                 } else {
                     if (run_sum<TP>(keyB, aB) && keyB >= 0) add_slots<TP>(sJ, JC, keyB, jx, jx * jy, ey, ez, aB);
                 }
@@ -375,8 +425,8 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                     TP aA[12];
                     segment_slots<TP>(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], aA);
                     if constexpr (kFixed) {
-                        if (run_sum<TP>(keyA, aA) && keyA >= 0)
-                            add_slots_fx(sLo, sHi, (int)JC, keyA, jx, jx * jy, ey, ez, (const float*)aA, fx_scale);
+                        const bool ha = run_sum<TP>(keyA, aA);
+                        add_runs_fx(sLo, sHi, (int)JC, jx, jx * jy, ey, ez, ha, keyA, (const float*)aA, fx_scale, sW);
                     } else {
                         if (run_sum<TP>(keyA, aA) && keyA >= 0) add_slots<TP>(sJ, JC, keyA, jx, jx * jy, ey, ez, aA);
                     }

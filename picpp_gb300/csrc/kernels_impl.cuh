@@ -178,8 +178,10 @@ void PK<T>::zigzag(cudaStream_t s, const GridP& g, PartView<T> p, double q, doub
 template <typename T>
 size_t PK<T>::tile_smem_bytes(const TileShape& sh) {
     size_t F = (size_t)sh.fx * sh.fy * sh.fz;
-    // FP32: the current block is 64-bit fixed point in two 32-bit words
-    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + 3 * (size_t)sh.jcells * 8;
+    // FP32: the current block is 64-bit fixed point in two 32-bit words,
+    // followed by the warps' scratch for spreading the run heads' adds
+    const size_t fixed_scratch = sizeof(T) == 4 ? (size_t)(kTileThreads / 32) * kSpreadBytes : 0;
+    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + ((3 * (size_t)sh.jcells * 8 + 15) & ~size_t(15)) + fixed_scratch;
 }
 
 template <typename T>

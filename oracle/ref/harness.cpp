@@ -35,6 +35,7 @@
 #include <cmath>
 #include <vector>
 #include <algorithm>
+#include <chrono>
 #include <mpi.h>
 #include "simulation.h"
 #include "particle.h"
@@ -173,6 +174,7 @@ int main(int argc, char** argv) {
     S->updateParticlesBeta();
 
     std::vector<double> dJ, dMu, dRho, dPi, dRhs, dEt;
+    const auto t_loop = std::chrono::steady_clock::now();   // the step loop's wall time goes to stdout
     if (solver == 0) {
         S->exchangeBunemanBfield(S->bunemanBx, S->bunemanBy, S->bunemanBz);
         S->exchangeBunemanEfield(S->bunemanEx, S->bunemanEy, S->bunemanEz);
@@ -251,6 +253,9 @@ int main(int argc, char** argv) {
             S->currentIteration++;
         }
     }
+
+    printf("harness: %d steps in %.6f s\n", steps,
+           std::chrono::duration<double>(std::chrono::steady_clock::now() - t_loop).count());
 
     // collect particles back in input order (Particle::number)
     long total = base[ns];

@@ -28,6 +28,8 @@ struct Species {
     void* b[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int* perm = nullptr;
     int* off = nullptr;     // nkeys + 1
+    unsigned* defer = nullptr;   // 2 * dwords: the fused explicit kernel's push-later and deposit-later bits
+    long long dwords = 0;
     bool sorted = false;
     long long next_id = 0;  // id of the next appended particle when the caller gives none
 };
@@ -293,10 +295,12 @@ pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
                 S.p[q] = view<T>(ctx->sp[q]);
                 S.q[q] = T(ctx->sp[q].q); S.m[q] = T(ctx->sp[q].m); S.w[q] = T(ctx->sp[q].w);
                 S.off[q] = ctx->sp[q].off;
+                S.defer[q] = ctx->sp[q].defer;
+                S.dwords[q] = ctx->sp[q].dwords;
             }
             int grid = ctx->ntiles < kNumSM * 8 ? ctx->ntiles : kNumSM * 8;
             {
-                Phase ph(ctx, PIC_PHASE_PUSH_DEPOSIT, 1);
+                Phase ph(ctx, PIC_PHASE_PUSH_DEPOSIT, 2);   // the fused kernel and its deferred pass
                 PK<T>::push_deposit_tiled(s, g, ctx->tg, ctx->ts, S, ctx->E, ctx->B, (double*)ctx->Jpart, ctx->Jfix,
                                           grid, PK<T>::tile_smem_bytes(ctx->ts));
             }
@@ -600,7 +604,7 @@ pic_status pic_destroy(pic_ctx* ctx) {
     for (auto& sp : ctx->sp) {
         cudaFree(sp.cell); cudaFree(sp.id); cudaFree(sp.cell2); cudaFree(sp.id2);
         for (int q = 0; q < 6; ++q) { cudaFree(sp.a[q]); cudaFree(sp.b[q]); }
-        cudaFree(sp.perm); cudaFree(sp.off);
+        cudaFree(sp.perm); cudaFree(sp.off); cudaFree(sp.defer);
     }
     void* bufs[] = {ctx->E, ctx->B, ctx->J, ctx->Jfix, ctx->Jpart, ctx->Ei, ctx->Bi, ctx->Jh, ctx->mu, ctx->rho,
                     ctx->rho_ext, ctx->Pi, ctx->Jg, ctx->rhs, ctx->Et, ctx->En, ctx->Bn, ctx->key, ctx->counts,
@@ -639,6 +643,12 @@ pic_status pic_add_species(pic_ctx* ctx, double q, double m, double w, long capa
         CK(dalloc(&sp.b[a], ctx->rsz * n));
     }
     CK(dalloc(&sp.perm, sizeof(int) * n));
+    // one bit per particle and kind, plus the word a chunk that starts in the
+    // last one spills into; zero between steps (the deferred pass clears
+    // what it reads)
+    sp.dwords = ((long long)n + 31) / 32 + 1;
+    CK(dalloc(&sp.defer, sizeof(unsigned) * 2 * (size_t)sp.dwords));
+    CK(cudaMemsetAsync(sp.defer, 0, sizeof(unsigned) * 2 * (size_t)sp.dwords, ctx->s));
     CK(dalloc(&sp.off, sizeof(int) * ((size_t)ctx->nkeys + 1)));
     CK(cudaMemsetAsync(sp.off, 0, sizeof(int) * ((size_t)ctx->nkeys + 1), ctx->s));
     if ((long long)n > ctx->sort_cap) {

@@ -25,8 +25,12 @@
 //      FP32 particles the exact fixed-point sums).
 // k_assemble_j then sums the partials of every cell in a fixed order into
 // the FP64 current grid: no global floating-point atomics on the fast path.
-// A particle more than one cell outside its tile takes the global path
-// (global gather, FP64 global atomics into a correction grid).
+// A particle more than one cell outside its tile, or whose zigzag segments
+// leave the tile's current block, is left to k_push_deposit_deferred: the
+// fused kernel sets its bit in a per-species mask and the deferred pass
+// pushes it with the global gather and/or deposits its current with FP64
+// global atomics into a correction grid.  The fused kernel itself calls no
+// function out of line (a call site costs its hot loop register spills).
 #pragma once
 #include "boris.cuh"
 #include "types.cuh"
@@ -58,22 +62,23 @@ __device__ __forceinline__ TP tri(const TF* __restrict__ F, int base, int sy, in
     return lerp(a, b, wz);
 }
 
-// Global gather for particles far from their tile (out of line: rare).
-template <typename TP, typename TF>
-__device__ __noinline__ void gather_global(const GridP& g, int cell, TP ox, TP oy, TP oz, const TF* __restrict__ E,
-                                           const TF* __restrict__ B, TP* e, TP* b) {
-    yee_gather<TP, TF>(g, cell, ox, oy, oz, E, B, e, b);
-}
-
-// The 24 zigzag terms of a particle straight into the FP64 correction grid
-// (particles whose segments fall outside the shared block; rare).
+// The 24 zigzag terms of a particle straight into the FP64 correction grid.
 template <typename TP>
-__device__ __noinline__ void deposit_global(const GridP& g, TP fcd, TP ox, TP oy, TP oz, TP vx, TP vy, TP vz, int ni,
-                                            int nj, int nk, double* __restrict__ Jfix) {
-    const TP v[3] = {vx, vy, vz};
+__device__ __forceinline__ void deposit_global(const GridP& g, TP fcd, TP ox, TP oy, TP oz, const TP v[3], int ni,
+                                               int nj, int nk, double* __restrict__ Jfix) {
     zigzag_terms<TP>(g, fcd, ox, oy, oz, v, [&](int comp, int di, int dj, int dk, TP val) {
         atomicAdd(&Jfix[comp * g.N + linw(g, ni + di, nj + dj, nk + dk)], double(val));
     }, g.wall && ni == kTristanWallNode);
+}
+
+// Sets the bits of a warp's chunk of particles s0 .. s0 + 31 (bit l for
+// particle s0 + l) in a particle bit mask.
+__device__ __forceinline__ void set_defer_bits(unsigned* __restrict__ mask, long long s0, unsigned bits) {
+    if (!bits) return;
+    const long long w = s0 >> 5;
+    const int sh = (int)(s0 & 31);
+    atomicOr(&mask[w], bits << sh);
+    if (sh && (bits >> (32 - sh))) atomicOr(&mask[w + 1], bits >> (32 - sh));
 }
 
 // One zigzag segment's 12 terms relative to its cell
@@ -228,8 +233,7 @@ __device__ __forceinline__ void add_runs_fx(unsigned* __restrict__ lo, int* __re
 template <typename TP, typename TF, int CT, bool kWall>
 __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
                                                                        const TF* __restrict__ E, const TF* __restrict__ B,
-                                                                       double* __restrict__ Jpart, double* __restrict__ Jfix,
-                                                                       float fx_scale) {
+                                                                       double* __restrict__ Jpart, float fx_scale) {
     constexpr bool kFixed = sizeof(TP) == sizeof(float);   // FP32 particles: fixed-point block
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int fx = CT ? CT + 4 : s.fx, fy = CT ? CT + 4 : s.fy, fz = CT ? CT + 4 : s.fz;
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int T3 = tx * ty * tz;
     const long long N = g.N;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TP dt = TP(g.dt), idt = TP(1.0 / g.dt);
     const TP dx = TP(g.dx), dy = TP(g.dy), dz = TP(g.dz);
     const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
@@ -281,11 +285,13 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
             const TP beta = q * dt / (TP(2) * m);
             const TP fcd = q * S.w[sp] / vol;
             const long long pb = S.off[sp][(long long)tile * T3], pe = S.off[sp][(long long)(tile + 1) * T3];
-            for (long long base = pb + 32LL * warp; base < pe; base += 32LL * nwarps) {
-                const long long n = base + lane;
+            // CTA-uniform chunk loop: warp w takes particles cb + 32 w + lane
+            for (long long cb = pb; cb < pe; cb += blockDim.x) {
+                const long long n = cb + threadIdx.x;
                 TP aB[12];
                 TP s1[6] = {TP(0), TP(0), TP(0), TP(0), TP(0), TP(0)};   // F1 and W1 of the old-side segment
                 int keyA = -1 - lane, keyB = -1 - lane;   // lanes outside a reduction keep unique keys
+                bool push_later = false, deposit_later = false;
                 const int cell = n < pe ? P.cell[n] : -1;
                 // (an escaped particle of a wall box waits with cell -1 for the sort)
                 if (n < pe && (!kWall || cell >= 0)) {
@@ -303,8 +309,9 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                     const int lj = ey ? local(j, loy, ty, g.ny) : 0;
                     const int lk = ez ? local(k, loz, tz, g.nz) : 0;
                     const bool fast = li >= -1 && li <= tx && lj >= -ey && lj <= ty * ey && lk >= -ez && lk <= tz * ez;
-                    TP e3[3], b3[3];
+                    push_later = !fast;
                     if (fast) {
+                        TP e3[3], b3[3];
                         // upper-neighbour weights: node grids (c, c+1) with weight u;
                         // cell-centred grids (c-1, c) with u + 1/2 below the centre,
                         // (c, c+1) with u - 1/2 above it (correlation.cpp:471-496)
@@ -322,79 +329,87 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
                         b3[0] = tri<TP, TF>(sF + 3 * F, c0 + cys + czs, fsy, fsz, ox, wcy, wcz);
                         b3[1] = tri<TP, TF>(sF + 4 * F, c0 + cxs + czs, fsy, fsz, wcx, wny, wcz);
                         b3[2] = tri<TP, TF>(sF + 5 * F, c0 + cxs + cys, fsy, fsz, wcx, wcy, wnz);
-                    } else {
-                        gather_global<TP, TF>(g, cell, ox, oy, oz, E, B, e3, b3);
+                        boris_t<TP>(q, m, dt, beta, e3, b3, mom);
+                        TP v[3];
+                        velocity_t<TP>(mom, m, v);
+                        int ni = i, nj = j, nk = k;
+                        int wall_r = 0;
+                        if constexpr (kWall) {
+                            wall_r = tristan_wall_x<TP>(g, ni, ox, (v[0] * dt) * idx);
+                            if (wall_r & 1) { mom[0] = -mom[0]; v[0] = -v[0]; }   // reflectMomentumX
+                        } else {
+                            advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
+                        }
+                        advance_axis<TP>(oy, nj, (v[1] * dt) * idy, g.ny);
+                        advance_axis<TP>(oz, nk, (v[2] * dt) * idz, g.nz);
+                        P.px[n] = mom[0]; P.py[n] = mom[1]; P.pz[n] = mom[2];
+                        P.ox[n] = ox; P.oy[n] = oy; P.oz[n] = oz;
+                        auto shift = [](int nw, int old, int nn) {
+                            int d = nw - old;
+                            if (d > 1) d -= nn;
+                            if (d < -1) d += nn;
+                            return d;
+                        };
+                        // block cell of the new position (a wall box has no x
+                        // wrap; a particle reflected from left of the wall may
+                        // land far from its old cell and is deposited by the
+                        // deferred pass)
+                        const int sxw = kWall ? ni - i : shift(ni, i, g.nx);
+                        const bool nearx = !kWall || (sxw >= -1 && sxw <= 1);
+                        const int bx = li + sxw + hx;
+                        const int by = (ey ? lj + shift(nj, j, g.ny) : 0) + hy;
+                        const int bz = (ez ? lk + shift(nk, k, g.nz) : 0) + hz;
+                        // zigzag split (zig_axis, momentum_collecting.cpp:91-221) in the
+                        // new cell's frame: old position P, relay R, relay shift r
+                        const TP X = ox * dx, Y = oy * dy, Z = oz * dz;
+                        TP PX = X - v[0] * dt;
+                        const TP PY = Y - v[1] * dt, PZ = Z - v[2] * dt;
+                        if constexpr (kWall) {
+                            if (ni == kTristanWallNode && v[0] > TP(0) && PX < TP(0)) PX = -PX;
+                        }
+                        const int rx = (int)dev_floor(divd<TP>(PX, dx, idx));
+                        const int ry = ey ? (int)dev_floor(divd<TP>(PY, dy, idy)) : 0;
+                        const int rz = ez ? (int)dev_floor(divd<TP>(PZ, dz, idz)) : 0;
+                        const TP RX = rx == 0 ? (X + PX) / TP(2) : TP(rx > 0 ? rx : 0) * dx;
+                        const TP RY = ry == 0 ? (Y + PY) / TP(2) : TP(ry > 0 ? ry : 0) * dy;
+                        const TP RZ = rz == 0 ? (Z + PZ) / TP(2) : TP(rz > 0 ? rz : 0) * dz;
+                        const int ax = bx + rx, ay = by + ry, az = bz + rz;   // block cell of the old-side segment
+                        // unsigned compares: (unsigned)x < n is 0 <= x < n
+                        const bool inblock = nearx && (unsigned)(rx + 1) <= 2u && (unsigned)(ry + 1) <= 2u &&
+                                             (unsigned)(rz + 1) <= 2u && (unsigned)ax < (unsigned)(jx - 1) &&
+                                             (unsigned)bx < (unsigned)(jx - 1) && (unsigned)ay < (unsigned)(jy - ey) &&
+                                             (unsigned)by < (unsigned)(jy - ey) && (unsigned)az < (unsigned)(jz - ez) &&
+                                             (unsigned)bz < (unsigned)(jz - ez);
+                        if (inblock) {
+                            const TP F1x = divd<TP>(fcd * (RX - PX), dt, idt);
+                            const TP F1y = divd<TP>(fcd * (RY - PY), dt, idt);
+                            const TP F1z = divd<TP>(fcd * (RZ - PZ), dt, idt);
+                            const TP F2x = divd<TP>(fcd * (X - RX), dt, idt);
+                            const TP F2y = fcd * v[1] - F1y, F2z = fcd * v[2] - F1z;
+                            const TP hxx = TP(0.5) * idx, hyy = TP(0.5) * idy, hzz = TP(0.5) * idz;
+                            const TP W1x = divd<TP>(PX + RX, TP(2) * dx, hxx) - TP(rx);
+                            const TP W1y = ey ? divd<TP>(PY + RY, TP(2) * dy, hyy) - TP(ry) : TP(0);
+                            const TP W1z = ez ? divd<TP>(PZ + RZ, TP(2) * dz, hzz) - TP(rz) : TP(0);
+                            const TP W2x = divd<TP>(X + RX, TP(2) * dx, hxx);
+                            const TP W2y = ey ? divd<TP>(Y + RY, TP(2) * dy, hyy) : TP(0);
+                            const TP W2z = ez ? divd<TP>(Z + RZ, TP(2) * dz, hzz) : TP(0);
+                            segment_slots<TP>(F2x, F2y, F2z, W2x, W2y, W2z, aB);
+                            s1[0] = F1x; s1[1] = F1y; s1[2] = F1z; s1[3] = W1x; s1[4] = W1y; s1[5] = W1z;
+                            keyA = (az * jy + ay) * jx + ax;
+                            keyB = (bz * jy + by) * jx + bx;
+                        }
+                        deposit_later = !inblock;
+                        // an escaped particle is marked once its current is
+                        // deposited (the deferred pass marks its own)
+                        P.cell[n] = ((wall_r & 2) && inblock) ? -1 : (int)lin(g, ni, nj, nk);
                     }
-                    boris_t<TP>(q, m, dt, beta, e3, b3, mom);
-                    TP v[3];
-                    velocity_t<TP>(mom, m, v);
-                    int ni = i, nj = j, nk = k;
-                    int wall_r = 0;
-                    if constexpr (kWall) {
-                        wall_r = tristan_wall_x<TP>(g, ni, ox, (v[0] * dt) * idx);
-                        if (wall_r & 1) { mom[0] = -mom[0]; v[0] = -v[0]; }   // reflectMomentumX
-                    } else {
-                        advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
-                    }
-                    advance_axis<TP>(oy, nj, (v[1] * dt) * idy, g.ny);
-                    advance_axis<TP>(oz, nk, (v[2] * dt) * idz, g.nz);
-                    P.px[n] = mom[0]; P.py[n] = mom[1]; P.pz[n] = mom[2];
-                    P.ox[n] = ox; P.oy[n] = oy; P.oz[n] = oz;
-                    P.cell[n] = (wall_r & 2) ? -1 : (int)lin(g, ni, nj, nk);
-                    auto shift = [](int nw, int old, int nn) {
-                        int d = nw - old;
-                        if (d > 1) d -= nn;
-                        if (d < -1) d += nn;
-                        return d;
-                    };
-                    // block cell of the new position (a wall box has no x
-                    // wrap; a particle reflected from left of the wall may
-                    // land far from its old cell and takes the global path)
-                    const int sxw = kWall ? ni - i : shift(ni, i, g.nx);
-                    const bool nearx = !kWall || (sxw >= -1 && sxw <= 1);
-                    const int bx = li + sxw + hx;
-                    const int by = (ey ? lj + shift(nj, j, g.ny) : 0) + hy;
-                    const int bz = (ez ? lk + shift(nk, k, g.nz) : 0) + hz;
-                    // zigzag split (zig_axis, momentum_collecting.cpp:91-221) in the
-                    // new cell's frame: old position P, relay R, relay shift r
-                    const TP X = ox * dx, Y = oy * dy, Z = oz * dz;
-                    TP PX = X - v[0] * dt;
-                    const TP PY = Y - v[1] * dt, PZ = Z - v[2] * dt;
-                    if constexpr (kWall) {
-                        if (ni == kTristanWallNode && v[0] > TP(0) && PX < TP(0)) PX = -PX;
-                    }
-                    const int rx = (int)dev_floor(divd<TP>(PX, dx, idx));
-                    const int ry = ey ? (int)dev_floor(divd<TP>(PY, dy, idy)) : 0;
-                    const int rz = ez ? (int)dev_floor(divd<TP>(PZ, dz, idz)) : 0;
-                    const TP RX = rx == 0 ? (X + PX) / TP(2) : TP(rx > 0 ? rx : 0) * dx;
-                    const TP RY = ry == 0 ? (Y + PY) / TP(2) : TP(ry > 0 ? ry : 0) * dy;
-                    const TP RZ = rz == 0 ? (Z + PZ) / TP(2) : TP(rz > 0 ? rz : 0) * dz;
-                    const int ax = bx + rx, ay = by + ry, az = bz + rz;   // block cell of the old-side segment
-                    // unsigned compares: (unsigned)x < n is 0 <= x < n
-                    const bool inblock = fast && nearx && (unsigned)(rx + 1) <= 2u && (unsigned)(ry + 1) <= 2u &&
-                                         (unsigned)(rz + 1) <= 2u && (unsigned)ax < (unsigned)(jx - 1) &&
-                                         (unsigned)bx < (unsigned)(jx - 1) && (unsigned)ay < (unsigned)(jy - ey) &&
-                                         (unsigned)by < (unsigned)(jy - ey) && (unsigned)az < (unsigned)(jz - ez) &&
-                                         (unsigned)bz < (unsigned)(jz - ez);
-                    if (inblock) {
-                        const TP F1x = divd<TP>(fcd * (RX - PX), dt, idt);
-                        const TP F1y = divd<TP>(fcd * (RY - PY), dt, idt);
-                        const TP F1z = divd<TP>(fcd * (RZ - PZ), dt, idt);
-                        const TP F2x = divd<TP>(fcd * (X - RX), dt, idt);
-                        const TP F2y = fcd * v[1] - F1y, F2z = fcd * v[2] - F1z;
-                        const TP hxx = TP(0.5) * idx, hyy = TP(0.5) * idy, hzz = TP(0.5) * idz;
-                        const TP W1x = divd<TP>(PX + RX, TP(2) * dx, hxx) - TP(rx);
-                        const TP W1y = ey ? divd<TP>(PY + RY, TP(2) * dy, hyy) - TP(ry) : TP(0);
-                        const TP W1z = ez ? divd<TP>(PZ + RZ, TP(2) * dz, hzz) - TP(rz) : TP(0);
-                        const TP W2x = divd<TP>(X + RX, TP(2) * dx, hxx);
-                        const TP W2y = ey ? divd<TP>(Y + RY, TP(2) * dy, hyy) : TP(0);
-                        const TP W2z = ez ? divd<TP>(Z + RZ, TP(2) * dz, hzz) : TP(0);
-                        segment_slots<TP>(F2x, F2y, F2z, W2x, W2y, W2z, aB);
-                        s1[0] = F1x; s1[1] = F1y; s1[2] = F1z; s1[3] = W1x; s1[4] = W1y; s1[5] = W1z;
-                        keyA = (az * jy + ay) * jx + ax;
-                        keyB = (bz * jy + by) * jx + bx;
-                    } else {
-                        deposit_global<TP>(g, fcd, ox, oy, oz, v[0], v[1], v[2], ni, nj, nk, Jfix);
+                }
+                {
+                    const unsigned mp = __ballot_sync(0xffffffffu, push_later);
+                    const unsigned md = __ballot_sync(0xffffffffu, deposit_later);
+                    if ((mp | md) && lane == 0) {
+                        set_defer_bits(S.defer[sp], cb + 32LL * warp, mp);
+                        set_defer_bits(S.defer[sp] + S.dwords[sp], cb + 32LL * warp, md);
                     }
                 }
                 if (keyB < 0) {
@@ -447,6 +462,71 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
             for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) dst[e] = sJ[e];
         }
         __syncthreads();
+    }
+}
+
+// The particles k_push_deposit_tile left over, by their mask bits (each
+// word read once and cleared for the next step):
+//   * push-later (more than one cell outside their tile): the same gather
+//     from global memory, Boris push and move, then the zigzag current;
+//   * deposit-later (pushed there, segments outside the tile's current
+//     block): the zigzag current of the stored new position and velocity.
+// The current goes into Jfix with FP64 global atomics; a particle that left a
+// wall box is marked (cell -1) once its current is in.
+template <typename TP, typename TF>
+__global__ void __launch_bounds__(256) k_push_deposit_deferred(GridP g, SpeciesSet<TP> S, const TF* __restrict__ E,
+                                                               const TF* __restrict__ B, double* __restrict__ Jfix) {
+    const TP dt = TP(g.dt);
+    const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
+    const TP vol = TP(g.dx) * TP(g.dy) * TP(g.dz);
+    for (int sp = 0; sp < S.ns; ++sp) {
+        const PartView<TP> P = S.p[sp];
+        const TP q = S.q[sp], m = S.m[sp];
+        const TP beta = q * dt / (TP(2) * m);
+        const TP fcd = q * S.w[sp] / vol;
+        unsigned* mp = S.defer[sp];
+        unsigned* md = mp + S.dwords[sp];
+        const long long words = (P.n + 31) / 32 + 1;
+        for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < words;
+             w += (long long)gridDim.x * blockDim.x) {
+            unsigned bp = mp[w], bd = md[w];
+            if (!(bp | bd)) continue;
+            mp[w] = 0u;
+            md[w] = 0u;
+            while (bp | bd) {
+                const bool push = bp != 0u;
+                unsigned& bits = push ? bp : bd;
+                const long long n = w * 32 + (__ffs(bits) - 1);
+                bits &= bits - 1u;
+                TP ox = P.ox[n], oy = P.oy[n], oz = P.oz[n];
+                TP mom[3] = {P.px[n], P.py[n], P.pz[n]};
+                int ni, nj, nk;
+                decode(g, P.cell[n], ni, nj, nk);
+                TP v[3];
+                if (push) {
+                    TP e3[3], b3[3];
+                    yee_gather<TP, TF>(g, P.cell[n], ox, oy, oz, E, B, e3, b3);
+                    boris_t<TP>(q, m, dt, beta, e3, b3, mom);
+                    velocity_t<TP>(mom, m, v);
+                    if (g.wall) {
+                        if (tristan_wall_x<TP>(g, ni, ox, (v[0] * dt) * idx) & 1) {   // reflectMomentumX
+                            mom[0] = -mom[0];
+                            v[0] = -v[0];
+                        }
+                    } else {
+                        advance_axis<TP>(ox, ni, (v[0] * dt) * idx, g.nx);
+                    }
+                    advance_axis<TP>(oy, nj, (v[1] * dt) * idy, g.ny);
+                    advance_axis<TP>(oz, nk, (v[2] * dt) * idz, g.nz);
+                    P.px[n] = mom[0]; P.py[n] = mom[1]; P.pz[n] = mom[2];
+                    P.ox[n] = ox; P.oy[n] = oy; P.oz[n] = oz;
+                } else {
+                    velocity_t<TP>(mom, m, v);
+                }
+                deposit_global<TP>(g, fcd, ox, oy, oz, v, ni, nj, nk, Jfix);
+                P.cell[n] = (g.wall && tristan_escaped<TP>(g, ni, ox)) ? -1 : (int)lin(g, ni, nj, nk);
+            }
+        }
     }
 }
 

@@ -208,13 +208,17 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
     // a wall box runs its own instantiation (run-time tile shape)
     if (g.wall)
         k_push_deposit_tile<T, T, 0, true><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
-                                                                           Jfix, fx_scale);
+                                                                           fx_scale);
     else if (cube8)
         k_push_deposit_tile<T, T, 8, false><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
-                                                                            Jfix, fx_scale);
+                                                                            fx_scale);
     else
         k_push_deposit_tile<T, T, 0, false><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
-                                                                            Jfix, fx_scale);
+                                                                            fx_scale);
+    // the particles it left over: one thread per mask word
+    long long words = 1;
+    for (int q = 0; q < S.ns; ++q) words = std::max(words, (S.p[q].n + 31) / 32 + 1);
+    k_push_deposit_deferred<T, T><<<grid_for(words, 256), 256, 0, s>>>(g, S, (const T*)E, (const T*)B, Jfix);
 }
 
 template <typename T>

@@ -35,6 +35,11 @@ struct SpeciesSet {
     PartView<TP> p[kMaxSpecies];
     TP q[kMaxSpecies], m[kMaxSpecies], w[kMaxSpecies];
     const int* off[kMaxSpecies];   // per-species sort offsets (nkeys + 1)
+    // per species: the particles the fused explicit kernel leaves to its
+    // deferred pass, one bit each -- dwords words of push-later bits, then
+    // dwords words of deposit-later bits
+    unsigned* defer[kMaxSpecies];
+    long long dwords[kMaxSpecies];
     int ns;
 };
 

@@ -161,6 +161,37 @@ def test_buneman_sort_cadence_does_not_change_results(pg):
         assert rel_err(B, out[0][1]) < TOL64
 
 
+@pytest.mark.parametrize("real,tol", [(1, TOL64), (0, TOL32)])
+def test_buneman_far_drift_takes_the_deferred_pass(pg, real, tol):
+    """A beam at |p_x| = 5 m c (0.44 cells per step) sorted every eighth step:
+    after the third step since a sort most particles lie more than a cell
+    outside their tile, and segments leave the tiles' current blocks, so the
+    fused kernel leaves them to its deferred pass (global gather, FP64 global
+    atomics).  Fields, current and particles after 8 steps against the
+    oracle."""
+    st = noisy(I.buneman_plasma(16, 8, 8, ppc=3, seed=39))
+    for sp in st.species:
+        sign = np.where(np.arange(len(sp["px"])) % 2 == 0, 1.0, -1.0)
+        sp["px"] = sign * 5.0 * sp["m"] + 0.1 * sp["px"]
+    steps = 8 if real else 3
+    sim = pg.GpuSimulation(st.box, pg.BUNEMAN, particle_real=real, sort_every=8, tile=(4, 4, 4))
+    sim.upload_state(st)
+    sim.buneman_step(steps)
+    E, B, J = sim.download_fields()
+    sp, Eo, Bo, Jo = oracle_buneman(st, steps)
+    assert rel_err(E, Eo) < tol
+    assert rel_err(B, Bo) < tol
+    assert rel_err(J, Jo.reshape(J.shape)) < tol
+    L = (st.box.nx * st.box.dx, st.box.ny * st.box.dy, st.box.nz * st.box.dz)
+    for s in range(2):
+        got = by_id(sim.download_particles(s))   # oracle particles stay in input order
+        x, _, _ = I.positions(st.box, got)
+        xr, _, _ = I.positions(st.box, sp[s])
+        assert periodic_dist(x, xr, L[0]).max() < (1e-11 if real else 1e-5) * L[0]
+        for k in ("px", "py", "pz"):
+            assert rel_err(got[k], sp[s][k]) < tol
+
+
 def test_buneman_reduced_dimension_matches_oracle(pg):
     st = noisy(I.buneman_plasma(16, 8, 1, ppc=4, seed=34))
     for sort_every in (0, 1):

@@ -412,7 +412,8 @@ pic_status implicit_moments(pic_ctx* ctx) {
 
 template <typename T>
 pic_status implicit_move(pic_ctx* ctx) {
-    Phase ph(ctx, PIC_PHASE_MOVER, (int)ctx->sp.size());
+    // the tiled mover and its deferred pass, or one untiled launch per species
+    Phase ph(ctx, PIC_PHASE_MOVER, all_sorted(ctx) ? 2 : (int)ctx->sp.size());
     bool tiled = false;
     if (all_sorted(ctx)) {
         ImpSpecies<T> S{};
@@ -421,6 +422,7 @@ pic_status implicit_move(pic_ctx* ctx) {
             S.p[q] = view<T>(ctx->sp[q]);
             S.q[q] = ctx->sp[q].q; S.m[q] = ctx->sp[q].m; S.w[q] = ctx->sp[q].w;
             S.off[q] = ctx->sp[q].off;
+            S.defer[q] = ctx->sp[q].defer;
         }
         tiled = PK<T>::implicit_push_tiled(ctx->s, ctx->g, ctx->tg, S, ctx->Ei, ctx->Bi, ctx->Et);
     }

@@ -221,121 +221,175 @@ __device__ __forceinline__ void evaluate_velocity(const T p[3], T m, T v[3]) {
     }
 }
 
-// moveParticle (PIC++/mover.cpp:194-491), periodic box: predictor and up to
-// three Picard iterations re-gathering E^{n+theta} (nodes) and B^n (cells).
-// alpha is recomputed from E^n, B^n at x^n (what evaluateParticlesRotationTensor
-// stored, mover.cpp:810-841).
+// Constants of the implicit mover for one species.
+template <typename T>
+struct MoverConst {
+    T beta, edt, dt, eta, qdt, mm, dxT, redt;
+    T id[3];
+    int nn[3];
+};
+template <typename T>
+__device__ __forceinline__ MoverConst<T> mover_const(const GridP& g, double q, double m) {
+    MoverConst<T> c;
+    c.beta = T(0.5 * q * g.dt / m);
+    c.edt = T(g.eta * g.dt);
+    c.dt = T(g.dt);
+    c.eta = T(g.eta);
+    c.qdt = T(q * g.dt);
+    c.mm = T(m);
+    c.dxT = T(g.dx);
+    c.redt = T((1.0 - g.eta) * g.dt);
+    c.id[0] = T(1.0 / g.dx); c.id[1] = T(1.0 / g.dy); c.id[2] = T(1.0 / g.dz);
+    c.nn[0] = g.nx; c.nn[1] = g.ny; c.nn[2] = g.nz;
+    return c;
+}
+
+// moveParticle (PIC++/mover.cpp:194-491) of particle n: predictor and up to
+// three Picard iterations re-gathering E^{n+theta} (nodes) and B^n (cells)
+// from the FP64 grids.  alpha is recomputed from E^n, B^n at x^n (what
+// evaluateParticlesRotationTensor stored, mover.cpp:810-841).
+template <typename T, bool kWall>
+__device__ __forceinline__ void implicit_move_particle(const GridP& g, const PartView<T>& p, long long n,
+                                                       const MoverConst<T>& c, const double* __restrict__ E,
+                                                       const double* __restrict__ B,
+                                                       const double* __restrict__ Et) {
+    const T beta = c.beta, edt = c.edt, dt = c.dt, eta = c.eta, qdt = c.qdt, mm = c.mm, dxT = c.dxT, redt = c.redt;
+    const T id[3] = {c.id[0], c.id[1], c.id[2]};
+    const int nn[3] = {c.nn[0], c.nn[1], c.nn[2]};
+    int ci[3];
+    decode(g, p.cell[n], ci[0], ci[1], ci[2]);
+    T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
+    T mom0[3] = {p.px[n], p.py[n], p.pz[n]};
+    T gam, v[3];
+    gamma_vel<T>(mom0, mm, gam, v);
+    T e[3], b[3], al[9];
+    gather_node<T>(g, ci[0], ci[1], ci[2], u0[0], u0[1], u0[2], E, e);
+    gather_cell<T>(g, ci[0], ci[1], ci[2], u0[0], u0[1], u0[2], B, b);
+    alpha_tensor<T>(beta, v, gam, e, b, al);
+    gather_node<T>(g, ci[0], ci[1], ci[2], u0[0], u0[1], u0[2], Et, e);
+    // b already holds B^n at x^n
+    T vxb[3] = {v[1] * b[2] - v[2] * b[1], -v[0] * b[2] + v[2] * b[0], v[0] * b[1] - v[1] * b[0]};
+    T pnew[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + vxb[d]) * qdt;
+    T vnew[3];
+    evaluate_velocity<T>(pnew, mm, vnew);
+    T mv[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
+    if constexpr (kWall) {
+        if (wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
+            wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+            p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+            p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+            p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+            return;
+        }
+    }
+    T vh[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
+    const T momNorm = picard_norm<T>(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
+    T err = picard_norm<T>((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
+                     (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
+    const T dxN = picard_ref<T>(dxT);
+    T cerr = dxN;
+    T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
+    T prevDisp[3];
+    int it = 0;
+    bool reflected = false;
+    while (picard_continue<T>(err, momNorm, cerr, dxN, it)) {
+        ++it;
+        T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) prevDisp[d] = newDisp[d];
+        T re[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) re[a] = al[3 * a] * e[0] + al[3 * a + 1] * e[1] + al[3 * a + 2] * e[2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
+        if constexpr (kWall) {
+            if (wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
+                wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
+                reflected = true;
+                break;
+            }
+        }
+        int tc[3];
+        T tu[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            tc[d] = ci[d]; tu[d] = u0[d];
+            advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
+        }
+        gather_node<T>(g, tc[0], tc[1], tc[2], tu[0], tu[1], tu[2], Et, e);
+        gather_cell<T>(g, tc[0], tc[1], tc[2], tu[0], tu[1], tu[2], B, b);
+        T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
+        err = picard_norm<T>((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) + (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
+                       (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
+        cerr = picard_norm<T>((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
+                        (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
+                        (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
+    }
+    if (!reflected) {
+        if constexpr (kWall) {
+            const int o = wall_final_x<T>(g, ci[0], u0[0], (mv[0] * dt) * id[0]);
+            if (o == 2) { p.cell[n] = -1; return; }   // escaped through the open boundary
+            if (o == 1) pnew[0] = -pnew[0];
+#pragma unroll
+            for (int d = 1; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
+        }
+    }
+    p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
+    p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
+    p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
+}
+
+// The mover over every particle of one species (periodic or wall box).
 template <typename T, bool kWall>
 __global__ void __launch_bounds__(128) k_implicit_push(GridP g, PartView<T> p, double q, double m,
                                                        const double* __restrict__ E, const double* __restrict__ B,
                                                        const double* __restrict__ Et) {
-    const T beta = T(0.5 * q * g.dt / m);
-    const T edt = T(g.eta * g.dt);
-    const T dt = T(g.dt), eta = T(g.eta);
-    const T qdt = T(q * g.dt);
-    const T mm = T(m);
-    const T id[3] = {T(1.0 / g.dx), T(1.0 / g.dy), T(1.0 / g.dz)};
-    const int nn[3] = {g.nx, g.ny, g.nz};
-    const T dxT = T(g.dx);
-    const T redt = T((1.0 - g.eta) * g.dt);
+    const MoverConst<T> c = mover_const<T>(g, q, m);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n;
          n += (long long)gridDim.x * blockDim.x) {
         if (p.cell[n] < 0) continue;   // escaped, erased by the next sort
-        int ci[3];
-        decode(g, p.cell[n], ci[0], ci[1], ci[2]);
-        T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
-        T mom0[3] = {p.px[n], p.py[n], p.pz[n]};
-        T gam, v[3];
-        gamma_vel<T>(mom0, mm, gam, v);
-        T e[3], b[3], al[9];
-        gather_node<T>(g, ci[0], ci[1], ci[2], u0[0], u0[1], u0[2], E, e);
-        gather_cell<T>(g, ci[0], ci[1], ci[2], u0[0], u0[1], u0[2], B, b);
-        alpha_tensor<T>(beta, v, gam, e, b, al);
-        gather_node<T>(g, ci[0], ci[1], ci[2], u0[0], u0[1], u0[2], Et, e);
-        // b already holds B^n at x^n
-        T vxb[3] = {v[1] * b[2] - v[2] * b[1], -v[0] * b[2] + v[2] * b[0], v[0] * b[1] - v[1] * b[0]};
-        T pnew[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + vxb[d]) * qdt;
-        T vnew[3];
-        evaluate_velocity<T>(pnew, mm, vnew);
-        T mv[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) mv[d] = v[d] * (T(1) - eta) + vnew[d] * eta;
-        if constexpr (kWall) {
-            if (wall_left_of<T>(ci[0], u0[0], (mv[0] * edt) * id[0])) {
-                wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
-                p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
-                p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
-                p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
-                continue;
+        implicit_move_particle<T, kWall>(g, p, n, c, E, B, Et);
+    }
+}
+
+// The particles the tiled mover left over (a position it had to gather at
+// lay outside its staged block), by the bits of S.defer: one thread per mask
+// word, each word read once and cleared for the next step.
+template <typename T, bool kWall>
+__global__ void __launch_bounds__(128) k_implicit_push_deferred(GridP g, ImpSpecies<T> S,
+                                                                const double* __restrict__ E,
+                                                                const double* __restrict__ B,
+                                                                const double* __restrict__ Et) {
+    for (int s = 0; s < S.ns; ++s) {
+        const PartView<T> p = S.p[s];
+        const MoverConst<T> c = mover_const<T>(g, S.q[s], S.m[s]);
+        unsigned* mask = S.defer[s];
+        const long long words = (p.n + 31) / 32;
+        for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < words;
+             w += (long long)gridDim.x * blockDim.x) {
+            unsigned bits = mask[w];
+            if (!bits) continue;
+            mask[w] = 0u;
+            while (bits) {
+                const long long n = w * 32 + (__ffs(bits) - 1);
+                bits &= bits - 1u;
+                implicit_move_particle<T, kWall>(g, p, n, c, E, B, Et);
             }
         }
-        T vh[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-            vh[a] = (al[3 * a] * gam) * v[0] + (al[3 * a + 1] * gam) * v[1] + (al[3 * a + 2] * gam) * v[2];
-        const T momNorm = picard_norm<T>(mom0[0] * mom0[0] + mom0[1] * mom0[1] + mom0[2] * mom0[2]);
-        T err = picard_norm<T>((mom0[0] - pnew[0]) * (mom0[0] - pnew[0]) + (mom0[1] - pnew[1]) * (mom0[1] - pnew[1]) +
-                         (mom0[2] - pnew[2]) * (mom0[2] - pnew[2]));
-        const T dxN = picard_ref<T>(dxT);
-        T cerr = dxN;
-        T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
-        T prevDisp[3];
-        int it = 0;
-        bool reflected = false;
-        while (picard_continue<T>(err, momNorm, cerr, dxN, it)) {
-            ++it;
-            T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
-#pragma unroll
-            for (int d = 0; d < 3; ++d) prevDisp[d] = newDisp[d];
-            T re[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) re[a] = al[3 * a] * e[0] + al[3 * a + 1] * e[1] + al[3 * a + 2] * e[2];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) mv[d] = vh[d] + re[d] * beta;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) newDisp[d] = mv[d] * edt;
-            if constexpr (kWall) {
-                if (wall_left_of<T>(ci[0], u0[0], newDisp[0] * id[0])) {
-                    wall_reflect_trial<T>(g, ci, u0, mv, vnew, mm, edt, redt, id, pnew);
-                    reflected = true;
-                    break;
-                }
-            }
-            int tc[3];
-            T tu[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                tc[d] = ci[d]; tu[d] = u0[d];
-                advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
-            }
-            gather_node<T>(g, tc[0], tc[1], tc[2], tu[0], tu[1], tu[2], Et, e);
-            gather_cell<T>(g, tc[0], tc[1], tc[2], tu[0], tu[1], tu[2], B, b);
-            T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
-#pragma unroll
-            for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
-            err = picard_norm<T>((prevMom[0] - pnew[0]) * (prevMom[0] - pnew[0]) + (prevMom[1] - pnew[1]) * (prevMom[1] - pnew[1]) +
-                           (prevMom[2] - pnew[2]) * (prevMom[2] - pnew[2]));
-            cerr = picard_norm<T>((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
-                            (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
-                            (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
-        }
-        if (!reflected) {
-            if constexpr (kWall) {
-                const int o = wall_final_x<T>(g, ci[0], u0[0], (mv[0] * dt) * id[0]);
-                if (o == 2) { p.cell[n] = -1; continue; }   // escaped through the open boundary
-                if (o == 1) pnew[0] = -pnew[0];
-#pragma unroll
-                for (int d = 1; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
-            } else {
-#pragma unroll
-                for (int d = 0; d < 3; ++d) advance_axis<T>(u0[d], ci[d], (mv[d] * dt) * id[d], nn[d]);
-            }
-        }
-        p.px[n] = pnew[0]; p.py[n] = pnew[1]; p.pz[n] = pnew[2];
-        p.ox[n] = u0[0]; p.oy[n] = u0[1]; p.oz[n] = u0[2];
-        p.cell[n] = (int)lin(g, ci[0], ci[1], ci[2]);
     }
 }
 

@@ -304,7 +304,7 @@ __device__ __forceinline__ void imp_deposit_direct(const T row[kScrRow], double 
 // All 8 node and 8 cell contributions of one particle to the FP64 grids
 // (particles outside the tile's block; rare).
 template <typename T>
-__device__ __noinline__ void imp_deposit_global(const GridP& g, int i, int j, int k, T ox, T oy, T oz,
+__device__ __noinline__ void imp_deposit_global(const GridP g, int i, int j, int k, T ox, T oy, T oz,
                                                 const double* QN, const double* QC, double* __restrict__ J,
                                                 double* __restrict__ mu, double* __restrict__ rho,
                                                 double* __restrict__ Pi) {
@@ -338,11 +338,19 @@ __device__ __noinline__ void imp_deposit_global(const GridP& g, int i, int j, in
 
 // Global trilinear gathers of E (nodes) and B (cells), out of line for the
 // staged kernel, where a particle outside its tile cannot occur after a sort.
+// The grid in and the six components out by value: an address taken of the
+// caller's arrays would send their every store to the stack.
 template <typename T>
-__device__ __noinline__ void gather_eb_global(const GridP& g, int i, int j, int k, T ox, T oy, T oz,
-                                              const T* __restrict__ E, const T* __restrict__ B, T* e, T* b) {
-    gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
-    gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, b);
+struct EB6 {
+    T e[3], b[3];
+};
+template <typename T>
+__device__ __noinline__ EB6<T> gather_eb_global(const GridP g, int i, int j, int k, T ox, T oy, T oz,
+                                                const T* __restrict__ E, const T* __restrict__ B) {
+    EB6<T> r;
+    gather_node<T, T>(g, i, j, k, ox, oy, oz, E, r.e);
+    gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, r.b);
+    return r;
 }
 
 // E and B come in the particle precision (FP32 copies for the FP32 path:
@@ -464,7 +472,9 @@ __global__ void __launch_bounds__(imp_threads<T>(), 2) k_implicit_deposit_tile(G
                                 bf[c] = tri_block<T>(sB + c * bk.CB, cbase, oxc, oyc, ozc, ux, uy, uz);
                             }
                         } else if (kStaged) {
-                            gather_eb_global<T>(g, i, j, k, ox, oy, oz, E, B, e, bf);
+                            const EB6<T> r = gather_eb_global<T>(g, i, j, k, ox, oy, oz, E, B);
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) { e[c] = r.e[c]; bf[c] = r.b[c]; }
                         } else {
                             gather_node<T, T>(g, i, j, k, ox, oy, oz, E, e);
                             gather_cell<T, T>(g, i, j, k, ox, oy, oz, B, bf);
@@ -601,29 +611,14 @@ struct MoverBlock {
     int cbx, cby, cbz, CB;
 };
 
-// Global trilinear gather of one node (E) or cell (B) field for a particle
-// whose stencil leaves the staged block (out of line: rare).
-// Scalars in, the three components out by value: no caller array has its
-// address taken, so nothing goes through the stack on the common path.
-template <typename T>
-struct Comp3 {
-    T v[3];
-};
-template <typename T>
-__device__ __noinline__ Comp3<T> gather_global_1(const GridP g, int c0, int c1, int c2, T u0, T u1, T u2,
-                                                 const double* __restrict__ F, bool node) {
-    Comp3<T> r;
-    if (node) gather_node<T>(g, c0, c1, c2, u0, u1, u2, F, r.v);
-    else gather_cell<T>(g, c0, c1, c2, u0, u1, u2, F, r.v);
-    return r;
-}
-
-// moveParticle (PIC++/mover.cpp:194-491), periodic box, one CTA per tile of
-// tile-ordered particles: E^n and E^{n+theta} (nodes) and B^n (cells) of
-// the tile and a two-cell halo are staged in shared memory in the particle
-// precision, so the predictor and the up to three Picard gathers read
-// shared memory; a particle whose stencil leaves the block gathers from the
-// FP64 grids.  Same arithmetic as k_implicit_push.
+// moveParticle (PIC++/mover.cpp:194-491), one CTA per tile of tile-ordered
+// particles: E^n and E^{n+theta} (nodes) and B^n (cells) of the tile and a
+// two-cell halo are staged in shared memory in the particle precision, so
+// the predictor and the up to three Picard gathers read shared memory.  A
+// particle with a position whose stencil leaves the block is left untouched
+// and its bit set in S.defer: k_implicit_push_deferred moves it from the
+// FP64 grids (the kernel itself calls nothing out of line, which would cost
+// its hot loop register spills).  Same arithmetic as k_implicit_push.
 template <typename T, bool kWall>
 __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g, TileGeom t, MoverBlock mb, ImpSpecies<T> S,
                                                             const double* __restrict__ E, const double* __restrict__ B,
@@ -726,13 +721,8 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     }
                     locate_l(l, u, L);
                 };
-                auto gat = [&](const Loc& L, const int c[3], const T u[3], const T* __restrict__ blkN,
-                               const double* __restrict__ glbN, bool node, T out[3]) {
-                    if (!L.inb) {
-                        const Comp3<T> r = gather_global_1<T>(g, c[0], c[1], c[2], u[0], u[1], u[2], glbN, node);
-                        out[0] = r.v[0]; out[1] = r.v[1]; out[2] = r.v[2];
-                        return;
-                    }
+                // gathers at a located position inside the block
+                auto gat = [&](const Loc& L, const T* __restrict__ blkN, bool node, T out[3]) {
                     if (node) {
 #pragma unroll
                         for (int q = 0; q < 3; ++q)
@@ -744,24 +734,15 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     }
                 };
                 // E^theta (node) and B^n (cell): float4 blocks for FP32
-                auto gatEt = [&](const Loc& L, const int c[3], const T u[3], T out[3]) {
-                    if constexpr (kVec) {
-                        if (L.inb) {
-                            tri_block4(sEt4, L.nbase, nsx, nsy, nsz, L.wn[0], L.wn[1], L.wn[2], out);
-                            return;
-                        }
-                    }
-                    gat(L, c, u, sEt, Et, true, out);
+                auto gatEt = [&](const Loc& L, T out[3]) {
+                    if constexpr (kVec) tri_block4(sEt4, L.nbase, nsx, nsy, nsz, L.wn[0], L.wn[1], L.wn[2], out);
+                    else gat(L, sEt, true, out);
                 };
-                auto gatB = [&](const Loc& L, const int c[3], const T u[3], T out[3]) {
-                    if constexpr (kVec) {
-                        if (L.inb) {
-                            tri_block4(sB4, L.cbase, csx, csy, csz, L.wc[0], L.wc[1], L.wc[2], out);
-                            return;
-                        }
-                    }
-                    gat(L, c, u, sB, B, false, out);
+                auto gatB = [&](const Loc& L, T out[3]) {
+                    if constexpr (kVec) tri_block4(sB4, L.cbase, csx, csy, csz, L.wc[0], L.wc[1], L.wc[2], out);
+                    else gat(L, sB, false, out);
                 };
+                auto defer = [&]() { atomicOr(&S.defer[s][n >> 5], 1u << (n & 31)); };
                 T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
                 T mom0[3] = {p.px[n], p.py[n], p.pz[n]};
                 T gam, v[3];
@@ -770,10 +751,14 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 Loc L0;
                 int l0[3];
                 locate(ci, u0, L0, l0);
-                gat(L0, ci, u0, sE, E, true, e);
-                gatB(L0, ci, u0, b);
+                if (!L0.inb) {
+                    defer();
+                    continue;
+                }
+                gat(L0, sE, true, e);
+                gatB(L0, b);
                 alpha_tensor<T>(beta, v, gam, e, b, al);
-                gatEt(L0, ci, u0, e);
+                gatEt(L0, e);
                 T vxb[3] = {v[1] * b[2] - v[2] * b[1], -v[0] * b[2] + v[2] * b[0], v[0] * b[1] - v[1] * b[0]};
                 T pnew[3];
 #pragma unroll
@@ -804,7 +789,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                 T newDisp[3] = {mv[0] * edt, mv[1] * edt, mv[2] * edt};
                 T prevDisp[3];
                 int it = 0;
-                bool reflected = false;
+                bool reflected = false, left = false;
                 while (picard_continue<T>(err, momNorm, cerr, dxN, it)) {
                     ++it;
                     const T prevMom[3] = {pnew[0], pnew[1], pnew[2]};
@@ -825,40 +810,27 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                         }
                     }
                     // the trial position x^n + newDisp: the offsets as advance_axis
-                    // forms them; the cell in tile-local terms (no periodic wrap),
-                    // the global cell only for a position outside the block
-                    int tc[3] = {0, 0, 0};
+                    // forms them, the cell in tile-local terms (no periodic wrap)
                     T tu[3];
+                    int tl[3];
                     Loc L1;
-                    if (L0.inb) {
-                        int tl[3];
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            const T sd = u0[d] + newDisp[d] * id[d];
-                            const T fd = dev_floor(sd);
-                            T ud = sd - fd;
-                            int cd = l0[d] + (int)fd;
-                            if (ud >= T(1)) { ud -= T(1); cd += 1; }
-                            tl[d] = nn[d] > 1 ? cd : 0;
-                            tu[d] = ud;
-                        }
-                        locate_l(tl, tu, L1);
-                        if (!L1.inb) {
-                            const int org[3] = {x0, y0, z0};
-#pragma unroll
-                            for (int d = 0; d < 3; ++d) tc[d] = nn[d] > 1 ? wrap_any(org[d] + tl[d], nn[d]) : 0;
-                        }
-                    } else {
-                        int tl[3];
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            tc[d] = ci[d]; tu[d] = u0[d];
-                            advance_axis<T>(tu[d], tc[d], newDisp[d] * id[d], nn[d]);
-                        }
-                        locate(tc, tu, L1, tl);
+                    for (int d = 0; d < 3; ++d) {
+                        const T sd = u0[d] + newDisp[d] * id[d];
+                        const T fd = dev_floor(sd);
+                        T ud = sd - fd;
+                        int cd = l0[d] + (int)fd;
+                        if (ud >= T(1)) { ud -= T(1); cd += 1; }
+                        tl[d] = nn[d] > 1 ? cd : 0;
+                        tu[d] = ud;
                     }
-                    gatEt(L1, tc, tu, e);
-                    gatB(L1, tc, tu, b);
+                    locate_l(tl, tu, L1);
+                    if (!L1.inb) {
+                        left = true;
+                        break;
+                    }
+                    gatEt(L1, e);
+                    gatB(L1, b);
                     const T mvxb[3] = {mv[1] * b[2] - mv[2] * b[1], -mv[0] * b[2] + mv[2] * b[0], mv[0] * b[1] - mv[1] * b[0]};
 #pragma unroll
                     for (int d = 0; d < 3; ++d) pnew[d] = mom0[d] + (e[d] + mvxb[d]) * qdt;
@@ -868,6 +840,10 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     cerr = picard_norm<T>((prevDisp[0] - newDisp[0]) * (prevDisp[0] - newDisp[0]) +
                                     (prevDisp[1] - newDisp[1]) * (prevDisp[1] - newDisp[1]) +
                                     (prevDisp[2] - newDisp[2]) * (prevDisp[2] - newDisp[2]));
+                }
+                if (left) {   // nothing written yet: the deferred pass moves it from the start
+                    defer();
+                    continue;
                 }
                 if (!reflected) {
                     if constexpr (kWall) {

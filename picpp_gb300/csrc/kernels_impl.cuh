@@ -308,10 +308,16 @@ bool PK<T>::implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& 
     const int cap = kNumSM * (per_sm > 0 ? per_sm : 1);
     // the wall rules are a separate instantiation: the periodic mover keeps
     // none of their code in its loop
-    if (g.wall)
+    // the particles it left over: one thread per mask word
+    long long words = 1;
+    for (int q = 0; q < S.ns; ++q) words = std::max(words, (S.p[q].n + 31) / 32);
+    if (g.wall) {
         k_implicit_push_tile<T, true><<<ntiles < cap ? ntiles : cap, kMoverThreads, smem, s>>>(g, t, mb, S, E, B, Et);
-    else
+        k_implicit_push_deferred<T, true><<<grid_for(words, 128), 128, 0, s>>>(g, S, E, B, Et);
+    } else {
         k_implicit_push_tile<T, false><<<ntiles < cap ? ntiles : cap, kMoverThreads, smem, s>>>(g, t, mb, S, E, B, Et);
+        k_implicit_push_deferred<T, false><<<grid_for(words, 128), 128, 0, s>>>(g, S, E, B, Et);
+    }
     return true;
 }
 

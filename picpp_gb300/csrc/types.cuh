@@ -49,6 +49,7 @@ struct ImpSpecies {
     PartView<T> p[kMaxSpecies];
     double q[kMaxSpecies], m[kMaxSpecies], w[kMaxSpecies];
     const int* off[kMaxSpecies];   // sort offsets by key (nkeys + 1)
+    unsigned* defer[kMaxSpecies];  // the tiled mover's deferred particles, one bit each
     int ns;
 };
 

@@ -375,6 +375,32 @@ def test_implicit_steps_with_drift_since_sort_match_oracle(pg, real, tile):
         compare_particles(st.box, got, sp[s], tol, TOL64 if real else TOL32)
 
 
+@pytest.mark.parametrize("tile", [(1, 1, 1), (2, 3, 5)])
+def test_implicit_far_drift_takes_the_mover_deferred_pass(pg, tile):
+    """Sorting only at the first step: by the fifth of 8 steps the beam
+    particles (0.4 cells per step) lie more than the two-cell halo away from
+    their tile, so the tiled mover leaves them to its deferred pass and the
+    deposit to its halo or global path.  FP64 fields and particles against
+    the oracle."""
+    st = implicit_state(ppc=3, gamma=6.0, seed=43)
+    steps = 8
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, pressure_compat=0, sort_every=10, tile=tile)
+    sim.upload_state(st)
+    for _ in range(steps):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+    E, B, _ = sim.download_fields()
+    g = O.make_grid(st.box, pressure_compat=0)
+    sp = copy_species(st.species)
+    Eo, Bo = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(steps):
+        O.implicit_step(g, sp, Eo, Bo)
+    assert rel_err(E.reshape(-1), Eo) < TOL64
+    assert rel_err(B.reshape(-1), Bo) < TOL64
+    for s in range(2):
+        got = by_id(sim.download_particles(s))
+        compare_particles(st.box, got, sp[s], TOL64, TOL64)
+
+
 def test_maxwell_operator_matches_oracle(pg):
     box = I.Box(7, 6, 5, 0.5, 0.5, 0.5, 0.5)
     rng = np.random.default_rng(2)

@@ -55,6 +55,8 @@ def _args():
     p.add_argument("--shock-drift-steps", type=int, default=100)
     p.add_argument("--no-shock", action="store_true")
     p.add_argument("--only-shock", action="store_true", help="run and print only the reflecting-wall shock section")
+    p.add_argument("--mixed-inner", type=int, default=12, help="FP32 inner steps of the mixed-precision solve")
+    p.add_argument("--mixed-steps", type=int, default=10, help="implicit steps timed with the mixed-precision solve")
     p.add_argument("--nn-steps", type=int, default=4000, help="training steps of the learned preconditioner")
     p.add_argument("--nn-batch", type=int, default=4, help="triples per training step (Adam, lr 1e-3)")
     p.add_argument("--nn-triples", type=int, default=2000, help="recorded plain-solve triples to train on")
@@ -166,6 +168,7 @@ def implicit_section(a):
     out["plain"] = {"solver": "GMRES(30), classical Gram-Schmidt with selective second pass, FP64",
                     "iterations": info["iterations"], "restarts": info["restarts"],
                     "rel_residual": info["rel_residual"], "seconds": info["seconds"]}
+    out["mixed_vs_plain"] = mixed_solve(a, sim, opts)
     if a.nn_steps > 0:
         out["learned_vs_plain"] = learned_solve(a, sim, box, w, opts)
     sim.close()
@@ -438,6 +441,52 @@ def stiff_solve(a, w):
 
 NET_LAYERS = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1),
               (32, 32, 1), (48, 16, 0), (16, 16, 0), (16, 16, 0)]   # (cin, cout, level) of the network
+
+
+def mixed_solve(a, sim, plain_opts):
+    """The mixed-precision right preconditioner (FGMRES(30) in FP64 around an
+    FP32 GMRES solve of `inner` Arnoldi steps) against plain GMRES(30) on the
+    system of the state after the timed steps, to an FP64 true relative
+    residual of 1e-8: iterations and device time for several inner lengths;
+    then a.mixed_steps implicit steps with the mixed solve (inner
+    a.mixed_inner), timed like the stated run."""
+    import torch
+    import picpp_gb300 as P
+    sim.updateElectroMagneticParameters()
+    _, mu, _, rhs = sim.download_moments()
+    sim.maxwell_solve(mu, rhs, plain_opts)   # warm-up
+    _, ip = sim.maxwell_solve(mu, rhs, plain_opts)
+    rows = []
+    for k in (4, 8, 12, 16, 24):
+        o = P.solve_opts(P.FGMRES_MIXED, restart=30, max_iter=600, tol=1e-8, inner=k)
+        sim.maxwell_solve(mu, rhs, o)   # warm-up (workspace)
+        _, im = sim.maxwell_solve(mu, rhs, o)
+        rows.append({"inner": k, "outer_iterations": im["iterations"], "ms": im["seconds"] * 1e3,
+                     "rel_residual": im["rel_residual"], "fallback": im["used_fallback"],
+                     "speedup": ip["seconds"] / im["seconds"]})
+    out = {"system": "the state after the timed steps", "tol": 1e-8,
+           "plain": {"iterations": ip["iterations"], "ms": ip["seconds"] * 1e3, "rel_residual": ip["rel_residual"]},
+           "mixed": rows}
+    if a.mixed_steps > 0:
+        mo = P.solve_opts(P.FGMRES_MIXED, restart=30, max_iter=600, tol=1e-8, inner=a.mixed_inner)
+        stream = torch.cuda.ExternalStream(sim.stream)
+        sim.implicit_step(mo)
+        sim.profile(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        times, its = [], []
+        for _ in range(a.mixed_steps):
+            e0.record(stream)
+            info = sim.implicit_step(mo)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            its.append(info["iterations"])
+        phases, _ = sim.profile(False)
+        out["steps"] = {"inner": a.mixed_inner, "timed_steps": len(times), "step_ms_median": statistics.median(times),
+                        "step_ms_min": min(times), "step_ms_max": max(times),
+                        "outer_iterations": {"min": min(its), "max": max(its)},
+                        "phase_ms": {k: v / len(times) for k, v in phases.items() if v > 0}}
+    return out
 
 
 def learned_solve(a, sim, box, w, opts):

@@ -105,15 +105,21 @@ typedef enum {
     PIC_GMRES_RESTARTED = 1, /* GMRES(restart), classical Gram-Schmidt with
                                 re-orthogonalisation, true FP64 residual checked
                                 against tol at every restart                     */
-    PIC_FGMRES_LEARNED = 2   /* flexible GMRES(restart) with the learned right
+    PIC_FGMRES_LEARNED = 2,  /* flexible GMRES(restart) with the learned right
                                 preconditioner; plain GMRES when it stalls       */
+    PIC_FGMRES_MIXED = 3     /* flexible GMRES(restart) in FP64 whose right
+                                preconditioner is an FP32 GMRES solve of `inner`
+                                Arnoldi steps (the FP64 true residual still
+                                reaches tol); plain GMRES when it stalls         */
 } pic_gmres_method;
 
 typedef struct {
     int method;              /* pic_gmres_method                              */
-    int restart;             /* Krylov vectors per cycle (methods 1, 2)       */
-    int max_iter;            /* total iteration cap                           */
+    int restart;             /* Krylov vectors per cycle (methods 1-3)        */
+    int max_iter;            /* total iteration cap (outer iterations)        */
     double tol;              /* relative residual target                      */
+    int inner;               /* PIC_FGMRES_MIXED: FP32 steps per apply, 0..64
+                                (0: 12)                                        */
 } pic_solve_opts;
 
 typedef struct {

@@ -23,7 +23,7 @@ PIC_NOALLOC_MAX_SPECIES = 16
 BUNEMAN, IMPLICIT = 0, 1
 BOUNDARY_PERIODIC, BOUNDARY_WALL_OPEN = 0, 1
 F32, F64 = 0, 1
-GMRES_REFERENCE, GMRES_RESTARTED, FGMRES_LEARNED = 0, 1, 2
+GMRES_REFERENCE, GMRES_RESTARTED, FGMRES_LEARNED, FGMRES_MIXED = 0, 1, 2, 3
 
 EXPORTS = [
     "pic_create", "pic_destroy", "pic_last_error", "pic_stream", "pic_add_species", "pic_upload_particles",
@@ -58,7 +58,8 @@ class Config(C.Structure):
 
 
 class SolveOpts(C.Structure):
-    _fields_ = [("method", C.c_int), ("restart", C.c_int), ("max_iter", C.c_int), ("tol", C.c_double)]
+    _fields_ = [("method", C.c_int), ("restart", C.c_int), ("max_iter", C.c_int), ("tol", C.c_double),
+                ("inner", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -174,8 +175,8 @@ def _i(a):
     return a.ctypes.data_as(_ip)
 
 
-def solve_opts(method=GMRES_REFERENCE, restart=30, max_iter=50, tol=1e-8) -> SolveOpts:
-    return SolveOpts(method, restart, max_iter, tol)
+def solve_opts(method=GMRES_REFERENCE, restart=30, max_iter=50, tol=1e-8, inner=0) -> SolveOpts:
+    return SolveOpts(method, restart, max_iter, tol, inner)
 
 
 class GpuSimulation:

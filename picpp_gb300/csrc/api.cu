@@ -957,7 +957,7 @@ pic_status pic_evaluate_electric_field(pic_ctx* ctx, const pic_solve_opts* opts,
     }
     if (st != PIC_OK && st != PIC_ERR_NOT_CONVERGED) return st;
     const int method = opts ? opts->method : PIC_GMRES_REFERENCE;
-    if (st == PIC_OK && ctx->trip.data && method != PIC_FGMRES_LEARNED) {
+    if (st == PIC_OK && ctx->trip.data && (method == PIC_GMRES_REFERENCE || method == PIC_GMRES_RESTARTED)) {
         pic_status rs = ctx->trip.add(ctx->s, ctx->rhs, ctx->mu, ctx->Et, ctx->partials + 7 * 1024, ctx->partials,
                                       &ctx->err);
         if (rs != PIC_OK) return rs;

@@ -6,6 +6,8 @@
 #include "sort.cuh"
 #include "wall.cuh"
 #include <algorithm>
+#include <cstdint>
+#include <initializer_list>
 
 namespace pic {
 
@@ -81,9 +83,18 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
 
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
                           double* y, double* wmu) {
-    k_mu_times<<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
-    k_maxwell_stencil<<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
-    if (g.wall) k_wall_rows<<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
+    k_mu_times<double><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
+    k_maxwell_stencil<double><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
+    if (g.wall) k_wall_rows<double><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
+}
+
+// The same operator in FP32 (inner solve of the mixed-precision
+// preconditioner; mu an FP32 copy).
+void launch_maxwell_apply_f32(cudaStream_t s, const GridP& g, const OpCoef& oc, const float* mu, const float* x,
+                              float* y, float* wmu) {
+    k_mu_times<float><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
+    k_maxwell_stencil<float><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
+    if (g.wall) k_wall_rows<float><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
 }
 
 void launch_wall_moments(cudaStream_t s, const GridP& g, double* J, double* mu, double* rho, double* Pi,
@@ -282,6 +293,52 @@ void launch_combine(cudaStream_t s, double* x, const double* V, long long ld, in
 
 void launch_residual(cudaStream_t s, double* r, const double* b, const double* Ax, long long n) {
     k_residual<<<grid_for(n, 256), 256, 0, s>>>(r, b, Ax, n);
+}
+
+// FP32 vectors: float4 accesses when the length is a multiple of 4 and the
+// bases are 16-byte aligned.
+static bool vec4_ok(long long n, std::initializer_list<const void*> ps) {
+    if (n % 4) return false;
+    for (const void* p : ps)
+        if (reinterpret_cast<uintptr_t>(p) % 16) return false;
+    return true;
+}
+
+void launch_dot_f32(cudaStream_t s, const float* a, const float* b, long long n, double* partials, int P,
+                    double* out, unsigned* counter) {
+    if (vec4_ok(n, {a, b})) k_dot_f32<4><<<P, kRedThreads, 0, s>>>(a, b, n / 4, partials, out, counter);
+    else k_dot_f32<1><<<P, kRedThreads, 0, s>>>(a, b, n, partials, out, counter);
+}
+
+void launch_multi_dot_f32(cudaStream_t s, const float* V, long long ld, int k, const float* w, long long n,
+                          double* partials, int P, double* out, unsigned* counter) {
+    const bool v4 = vec4_ok(n, {V, w}) && ld % 4 == 0;
+    for (int k0 = 0; k0 < k; k0 += 8) {
+        if (v4) k_multi_dot_f32<8, 4><<<P, kRedThreads, 0, s>>>(V, ld / 4, k0, k, w, n / 4, partials, out, counter);
+        else k_multi_dot_f32<8, 1><<<P, kRedThreads, 0, s>>>(V, ld, k0, k, w, n, partials, out, counter);
+    }
+}
+
+void launch_axpy_norm_f32(cudaStream_t s, float* w, const float* V, long long ld, int k, const double* h, long long n,
+                          double* partials, int P, double* out, unsigned* counter) {
+    if (vec4_ok(n, {V, w}) && ld % 4 == 0)
+        k_axpy_norm_f32<4><<<P, kRedThreads, 0, s>>>(w, V, ld / 4, k, h, n / 4, partials, out, counter);
+    else
+        k_axpy_norm_f32<1><<<P, kRedThreads, 0, s>>>(w, V, ld, k, h, n, partials, out, counter);
+}
+
+void launch_normalize_f32(cudaStream_t s, float* v, const float* w, const double* h2, long long n) {
+    if (vec4_ok(n, {v, w})) k_normalize_f32<4><<<grid_for(n / 4, 256), 256, 0, s>>>(v, w, h2, n / 4);
+    else k_normalize_f32<1><<<grid_for(n, 256), 256, 0, s>>>(v, w, h2, n);
+}
+
+void launch_to_f32(cudaStream_t s, float* dst, const double* src, long long n) {
+    k_to_f32<<<grid_for(n, 256), 256, 0, s>>>(dst, src, n);
+}
+
+void launch_combine_f32(cudaStream_t s, double* z, const float* V, long long ld, int k, const double* y,
+                        double scale, long long n) {
+    k_combine_f32<<<grid_for(n, 256), 256, 0, s>>>(z, V, ld, k, y, scale, n);
 }
 
 void launch_nonfinite(cudaStream_t s, const double* a, long long n, int* flag) {

@@ -226,9 +226,10 @@ __global__ void __launch_bounds__(256) k_maxwell_rhs(GridP g, const double* __re
 //         + sum_{d != a} K/(4 da dd) [w_d(++) + w_d(--) - w_d(-+) - w_d(+-)]
 // with w = mu x evaluated at the neighbour nodes: the same terms as the
 // reference's 37-entry rows regrouped (so FP64 results agree to rounding).
-__device__ __forceinline__ void mu_times(const double* __restrict__ mu, long long N, long long id,
-                                         const double* __restrict__ x, double w[3]) {
-    double x0 = x[id], x1 = x[N + id], x2 = x[2 * N + id];
+template <typename T>
+__device__ __forceinline__ void mu_times(const T* __restrict__ mu, long long N, long long id,
+                                         const T* __restrict__ x, T w[3]) {
+    T x0 = x[id], x1 = x[N + id], x2 = x[2 * N + id];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         w[a] = mu[(3 * a) * N + id] * x0 + mu[(3 * a + 1) * N + id] * x1 + mu[(3 * a + 2) * N + id] * x2;
@@ -238,13 +239,15 @@ __device__ __forceinline__ void mu_times(const double* __restrict__ mu, long lon
 // (about 1/64 of FP32) makes the apply arithmetic-bound, so mu x is formed
 // once per node (9 operations) instead of at every stencil point that reads
 // it (centre, 6 neighbours, 12 corners: about 190 operations per node).
-// Pass 1: w_a = sum_b mu_ab x_b.
-__global__ void __launch_bounds__(256) k_mu_times(long long N, const double* __restrict__ mu,
-                                                  const double* __restrict__ x, double* __restrict__ w) {
+// Pass 1: w_a = sum_b mu_ab x_b.  T: FP64, or FP32 for the inner solve of
+// the mixed-precision preconditioner.
+template <typename T>
+__global__ void __launch_bounds__(256) k_mu_times(long long N, const T* __restrict__ mu,
+                                                  const T* __restrict__ x, T* __restrict__ w) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
-        double wc[3];
-        mu_times(mu, N, c, x, wc);
+        T wc[3];
+        mu_times<T>(mu, N, c, x, wc);
         w[c] = wc[0]; w[N + c] = wc[1]; w[2 * N + c] = wc[2];
     }
 }
@@ -253,15 +256,17 @@ __global__ void __launch_bounds__(256) k_mu_times(long long N, const double* __r
 // 1961-2073, 2521-2633): diag x_a - c1 w_a; along axis a K/da^2 (w_a - x_a)
 // at both neighbours, along the other axes -K/d^2 x_a; in the (a, d) planes
 // K/(4 da dd) (w_d(++) - w_d(+-) - w_d(-+) + w_d(--)).  Periodic box.
-__global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, const double* __restrict__ x,
-                                                         const double* __restrict__ w, double* __restrict__ y) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, const T* __restrict__ x,
+                                                         const T* __restrict__ w, T* __restrict__ y) {
     const long long N = g.N;
     const int n[3] = {g.nx, g.ny, g.nz};
     const long long st[3] = {1, (long long)g.nx, (long long)g.nx * g.ny};
-    double diag = 1.0;
+    double diag64 = 1.0;
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax)
-        if (oc.has[ax]) diag += 2.0 * oc.kd2[ax];
+        if (oc.has[ax]) diag64 += 2.0 * oc.kd2[ax];
+    const T diag = T(diag64);
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
         int p[3];
@@ -274,23 +279,23 @@ __global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, con
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const double* xa = x + a * N + c;
-            const double* wa = w + a * N + c;
-            const double c1 = oc.has[a] ? 1.0 + 2.0 * oc.kd2[a] : 1.0;
-            double acc = fma(-c1, wa[0], diag * xa[0]);
+            const T* xa = x + a * N + c;
+            const T* wa = w + a * N + c;
+            const T c1 = T(oc.has[a] ? 1.0 + 2.0 * oc.kd2[a] : 1.0);
+            T acc = fma(-c1, wa[0], diag * xa[0]);
 #pragma unroll
             for (int ax = 0; ax < 3; ++ax) {
                 if (!oc.has[ax]) continue;
-                const double xs = xa[up[ax]] + xa[dn[ax]];
-                if (ax == a) acc = fma(oc.kd2[ax], (wa[up[ax]] + wa[dn[ax]]) - xs, acc);
-                else acc = fma(-oc.kd2[ax], xs, acc);
+                const T xs = xa[up[ax]] + xa[dn[ax]];
+                if (ax == a) acc = fma(T(oc.kd2[ax]), (wa[up[ax]] + wa[dn[ax]]) - xs, acc);
+                else acc = fma(T(-oc.kd2[ax]), xs, acc);
             }
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (d == a || !oc.has[a] || !oc.has[d]) continue;
-                const double* wd = w + d * N + c;
-                const double sum = (wd[up[a] + up[d]] - wd[up[a] + dn[d]]) - (wd[dn[a] + up[d]] - wd[dn[a] + dn[d]]);
-                acc = fma(oc.kx4[a][d], sum, acc);
+                const T* wd = w + d * N + c;
+                const T sum = (wd[up[a] + up[d]] - wd[up[a] + dn[d]]) - (wd[dn[a] + up[d]] - wd[dn[a] + dn[d]]);
+                acc = fma(T(oc.kx4[a][d]), sum, acc);
             }
             y[a * N + c] = acc;
         }

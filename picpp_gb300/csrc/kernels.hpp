@@ -102,6 +102,8 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
 // y = A(mu) x; wmu: scratch of 3N doubles (mu x)
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
                           double* y, double* wmu);
+void launch_maxwell_apply_f32(cudaStream_t s, const GridP& g, const OpCoef& oc, const float* mu, const float* x,
+                              float* y, float* wmu);
 // conductor wall at x = 0 / open boundary at x = (nx - 2) dx (wall.cuh)
 void launch_wall_moments(cudaStream_t s, const GridP& g, double* J, double* mu, double* rho, double* Pi,
                          int pi_mirror);
@@ -132,6 +134,19 @@ void launch_scale(cudaStream_t s, double* v, const double* w, double sc, long lo
 void launch_div(cudaStream_t s, double* v, const double* w, double d, long long n);
 void launch_combine(cudaStream_t s, double* x, const double* V, long long ld, int k, const double* y, double scale,
                     int accumulate, long long n);
+// FP32 vectors of the mixed-precision preconditioner (FP64 partials, outputs
+// and coefficients; each reduction one launch, finished by its last block,
+// counter: a zeroed device word)
+void launch_dot_f32(cudaStream_t s, const float* a, const float* b, long long n, double* partials, int P,
+                    double* out, unsigned* counter);
+void launch_multi_dot_f32(cudaStream_t s, const float* V, long long ld, int k, const float* w, long long n,
+                          double* partials, int P, double* out, unsigned* counter);
+void launch_axpy_norm_f32(cudaStream_t s, float* w, const float* V, long long ld, int k, const double* h, long long n,
+                          double* partials, int P, double* out, unsigned* counter);
+void launch_normalize_f32(cudaStream_t s, float* v, const float* w, const double* h2, long long n);
+void launch_to_f32(cudaStream_t s, float* dst, const double* src, long long n);
+void launch_combine_f32(cudaStream_t s, double* z, const float* V, long long ld, int k, const double* y,
+                        double scale, long long n);
 void launch_residual(cudaStream_t s, double* r, const double* b, const double* Ax, long long n);
 void launch_nonfinite(cudaStream_t s, const double* a, long long n, int* flag);
 void launch_finalize(cudaStream_t s, const double* partials, int P, int nvec, double* out, int ostride, int take_sqrt);

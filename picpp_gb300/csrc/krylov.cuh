@@ -109,6 +109,185 @@ __global__ void k_residual(double* __restrict__ r, const double* __restrict__ b,
         r[i] = b[i] - Ax[i];
 }
 
+// ---- FP32 vectors of the mixed-precision preconditioner's inner solve:
+// products accumulated in FP32 per thread and in FP64 across threads,
+// Hessenberg entries and coefficients kept in FP64.  Each reduction is one
+// launch: every block writes its partial sums, and the last block to finish
+// (a global counter) adds all partials in a fixed order, so the result does
+// not depend on the order in which blocks ran.
+
+// True in the block that finished last (counter reset for the next launch
+// by that block's caller after its final sums).
+__device__ __forceinline__ bool last_block(unsigned* counter) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    return is_last;
+}
+
+// out[m] = sum of partials[m * P .. m * P + P), m in [m0, m1), fixed order
+// (run by the last block; partials read around L1).
+__device__ __forceinline__ void finalize_rows(const double* partials, int P, int m0, int m1, double* out,
+                                              double* sh) {
+    for (int m = m0; m < m1; ++m) {
+        double t = 0.0;
+        for (int i = threadIdx.x; i < P; i += blockDim.x) t += __ldcg(&partials[(long long)m * P + i]);
+        t = block_sum(t, sh);
+        if (threadIdx.x == 0) out[m] = t;
+    }
+}
+
+// Element access of the FP32 kernels: W = 4 reads and writes float4 (the
+// vectors' length a multiple of 4 and their bases 16-byte aligned, which the
+// launchers check), W = 1 single floats.
+template <int W>
+struct F32Vec;
+template <>
+struct F32Vec<1> {
+    using T = float;
+    static __device__ __forceinline__ float dot(float a, float b, float acc) { return fmaf(a, b, acc); }
+    static __device__ __forceinline__ float axpy(float a, float x, float y) { return fmaf(a, x, y); }
+    static __device__ __forceinline__ float scale(float x, float f) { return x * f; }
+    static __device__ __forceinline__ float zero() { return 0.f; }
+};
+template <>
+struct F32Vec<4> {
+    using T = float4;
+    static __device__ __forceinline__ float dot(float4 a, float4 b, float acc) {
+        return fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, fmaf(a.x, b.x, acc))));
+    }
+    static __device__ __forceinline__ float4 axpy(float a, float4 x, float4 y) {
+        return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+    }
+    static __device__ __forceinline__ float4 scale(float4 x, float f) {
+        return make_float4(x.x * f, x.y * f, x.z * f, x.w * f);
+    }
+    static __device__ __forceinline__ float4 zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+};
+
+// out[0] = a . b (FP32 vectors; n counts elements of W floats).
+template <int W>
+__global__ void __launch_bounds__(kRedThreads) k_dot_f32(const float* __restrict__ a_, const float* __restrict__ b_,
+                                                         long long n, double* __restrict__ partials,
+                                                         double* __restrict__ out, unsigned* __restrict__ counter) {
+    using V = F32Vec<W>;
+    const typename V::T* a = reinterpret_cast<const typename V::T*>(a_);
+    const typename V::T* b = reinterpret_cast<const typename V::T*>(b_);
+    __shared__ double sh[32];
+    float s = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s = V::dot(a[i], b[i], s);
+    const double t = block_sum(double(s), sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = t;
+    if (last_block(counter)) {
+        finalize_rows(partials, gridDim.x, 0, 1, out, sh);
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+}
+
+// out[m] = V[m] . w for m in [k0, min(k0 + KB, k)) (FP32 basis, stride ld
+// in elements of W floats).
+template <int KB, int W>
+__global__ void __launch_bounds__(kRedThreads) k_multi_dot_f32(const float* __restrict__ V_, long long ld, int k0,
+                                                               int k, const float* __restrict__ w_, long long n,
+                                                               double* __restrict__ partials,
+                                                               double* __restrict__ out,
+                                                               unsigned* __restrict__ counter) {
+    using F = F32Vec<W>;
+    const typename F::T* V = reinterpret_cast<const typename F::T*>(V_);
+    const typename F::T* w = reinterpret_cast<const typename F::T*>(w_);
+    __shared__ double sh[32];
+    float acc[KB];
+#pragma unroll
+    for (int m = 0; m < KB; ++m) acc[m] = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const typename F::T wi = w[i];
+#pragma unroll
+        for (int m = 0; m < KB; ++m)
+            if (k0 + m < k) acc[m] = F::dot(V[(long long)(k0 + m) * ld + i], wi, acc[m]);
+    }
+    const int P = gridDim.x;
+#pragma unroll
+    for (int m = 0; m < KB; ++m) {
+        if (k0 + m >= k) break;
+        const double t = block_sum(double(acc[m]), sh);
+        if (threadIdx.x == 0) partials[(long long)(k0 + m) * P + blockIdx.x] = t;
+    }
+    if (last_block(counter)) {
+        finalize_rows(partials, P, k0, k0 + KB < k ? k0 + KB : k, out, sh);
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+}
+
+// w -= sum_m h[m] V[m], m < k; then out[0] = |w|^2 (FP32 vectors, FP64
+// coefficients).
+template <int W>
+__global__ void __launch_bounds__(kRedThreads) k_axpy_norm_f32(float* __restrict__ w_, const float* __restrict__ V_,
+                                                               long long ld, int k, const double* __restrict__ h,
+                                                               long long n, double* __restrict__ partials,
+                                                               double* __restrict__ out,
+                                                               unsigned* __restrict__ counter) {
+    using F = F32Vec<W>;
+    typename F::T* w = reinterpret_cast<typename F::T*>(w_);
+    const typename F::T* V = reinterpret_cast<const typename F::T*>(V_);
+    __shared__ double sh[32];
+    __shared__ float hs[64];
+    for (int m = threadIdx.x; m < k; m += blockDim.x) hs[m] = float(h[m]);
+    __syncthreads();
+    float nrm = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        typename F::T s = w[i];
+        for (int m = 0; m < k; ++m) s = F::axpy(-hs[m], V[(long long)m * ld + i], s);
+        w[i] = s;
+        nrm = F::dot(s, s, nrm);
+    }
+    const double t = block_sum(double(nrm), sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = t;
+    if (last_block(counter)) {
+        finalize_rows(partials, gridDim.x, 0, 1, out, sh);
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+}
+
+// v = w / sqrt(h2[0]) (zero for h2[0] <= 0); one square root per block.
+template <int W>
+__global__ void k_normalize_f32(float* __restrict__ v_, const float* __restrict__ w_, const double* __restrict__ h2,
+                                long long n) {
+    using F = F32Vec<W>;
+    typename F::T* v = reinterpret_cast<typename F::T*>(v_);
+    const typename F::T* w = reinterpret_cast<const typename F::T*>(w_);
+    __shared__ float inv;
+    if (threadIdx.x == 0) {
+        const double d = *h2;
+        inv = d > 0 ? float(1.0 / sqrt(d)) : 0.f;
+    }
+    __syncthreads();
+    const float f = inv;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        v[i] = F::scale(w[i], f);
+}
+
+// dst = src (FP64 to FP32).
+__global__ void k_to_f32(float* __restrict__ dst, const double* __restrict__ src, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = float(src[i]);
+}
+
+// z = scale * sum_m V[m] y[m] in FP64 (FP32 basis, FP64 coefficients).
+__global__ void k_combine_f32(double* __restrict__ z, const float* __restrict__ V, long long ld, int k,
+                              const double* __restrict__ y, double scale, long long n) {
+    __shared__ float ys[64];
+    for (int m = threadIdx.x; m < k; m += blockDim.x) ys[m] = float(y[m]);
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int m = 0; m < k; ++m) s = fmaf(ys[m], V[(long long)m * ld + i], s);
+        z[i] = double(s) * scale;
+    }
+}
+
 // flag[0] |= any non-finite value
 __global__ void k_nonfinite(const double* __restrict__ a, long long n, int* __restrict__ flag) {
     int bad = 0;

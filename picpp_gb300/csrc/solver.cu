@@ -28,6 +28,8 @@ OpCoef make_opcoef(const GridP& g) {
 void krylov_free(Krylov& k) {
     cudaFree(k.V); cudaFree(k.Z); cudaFree(k.w); cudaFree(k.mx); cudaFree(k.r); cudaFree(k.hdev); cudaFree(k.ydev);
     cudaFree(k.part); cudaFree(k.scal);
+    cudaFree(k.mu32); cudaFree(k.V32); cudaFree(k.w32); cudaFree(k.mx32); cudaFree(k.h32); cudaFree(k.part32);
+    cudaFree(k.cnt32);
     k = Krylov{};
 }
 
@@ -187,6 +189,105 @@ pic_status ensure_z(SolveCtx& c, int m, long long L) {
     return PIC_OK;
 }
 
+// ---- mixed-precision right preconditioner: z = an FP32 GMRES solve of
+// A z = v from zero, S Arnoldi steps long.  FP64 runs at about 1/64 of the
+// FP32 rate on this GPU, so the bulk of the Krylov work (operator applies,
+// Gram-Schmidt) moves to FP32, where it is bound by memory traffic; the
+// outer flexible GMRES keeps FP64 vectors and checks the FP64 true residual,
+// so the solve reaches the same tolerance.  One classical Gram-Schmidt pass
+// per step (the inner solve only preconditions: lost orthogonality costs it
+// accuracy, not the outer solve correctness), the Hessenberg entries stay on
+// the device, and one stream synchronisation per apply brings them to the
+// host for the small least-squares solve.
+// h32 layout: [0] |v|^2, then H (column j at 8 + j (S + 1)), the squared
+// norms of the new vectors, y.
+struct InnerLayout {
+    int S;
+    long long h() const { return 8; }
+    long long hn() const { return 8 + (long long)(S + 1) * S; }
+    long long y() const { return hn() + S; }
+    long long size() const { return y() + S + 1; }
+};
+
+pic_status ensure_inner(SolveCtx& c, int S, long long L) {
+    Krylov& k = *c.k;
+    if (k.steps32 >= S && k.V32) return PIC_OK;
+    cudaFree(k.mu32); cudaFree(k.V32); cudaFree(k.w32); cudaFree(k.mx32); cudaFree(k.h32); cudaFree(k.part32);
+    cudaFree(k.cnt32);
+    k.mu32 = nullptr; k.V32 = nullptr; k.w32 = nullptr; k.mx32 = nullptr; k.h32 = nullptr; k.part32 = nullptr;
+    k.cnt32 = nullptr;
+    k.steps32 = 0;
+    const InnerLayout lay{S};
+    CKS(cudaMalloc(&k.mu32, sizeof(float) * 3 * (size_t)L));
+    CKS(cudaMalloc(&k.V32, sizeof(float) * (size_t)(S + 1) * L));
+    CKS(cudaMalloc(&k.w32, sizeof(float) * (size_t)L));
+    CKS(cudaMalloc(&k.mx32, sizeof(float) * (size_t)L));
+    CKS(cudaMalloc(&k.h32, sizeof(double) * (size_t)lay.size()));
+    CKS(cudaMalloc(&k.part32, sizeof(double) * (size_t)(S + 2) * 1024));
+    CKS(cudaMalloc(&k.cnt32, sizeof(unsigned)));
+    CKS(cudaMemsetAsync(k.cnt32, 0, sizeof(unsigned), c.s));
+    k.steps32 = S;
+    return PIC_OK;
+}
+
+pic_status inner_apply(SolveCtx& c, const OpCoef& oc, int S, const double* v, double* z) {
+    const GridP& g = *c.g;
+    Krylov& k = *c.k;
+    const long long L = 3 * g.N;
+    const int P = red_blocks(L);
+    const InnerLayout lay{S};
+    auto V = [&](int j) { return k.V32 + (long long)j * L; };
+    double* h = k.h32;
+    launch_to_f32(c.s, k.w32, v, L);
+    launch_dot_f32(c.s, k.w32, k.w32, L, k.part32, P, h, k.cnt32);
+    launch_normalize_f32(c.s, V(0), k.w32, h, L);
+    for (int j = 0; j < S; ++j) {
+        float* w = V(j + 1);
+        double* col = h + lay.h() + (long long)j * (S + 1);
+        launch_maxwell_apply_f32(c.s, g, oc, k.mu32, V(j), w, k.mx32);
+        launch_multi_dot_f32(c.s, k.V32, L, j + 1, w, L, k.part32, P, col, k.cnt32);
+        launch_axpy_norm_f32(c.s, w, k.V32, L, j + 1, col, L, k.part32, P, h + lay.hn() + j, k.cnt32);
+        launch_normalize_f32(c.s, w, w, h + lay.hn() + j, L);
+    }
+    std::vector<double> hh((size_t)lay.y());
+    CKS(cudaMemcpyAsync(hh.data(), h, sizeof(double) * (size_t)lay.y(), cudaMemcpyDeviceToHost, c.s));
+    CKS(cudaStreamSynchronize(c.s));
+    // min |beta e1 - H y| by Givens rotations
+    std::vector<double> H((size_t)(S + 1) * S, 0.0), gv(S + 1, 0.0), y(S + 1, 0.0);
+    auto Hm = [&](int i, int j) -> double& { return H[(size_t)i * S + j]; };
+    gv[0] = std::sqrt(std::max(hh[0], 0.0));
+    for (int j = 0; j < S; ++j) {
+        for (int i = 0; i <= j; ++i) Hm(i, j) = hh[lay.h() + (size_t)j * (S + 1) + i];
+        Hm(j + 1, j) = std::sqrt(std::max(hh[lay.hn() + j], 0.0));
+    }
+    std::vector<double> cs(S), sn(S);
+    int kk = 0;
+    for (int j = 0; j < S; ++j) {
+        for (int i = 0; i < j; ++i) {
+            const double t = cs[i] * Hm(i, j) + sn[i] * Hm(i + 1, j);
+            Hm(i + 1, j) = -sn[i] * Hm(i, j) + cs[i] * Hm(i + 1, j);
+            Hm(i, j) = t;
+        }
+        const double a = Hm(j, j), bb = Hm(j + 1, j);
+        const double mod = std::hypot(a, bb);
+        if (mod == 0) { cs[j] = 1; sn[j] = 0; } else { cs[j] = a / mod; sn[j] = bb / mod; }
+        Hm(j, j) = mod;
+        Hm(j + 1, j) = 0;
+        gv[j + 1] = -sn[j] * gv[j];
+        gv[j] = cs[j] * gv[j];
+        kk = j + 1;
+        if (!(bb > 0)) break;   // the Krylov space is invariant: exact solution
+    }
+    for (int i = kk - 1; i >= 0; --i) {
+        double sacc = gv[i];
+        for (int q = i + 1; q < kk; ++q) sacc -= Hm(i, q) * y[q];
+        y[i] = Hm(i, i) != 0 ? sacc / Hm(i, i) : 0.0;
+    }
+    CKS(cudaMemcpyAsync(h + lay.y(), y.data(), sizeof(double) * (size_t)std::max(kk, 1), cudaMemcpyHostToDevice, c.s));
+    launch_combine_f32(c.s, z, k.V32, L, kk, h + lay.y(), 1.0, L);
+    return PIC_OK;
+}
+
 // Restarted GMRES(m): classical Gram-Schmidt with a second pass where the
 // first one cancels, Givens rotations on the host (one stream
 // synchronisation per iteration, two with the second pass), FP64 true
@@ -194,11 +295,13 @@ pic_status ensure_z(SolveCtx& c, int m, long long L) {
 // a network (pc != nullptr) it is flexible GMRES (Saad 1993) with the right
 // preconditioner z_j = pc(v_j), x += Z y; a cycle that does not halve the
 // true residual, or a non-finite preconditioned direction, switches the
-// rest of the solve to plain GMRES from the current iterate.
+// rest of the solve to plain GMRES from the current iterate.  With inner > 0
+// the right preconditioner is instead the FP32 inner solve of inner steps.
 pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, double* x, const pic_solve_opts& o,
-                           pic_solve_info* info, Net* pc = nullptr) {
+                           pic_solve_info* info, Net* pc = nullptr, int inner = 0) {
     const GridP& g = *c.g;
     Net* const net = pc;   // pc becomes nullptr on a fallback
+    bool have = pc != nullptr || inner > 0;   // a right preconditioner is in use
     const long long L = 3 * g.N;
     const int P = red_blocks(L);
     const int m = std::max(1, o.restart > 0 ? o.restart : 30);
@@ -206,8 +309,10 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
     const double tol = o.tol > 0 ? o.tol : 1e-8;
     pic_status st = PIC_OK;
     if ((st = ensure(c, m + 1, L)) != PIC_OK) return st;
-    if (pc && (st = ensure_z(c, m, L)) != PIC_OK) return st;
+    if (have && (st = ensure_z(c, m, L)) != PIC_OK) return st;
+    if (inner > 0 && (st = ensure_inner(c, inner, L)) != PIC_OK) return st;
     Krylov& k = *c.k;
+    if (inner > 0) launch_to_f32(c.s, k.mu32, c.mu, 3 * L);   // mu for the FP32 operator
     auto Vp = [&](int j) { return k.V + (long long)j * L; };
     auto Zp = [&](int j) { return k.Z + (long long)j * L; };
     bool fallback = false;
@@ -232,7 +337,7 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
         rel = beta / bnorm;
         if (!std::isfinite(rel)) return err(c, PIC_ERR_NUMERIC, "non-finite residual");
         if (rel <= tol || total >= maxIter) break;
-        if (pc && restarts > 0 && rel > 0.5 * prev_rel) { pc = nullptr; fallback = true; }
+        if (have && restarts > 0 && rel > 0.5 * prev_rel) { pc = nullptr; have = false; fallback = true; }
         prev_rel = rel;
         launch_scale(c.s, Vp(0), k.r, 1.0 / beta, L);   // one reciprocal, not an FP64 division per element
         std::fill(gv.begin(), gv.end(), 0.0);
@@ -241,8 +346,12 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
         bool bad = false, degenerate = false;
         for (; j < m; ++j) {
             double* w = Vp(j + 1);
-            if (pc) {
-                if ((st = pc->apply(c.s, g, c.mu, Vp(j), Zp(j), k.scal + 8, c.partials, c.err)) != PIC_OK) return st;
+            if (have) {
+                if (pc) {
+                    if ((st = pc->apply(c.s, g, c.mu, Vp(j), Zp(j), k.scal + 8, c.partials, c.err)) != PIC_OK) return st;
+                } else if ((st = inner_apply(c, oc, inner, Vp(j), Zp(j))) != PIC_OK) {
+                    return st;
+                }
                 launch_maxwell_apply(c.s, g, oc, c.mu, Zp(j), w, k.mx);
             } else {
                 launch_maxwell_apply(c.s, g, oc, c.mu, Vp(j), w, k.mx);
@@ -276,7 +385,7 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             // only the second pass copies values back; otherwise the host's
             // Givens update overlaps the normalisation and the next apply
             if (second) CKS(cudaStreamSynchronize(c.s));
-            if (pc) {
+            if (have) {
                 // a non-finite direction, or one already in the Krylov space
                 // (|h_{j+1,j}| below 1e-10 |A z_j|), ends the cycle
                 bool fin = std::isfinite(h1[j + 1]);
@@ -305,8 +414,9 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             ++total;
             if (std::fabs(gv[j + 1]) / bnorm <= tol || total >= maxIter || h1[j + 1] == 0) { ++j; break; }
         }
-        if (bad) {   // the network produced a non-finite direction: drop the cycle
+        if (bad) {   // the preconditioner produced a non-finite direction: drop the cycle
             pc = nullptr;
+            have = false;
             fallback = true;
             ++restarts;
             continue;
@@ -318,17 +428,17 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
             y[i] = Hm(i, i) != 0 ? s / Hm(i, i) : 0.0;
         }
         CKS(cudaMemcpyAsync(k.ydev, y.data(), sizeof(double) * std::max(kk, 1), cudaMemcpyHostToDevice, c.s));
-        if (pc) {
+        if (have) {
             // keep x and r: a preconditioned cycle that raises the true
             // residual (rounding with nearly dependent directions) is undone
             CKS(cudaMemcpyAsync(Vp(0), x, sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
             CKS(cudaMemcpyAsync(Vp(1), k.r, sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
         }
-        launch_combine(c.s, x, pc ? k.Z : k.V, L, kk, k.ydev, 1.0, 1, L);
+        launch_combine(c.s, x, have ? k.Z : k.V, L, kk, k.ydev, 1.0, 1, L);
         launch_maxwell_apply(c.s, g, oc, c.mu, x, k.w, k.mx);
         launch_residual(c.s, k.r, b, k.w, L);
         ++restarts;
-        if (pc) {
+        if (have) {
             launch_dot(c.s, k.r, k.r, L, k.part, P, k.scal, 1);
             const double after = read1(c, k.scal, &st) / bnorm;
             if (st != PIC_OK) return st;
@@ -337,7 +447,7 @@ pic_status gmres_restarted(SolveCtx& c, const OpCoef& oc, const double* b, doubl
                 CKS(cudaMemcpyAsync(k.r, Vp(1), sizeof(double) * L, cudaMemcpyDeviceToDevice, c.s));
                 degenerate = true;
             }
-            if (degenerate) { pc = nullptr; fallback = true; }
+            if (degenerate) { pc = nullptr; have = false; fallback = true; }
         }
     }
     if (net && (st = net->check_tc(c.s, c.err)) != PIC_OK) return st;
@@ -375,6 +485,10 @@ pic_status krylov_solve(SolveCtx& c, const double* rhs, double* x, const pic_sol
             } else {
                 st = gmres_restarted(c, oc, rhs, x, o, info, c.net);
             }
+            break;
+        case PIC_FGMRES_MIXED:
+            st = o.inner < 0 || o.inner > 64 ? err(c, PIC_ERR_ARG, "inner steps must lie in 0..64")
+                                              : gmres_restarted(c, oc, rhs, x, o, info, nullptr, o.inner > 0 ? o.inner : 12);
             break;
         default: st = err(c, PIC_ERR_ARG, "unknown solver method"); break;
     }

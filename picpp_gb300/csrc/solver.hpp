@@ -22,6 +22,15 @@ struct Krylov {
     int cap = 0;
     int zcap = 0;
     long long L = 0;
+    // inner FP32 solve of the mixed-precision preconditioner
+    float* mu32 = nullptr;    // FP32 copy of mu (9N)
+    float* V32 = nullptr;     // FP32 basis, steps32 + 1 vectors of length L
+    float* w32 = nullptr;     // FP32 scratch vector
+    float* mx32 = nullptr;    // mu x of the FP32 apply
+    double* h32 = nullptr;    // Arnoldi scalars of one inner solve (FP64)
+    double* part32 = nullptr; // reduction partials, (steps32 + 2) * 1024
+    unsigned* cnt32 = nullptr; // last-block counter of the FP32 reductions (zero between launches)
+    int steps32 = 0;
 };
 
 class Net;

@@ -90,12 +90,13 @@ __global__ void k_wall_rhs(GridP g, const double* __restrict__ rho_ext, int ex, 
 // The boundary rows of the operator, over y = A x of the interior rows:
 // wall node E_x(0) - E_x(1), E_y(0), E_z(0); identity rows on nodes nx - 2
 // and nx - 1.
-__global__ void k_wall_rows(GridP g, const double* __restrict__ x, double* __restrict__ y) {
+template <typename T>
+__global__ void k_wall_rows(GridP g, const T* __restrict__ x, T* __restrict__ y) {
     const long long N = g.N;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)g.ny * g.nz;
          e += (long long)gridDim.x * blockDim.x) {
         const long long row = e * g.nx;
-        y[row] = x[row] * 1.0 + x[row + 1] * -1.0;
+        y[row] = x[row] * T(1) + x[row + 1] * T(-1);
         y[N + row] = x[N + row];
         y[2 * N + row] = x[2 * N + row];
 #pragma unroll

@@ -445,6 +445,68 @@ def test_gmres_restarted_reaches_true_residual(pg):
     assert info["restarts"] >= 1
 
 
+@pytest.mark.parametrize("inner,wall,n", [(4, 0, 8), (12, 0, 8), (12, 1, 8), (8, 0, 5)])
+def test_mixed_fgmres_reaches_true_residual(pg, inner, wall, n):
+    """FGMRES in FP64 around the FP32 inner solve: the FP64 true residual
+    reaches the tolerance, in far fewer outer iterations than plain
+    GMRES(10) needs, and the solution is the plain one to the tolerance
+    (periodic and wall boxes; the operator's identity rows of a wall box are
+    solved exactly by the FP32 apply too).  n = 5: a vector length (375) that
+    is not a multiple of 4 takes the scalar FP32 kernels."""
+    box = I.Box(n, n, n, 0.5, 0.5, 0.5, 0.5)
+    rng = np.random.default_rng(5)
+    N = box.ncells
+    mu = np.zeros(9 * N)
+    for a in range(3):
+        mu[4 * a * N:(4 * a + 1) * N] = -0.8 * rng.random(N)
+    mu += 0.01 * rng.standard_normal(9 * N)
+    rhs = rng.standard_normal(3 * N)
+    kw = dict(boundary_x=pg.BOUNDARY_WALL_OPEN) if wall else {}
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1, pressure_compat=0, **kw)
+    xp, ip = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.GMRES_RESTARTED, restart=10, max_iter=2000, tol=1e-10))
+    x, info = sim.maxwell_solve(mu, rhs, pg.solve_opts(pg.FGMRES_MIXED, restart=10, max_iter=200, tol=1e-10,
+                                                      inner=inner))
+    g = O.make_grid(box, wall_x=wall)
+    r = O.maxwell_apply(g, mu, x) - rhs
+    assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1e-10 * 1.01
+    assert info["rel_residual"] <= 1e-10
+    assert info["used_fallback"] == 0
+    assert info["iterations"] < ip["iterations"]
+    assert rel_err(x, xp) < 1e-8
+
+
+def test_mixed_fgmres_rejects_bad_inner_length(pg):
+    box = I.Box(4, 4, 4, 0.5, 0.5, 0.5, 0.5)
+    N = box.ncells
+    sim = pg.GpuSimulation(box, pg.IMPLICIT, particle_real=1)
+    for k in (-1, 65):
+        with pytest.raises(pg.PicError):
+            sim.maxwell_solve(np.zeros(9 * N), np.ones(3 * N), pg.solve_opts(pg.FGMRES_MIXED, inner=k))
+
+
+@pytest.mark.parametrize("real", [0, 1])
+def test_implicit_steps_with_mixed_fgmres_match_oracle(pg, real):
+    """Implicit steps whose field solve is the mixed-precision FGMRES to
+    1e-10 against the oracle's reference GMRES: agreement to the solve
+    tolerance (FP64 particles) or the FP32 bound."""
+    st = implicit_state(ppc=2)
+    steps = 3
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=real, sort_every=1, tile=(8, 6, 5))
+    sim.upload_state(st)
+    for _ in range(steps):
+        info = sim.implicit_step(pg.solve_opts(pg.FGMRES_MIXED, restart=10, max_iter=100, tol=1e-10, inner=8))
+        assert info["rel_residual"] <= 1e-10
+    E, B, _ = sim.download_fields()
+    g = O.make_grid(st.box)
+    sp = copy_species(st.species)
+    Eo, Bo = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(steps):
+        O.implicit_step(g, sp, Eo, Bo)
+    tol = 1e-8 if real else TOL32
+    assert rel_err(E.reshape(-1), Eo) < tol
+    assert rel_err(B.reshape(-1), Bo) < tol
+
+
 @pytest.mark.parametrize("real", [1, 0])
 def test_implicit_step_matches_oracle(pg, real):
     st = implicit_state(ppc=2)

@@ -225,6 +225,36 @@ __device__ __forceinline__ void add_runs_fx(unsigned* __restrict__ lo, int* __re
     __syncwarp();
 }
 
+// Asynchronous global -> shared copies of 4 or 8 bytes (cp.async, no
+// registers held while in flight).
+template <int B>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (B == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// A warp's staged chunk of particles: cell, then ox oy oz px py pz, 32 each.
+template <typename TP>
+struct ChunkBuf {
+    TP a[6][32];
+    int cell[32];
+};
+
+// Starts the copy of particle n (this lane's slot) into the warp's buffer.
+template <typename TP>
+__device__ __forceinline__ void stage_particle(ChunkBuf<TP>* buf, const PartView<TP>& P, long long n, int lane) {
+    cp_async<4>(&buf->cell[lane], P.cell + n);
+    cp_async<sizeof(TP)>(&buf->a[0][lane], P.ox + n);
+    cp_async<sizeof(TP)>(&buf->a[1][lane], P.oy + n);
+    cp_async<sizeof(TP)>(&buf->a[2][lane], P.oz + n);
+    cp_async<sizeof(TP)>(&buf->a[3][lane], P.px + n);
+    cp_async<sizeof(TP)>(&buf->a[4][lane], P.py + n);
+    cp_async<sizeof(TP)>(&buf->a[5][lane], P.pz + n);
+}
+
 // CT: compile-time tile extent of a cubic 3-D tile (8), or 0 for shapes read
 // from TileShape at run time.  kWall: conductor-wall box (GridP::wall), the
 // Tristan mover's reflection and escape and the zigzag wall term
@@ -246,9 +276,12 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
     TP* sJ = reinterpret_cast<TP*>(smem_raw + ((6 * F * sizeof(TF) + 15) & ~size_t(15)));   // 3 * JC (FP64)
     unsigned* sLo = reinterpret_cast<unsigned*>(sJ);                                        // 3 * JC (FP32)
     int* sHi = reinterpret_cast<int*>(sLo + 3 * JC);                                        // 3 * JC (FP32)
-    // FP32: the warps' spread scratch after the block
-    float* sW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(sJ) + ((24 * JC + 15) & ~15ll) +
-                                         (threadIdx.x >> 5) * kSpreadBytes);
+    // FP32: the warps' spread scratch after the block; then every warp's
+    // staged chunk of particles
+    unsigned char* after_j = reinterpret_cast<unsigned char*>(sJ) + ((24 * JC + 15) & ~15ll);
+    float* sW = reinterpret_cast<float*>(after_j + (threadIdx.x >> 5) * kSpreadBytes);
+    ChunkBuf<TP>* sBuf = reinterpret_cast<ChunkBuf<TP>*>(after_j + (kFixed ? (blockDim.x >> 5) * kSpreadBytes : 0)) +
+                         (threadIdx.x >> 5);
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int T3 = tx * ty * tz;
     const long long N = g.N;
@@ -285,18 +318,27 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
             const TP beta = q * dt / (TP(2) * m);
             const TP fcd = q * S.w[sp] / vol;
             const long long pb = S.off[sp][(long long)tile * T3], pe = S.off[sp][(long long)(tile + 1) * T3];
-            // CTA-uniform chunk loop: warp w takes particles cb + 32 w + lane
+            // CTA-uniform chunk loop: warp w takes particles cb + 32 w + lane.
+            // Each warp's next chunk is copied into its shared buffer while
+            // it pushes the current one (the first before the loop).
+            if (pb + threadIdx.x < pe) stage_particle(sBuf, P, pb + threadIdx.x, lane);
+            cp_async_commit();
             for (long long cb = pb; cb < pe; cb += blockDim.x) {
                 const long long n = cb + threadIdx.x;
                 TP aB[12];
                 TP s1[6] = {TP(0), TP(0), TP(0), TP(0), TP(0), TP(0)};   // F1 and W1 of the old-side segment
                 int keyA = -1 - lane, keyB = -1 - lane;   // lanes outside a reduction keep unique keys
                 bool push_later = false, deposit_later = false;
-                const int cell = n < pe ? P.cell[n] : -1;
+                // a lane reads and refills only its own slots, and the wait
+                // covers the copies it started itself
+                cp_async_wait_all();
+                const int cell = n < pe ? sBuf->cell[lane] : -1;
+                TP ox = sBuf->a[0][lane], oy = sBuf->a[1][lane], oz = sBuf->a[2][lane];
+                TP mom[3] = {sBuf->a[3][lane], sBuf->a[4][lane], sBuf->a[5][lane]};
+                if (n + blockDim.x < pe) stage_particle(sBuf, P, n + blockDim.x, lane);
+                cp_async_commit();
                 // (an escaped particle of a wall box waits with cell -1 for the sort)
                 if (n < pe && (!kWall || cell >= 0)) {
-                    TP ox = P.ox[n], oy = P.oy[n], oz = P.oz[n];
-                    TP mom[3] = {P.px[n], P.py[n], P.pz[n]};
                     int i, j, k;
                     decode(g, cell, i, j, k);
                     auto local = [](int c, int lo, int te, int nn) {

@@ -181,7 +181,9 @@ size_t PK<T>::tile_smem_bytes(const TileShape& sh) {
     // FP32: the current block is 64-bit fixed point in two 32-bit words,
     // followed by the warps' scratch for spreading the run heads' adds
     const size_t fixed_scratch = sizeof(T) == 4 ? (size_t)(kTileThreads / 32) * kSpreadBytes : 0;
-    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + ((3 * (size_t)sh.jcells * 8 + 15) & ~size_t(15)) + fixed_scratch;
+    // and every warp's staged chunk of particles
+    return ((6 * F * sizeof(T) + 15) & ~size_t(15)) + ((3 * (size_t)sh.jcells * 8 + 15) & ~size_t(15)) + fixed_scratch +
+           (size_t)(kTileThreads / 32) * sizeof(ChunkBuf<T>);
 }
 
 template <typename T>

@@ -225,17 +225,6 @@ __device__ __forceinline__ void add_runs_fx(unsigned* __restrict__ lo, int* __re
     __syncwarp();
 }
 
-// Asynchronous global -> shared copies of 4 or 8 bytes (cp.async, no
-// registers held while in flight).
-template <int B>
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    if constexpr (B == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 // A warp's staged chunk of particles: cell, then ox oy oz px py pz, 32 each.
 template <typename TP>
 struct ChunkBuf {

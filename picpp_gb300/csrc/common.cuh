@@ -87,6 +87,18 @@ template <typename T> __device__ __forceinline__ T dev_floor(T x);
 template <> __device__ __forceinline__ double dev_floor<double>(double x) { return floor(x); }
 template <> __device__ __forceinline__ float dev_floor<float>(float x) { return floorf(x); }
 
+// Asynchronous global -> shared copies of 4 or 8 bytes (cp.async, no
+// registers held while in flight); the wait covers the copies the calling
+// thread started.
+template <int B>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (B == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Particle state of one species, SoA in device memory.
 template <typename T>
 struct PartView {

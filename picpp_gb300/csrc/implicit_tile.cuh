@@ -633,6 +633,23 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
     T* sE = kVec ? reinterpret_cast<T*>(sB4 + mb.CB) : reinterpret_cast<T*>(mv_smem);   // [3][NB]
     T* sEt = sE + 3 * mb.NB;                 // [3][NB] (FP64)
     T* sB = sEt + 3 * mb.NB;                 // [3][CB] (FP64)
+    // after the field blocks: every thread's next particle, copied with
+    // cp.async while it moves the current one ([6][threads] values, then
+    // [threads] cells)
+    const size_t fld = kVec ? ((size_t)mb.NB + mb.CB) * 16 + 3 * (size_t)mb.NB * sizeof(float)
+                            : (6 * (size_t)mb.NB + 3 * (size_t)mb.CB) * sizeof(T);
+    T* sPre = reinterpret_cast<T*>(mv_smem + ((fld + 15) & ~size_t(15)));
+    int* sPreCell = reinterpret_cast<int*>(sPre + 6 * blockDim.x);
+    auto stage = [&](const PartView<T>& pv, int m) {
+        const int me = threadIdx.x, bdim = blockDim.x;
+        cp_async<4>(&sPreCell[me], pv.cell + m);
+        cp_async<sizeof(T)>(&sPre[0 * bdim + me], pv.ox + m);
+        cp_async<sizeof(T)>(&sPre[1 * bdim + me], pv.oy + m);
+        cp_async<sizeof(T)>(&sPre[2 * bdim + me], pv.oz + m);
+        cp_async<sizeof(T)>(&sPre[3 * bdim + me], pv.px + m);
+        cp_async<sizeof(T)>(&sPre[4 * bdim + me], pv.py + m);
+        cp_async<sizeof(T)>(&sPre[5 * bdim + me], pv.pz + m);
+    };
     const int ntiles = t.ntx * t.nty * t.ntz;
     const int T3 = t.tx * t.ty * t.tz;
     const bool ax = g.nx > 1, ay = g.y3, az = g.z3;
@@ -679,9 +696,18 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
             const T qdt = T(qs * g.dt);
             const T mm = T(ms);
             const int b0 = S.off[s][tile * T3], b1 = S.off[s][(tile + 1) * T3];
+            if (b0 + (int)threadIdx.x < b1) stage(p, b0 + threadIdx.x);
+            cp_async_commit();
             for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x) {
+                cp_async_wait_all();   // this thread's particle n (its own slot)
+                const int bdim = blockDim.x, me = threadIdx.x;
+                const int cell_n = sPreCell[me];
+                const T pu[3] = {sPre[0 * bdim + me], sPre[1 * bdim + me], sPre[2 * bdim + me]};
+                const T pm[3] = {sPre[3 * bdim + me], sPre[4 * bdim + me], sPre[5 * bdim + me]};
+                if (n + bdim < b1) stage(p, n + bdim);
+                cp_async_commit();
                 int ci[3];
-                decode(g, p.cell[n], ci[0], ci[1], ci[2]);
+                decode(g, cell_n, ci[0], ci[1], ci[2]);
                 // A position (cell c, offset u) is located once: its node and cell
                 // stencils in the staged block (bases, upper weights), shared by the
                 // two or three gathers there; a stencil that leaves the block
@@ -743,8 +769,8 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
                     else gat(L, sB, false, out);
                 };
                 auto defer = [&]() { atomicOr(&S.defer[s][n >> 5], 1u << (n & 31)); };
-                T u0[3] = {p.ox[n], p.oy[n], p.oz[n]};
-                T mom0[3] = {p.px[n], p.py[n], p.pz[n]};
+                T u0[3] = {pu[0], pu[1], pu[2]};
+                T mom0[3] = {pm[0], pm[1], pm[2]};
                 T gam, v[3];
                 gamma_vel<T>(mom0, mm, gam, v);
                 T e[3], b[3], al[9];

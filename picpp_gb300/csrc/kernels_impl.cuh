@@ -295,9 +295,11 @@ bool PK<T>::implicit_push_tiled(cudaStream_t s, const GridP& g, const TileGeom& 
     mb.NB = mb.nbx * mb.nby * mb.nbz;
     mb.CB = mb.cbx * mb.cby * mb.cbz;
     // FP32: E^theta and B^n as float4 nodes / cells, E^n as three planes
-    const size_t smem = sizeof(T) == sizeof(float)
-                            ? ((size_t)mb.NB + (size_t)mb.CB) * 16 + 3 * (size_t)mb.NB * sizeof(float)
-                            : (6 * (size_t)mb.NB + 3 * (size_t)mb.CB) * sizeof(T);
+    const size_t fld = sizeof(T) == sizeof(float)
+                           ? ((size_t)mb.NB + (size_t)mb.CB) * 16 + 3 * (size_t)mb.NB * sizeof(float)
+                           : (6 * (size_t)mb.NB + 3 * (size_t)mb.CB) * sizeof(T);
+    // plus every thread's staged next particle (6 values and a cell)
+    const size_t smem = ((fld + 15) & ~size_t(15)) + (size_t)kMoverThreads * (6 * sizeof(T) + sizeof(int));
     if (smem > 227 * 1024) return false;
     static bool attr_set = false;
     if (!attr_set) {

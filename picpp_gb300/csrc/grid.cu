@@ -93,7 +93,12 @@ void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, cons
 void launch_maxwell_apply_f32(cudaStream_t s, const GridP& g, const OpCoef& oc, const float* mu, const float* x,
                               float* y, float* wmu) {
     k_mu_times<float><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
-    k_maxwell_stencil<float><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
+    if (g.nx % ZM_TX == 0 && g.ny % ZM_TY == 0 && g.nz >= 3 && oc.has[0] && oc.has[1] && oc.has[2]) {
+        const dim3 grid(g.nx / ZM_TX, g.ny / ZM_TY, (g.nz + ZM_ZC - 1) / ZM_ZC);
+        k_maxwell_stencil_zm<<<grid, ZM_TX * ZM_TY, 0, s>>>(g, oc, x, wmu, y);
+    } else {
+        k_maxwell_stencil<float><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
+    }
     if (g.wall) k_wall_rows<float><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
 }
 

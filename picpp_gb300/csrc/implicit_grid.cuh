@@ -302,6 +302,88 @@ __global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, con
     }
 }
 
+// Pass 2 in FP32 for 3-D boxes whose x and y extents are multiples of ZM_TX
+// and ZM_TY (the inner solve of the mixed-precision preconditioner): a block
+// owns a ZM_TX x ZM_TY column of cells and ZM_ZC consecutive z planes, and
+// marches up z with the planes z - 1, z, z + 1 of x and w (one cell of halo
+// in x and y, periodic) rotating through shared memory, so each value is
+// read from memory once per block instead of once per stencil point.  Same
+// terms as k_maxwell_stencil.
+constexpr int ZM_TX = 32, ZM_TY = 8, ZM_ZC = 8;
+__global__ void __launch_bounds__(ZM_TX * ZM_TY) k_maxwell_stencil_zm(GridP g, OpCoef oc, const float* __restrict__ x,
+                                                                      const float* __restrict__ w,
+                                                                      float* __restrict__ y) {
+    constexpr int SX = ZM_TX + 2, SY = ZM_TY + 2, PL = SX * SY;
+    __shared__ float sx[3][3][PL], sw[3][3][PL];   // [plane slot][component][y][x]
+    const long long N = g.N;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int tx = threadIdx.x % ZM_TX, ty = threadIdx.x / ZM_TX;
+    const int i0 = blockIdx.x * ZM_TX, j0 = blockIdx.y * ZM_TY, z0 = blockIdx.z * ZM_ZC;
+    const int z1 = z0 + ZM_ZC < nz ? z0 + ZM_ZC : nz;
+    const float diag = float(1.0 + 2.0 * (oc.kd2[0] + oc.kd2[1] + oc.kd2[2]));
+    float c1[3], kd2[3], kx4[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c1[a] = float(1.0 + 2.0 * oc.kd2[a]);
+        kd2[a] = float(oc.kd2[a]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) kx4[a][d] = float(oc.kx4[a][d]);
+    }
+    // plane z (periodic) of x and w with its halo into slot sl
+    auto load = [&](int z, int sl) {
+        const int zz = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+        for (int e = threadIdx.x; e < PL; e += ZM_TX * ZM_TY) {
+            const int hx = e % SX, hy = e / SX;
+            int ii = i0 + hx - 1, jj = j0 + hy - 1;
+            ii = ii < 0 ? ii + nx : (ii >= nx ? ii - nx : ii);
+            jj = jj < 0 ? jj + ny : (jj >= ny ? jj - ny : jj);
+            const long long id = ((long long)zz * ny + jj) * nx + ii;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                sx[sl][a][e] = x[a * N + id];
+                sw[sl][a][e] = w[a * N + id];
+            }
+        }
+    };
+    load(z0 - 1, 0);
+    load(z0, 1);
+    int sm = 0, sc = 1;   // slots of planes z - 1 and z
+    for (int z = z0; z < z1; ++z) {
+        const int sp = 3 - sm - sc;   // slot of plane z + 1
+        load(z + 1, sp);
+        __syncthreads();
+        const int slot[3] = {sm, sc, sp};
+        // value of field F, component a, at offset (dx, dy, dz) from this cell
+        auto X = [&](int a, int dx, int dy, int dz) { return sx[slot[dz + 1]][a][(ty + 1 + dy) * SX + tx + 1 + dx]; };
+        auto Wv = [&](int a, int dx, int dy, int dz) { return sw[slot[dz + 1]][a][(ty + 1 + dy) * SX + tx + 1 + dx]; };
+        const long long c = ((long long)z * ny + (j0 + ty)) * nx + (i0 + tx);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float acc = fmaf(-c1[a], Wv(a, 0, 0, 0), diag * X(a, 0, 0, 0));
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const int ux = ax == 0, uy = ax == 1, uz = ax == 2;
+                const float xs = X(a, ux, uy, uz) + X(a, -ux, -uy, -uz);
+                if (ax == a) acc = fmaf(kd2[ax], (Wv(a, ux, uy, uz) + Wv(a, -ux, -uy, -uz)) - xs, acc);
+                else acc = fmaf(-kd2[ax], xs, acc);
+            }
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (d == a) continue;
+                const int ax_ = a == 0, ay_ = a == 1, az_ = a == 2;
+                const int dx_ = d == 0, dy_ = d == 1, dz_ = d == 2;
+                const float sum = (Wv(d, ax_ + dx_, ay_ + dy_, az_ + dz_) - Wv(d, ax_ - dx_, ay_ - dy_, az_ - dz_)) -
+                                  (Wv(d, -ax_ + dx_, -ay_ + dy_, -az_ + dz_) - Wv(d, -ax_ - dx_, -ay_ - dy_, -az_ - dz_));
+                acc = fmaf(kx4[a][d], sum, acc);
+            }
+            y[a * N + c] = acc;
+        }
+        __syncthreads();   // every thread is done with slot sm before it is refilled
+        sm = sc;
+        sc = sp;
+    }
+}
+
 // Transpose of the operator (k_mu_times + k_maxwell_stencil).  The operator splits as A x = P x + Q (mu x)
 // with P and Q constant-coefficient periodic stencils that are symmetric
 // (P: the diagonal and the -K/d^2 neighbour couplings; Q: -c1 on the node,

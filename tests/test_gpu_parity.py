@@ -445,15 +445,18 @@ def test_gmres_restarted_reaches_true_residual(pg):
     assert info["restarts"] >= 1
 
 
-@pytest.mark.parametrize("inner,wall,n", [(4, 0, 8), (12, 0, 8), (12, 1, 8), (8, 0, 5)])
+@pytest.mark.parametrize("inner,wall,n", [(4, 0, (8, 8, 8)), (12, 0, (8, 8, 8)), (12, 1, (8, 8, 8)), (8, 0, (5, 5, 5)),
+                                          (8, 0, (32, 8, 4)), (8, 1, (64, 16, 3))])
 def test_mixed_fgmres_reaches_true_residual(pg, inner, wall, n):
     """FGMRES in FP64 around the FP32 inner solve: the FP64 true residual
     reaches the tolerance, in far fewer outer iterations than plain
     GMRES(10) needs, and the solution is the plain one to the tolerance
     (periodic and wall boxes; the operator's identity rows of a wall box are
-    solved exactly by the FP32 apply too).  n = 5: a vector length (375) that
-    is not a multiple of 4 takes the scalar FP32 kernels."""
-    box = I.Box(n, n, n, 0.5, 0.5, 0.5, 0.5)
+    solved exactly by the FP32 apply too).  5^3: a vector length (375) that
+    is not a multiple of 4 takes the scalar FP32 kernels; 32 x 8 x 4 and
+    64 x 16 x 3 take the z-marching FP32 stencil (one and several blocks
+    along x and y, three z planes)."""
+    box = I.Box(*n, 0.5, 0.5, 0.5, 0.5)
     rng = np.random.default_rng(5)
     N = box.ncells
     mu = np.zeros(9 * N)

@@ -108,9 +108,11 @@ typedef enum {
     PIC_FGMRES_LEARNED = 2,  /* flexible GMRES(restart) with the learned right
                                 preconditioner; plain GMRES when it stalls       */
     PIC_FGMRES_MIXED = 3     /* flexible GMRES(restart) in FP64 whose right
-                                preconditioner is an FP32 GMRES solve of `inner`
-                                Arnoldi steps (the FP64 true residual still
-                                reaches tol); plain GMRES when it stalls         */
+                                preconditioner is an FP32 GMRES solve of at most
+                                `inner` Arnoldi steps, stopped as soon as it
+                                meets what the outer iteration needs (the FP64
+                                true residual still reaches tol); plain GMRES
+                                when it stalls                                  */
 } pic_gmres_method;
 
 typedef struct {
@@ -118,8 +120,8 @@ typedef struct {
     int restart;             /* Krylov vectors per cycle (methods 1-3)        */
     int max_iter;            /* total iteration cap (outer iterations)        */
     double tol;              /* relative residual target                      */
-    int inner;               /* PIC_FGMRES_MIXED: FP32 steps per apply, 0..64
-                                (0: 12)                                        */
+    int inner;               /* PIC_FGMRES_MIXED: at most this many FP32 steps
+                                per apply, 0..64 (0: 12)                       */
 } pic_solve_opts;
 
 typedef struct {

@@ -83,23 +83,23 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
 
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
                           double* y, double* wmu) {
-    k_mu_times<double><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
-    k_maxwell_stencil<double><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
-    if (g.wall) k_wall_rows<double><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
+    k_mu_times<double><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu, nullptr);
+    k_maxwell_stencil<double><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y, nullptr);
+    if (g.wall) k_wall_rows<double><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y, nullptr);
 }
 
 // The same operator in FP32 (inner solve of the mixed-precision
 // preconditioner; mu an FP32 copy).
 void launch_maxwell_apply_f32(cudaStream_t s, const GridP& g, const OpCoef& oc, const float* mu, const float* x,
-                              float* y, float* wmu) {
-    k_mu_times<float><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu);
+                              float* y, float* wmu, const unsigned* skip) {
+    k_mu_times<float><<<grid_for(g.N, 256), 256, 0, s>>>(g.N, mu, x, wmu, skip);
     if (g.nx % ZM_TX == 0 && g.ny % ZM_TY == 0 && g.nz >= 3 && oc.has[0] && oc.has[1] && oc.has[2]) {
         const dim3 grid(g.nx / ZM_TX, g.ny / ZM_TY, (g.nz + ZM_ZC - 1) / ZM_ZC);
-        k_maxwell_stencil_zm<<<grid, ZM_TX * ZM_TY, 0, s>>>(g, oc, x, wmu, y);
+        k_maxwell_stencil_zm<<<grid, ZM_TX * ZM_TY, 0, s>>>(g, oc, x, wmu, y, skip);
     } else {
-        k_maxwell_stencil<float><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y);
+        k_maxwell_stencil<float><<<grid_for(g.N, 256), 256, 0, s>>>(g, oc, x, wmu, y, skip);
     }
-    if (g.wall) k_wall_rows<float><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y);
+    if (g.wall) k_wall_rows<float><<<grid_for((long long)g.ny * g.nz, 256), 256, 0, s>>>(g, x, y, skip);
 }
 
 void launch_wall_moments(cudaStream_t s, const GridP& g, double* J, double* mu, double* rho, double* Pi,
@@ -316,34 +316,45 @@ void launch_dot_f32(cudaStream_t s, const float* a, const float* b, long long n,
 }
 
 void launch_multi_dot_f32(cudaStream_t s, const float* V, long long ld, int k, const float* w, long long n,
-                          double* partials, int P, double* out, unsigned* counter) {
+                          double* partials, int P, double* out, unsigned* counter, const unsigned* skip) {
     const bool v4 = vec4_ok(n, {V, w}) && ld % 4 == 0;
     for (int k0 = 0; k0 < k; k0 += 8) {
-        if (v4) k_multi_dot_f32<8, 4><<<P, kRedThreads, 0, s>>>(V, ld / 4, k0, k, w, n / 4, partials, out, counter);
-        else k_multi_dot_f32<8, 1><<<P, kRedThreads, 0, s>>>(V, ld, k0, k, w, n, partials, out, counter);
+        if (v4)
+            k_multi_dot_f32<8, 4><<<P, kRedThreads, 0, s>>>(V, ld / 4, k0, k, w, n / 4, partials, out, counter, skip);
+        else
+            k_multi_dot_f32<8, 1><<<P, kRedThreads, 0, s>>>(V, ld, k0, k, w, n, partials, out, counter, skip);
     }
 }
 
 void launch_axpy_norm_f32(cudaStream_t s, float* w, const float* V, long long ld, int k, const double* h, long long n,
-                          double* partials, int P, double* out, unsigned* counter) {
+                          double* partials, int P, double* out, unsigned* counter, const unsigned* skip) {
     if (vec4_ok(n, {V, w}) && ld % 4 == 0)
-        k_axpy_norm_f32<4><<<P, kRedThreads, 0, s>>>(w, V, ld / 4, k, h, n / 4, partials, out, counter);
+        k_axpy_norm_f32<4><<<P, kRedThreads, 0, s>>>(w, V, ld / 4, k, h, n / 4, partials, out, counter, skip);
     else
-        k_axpy_norm_f32<1><<<P, kRedThreads, 0, s>>>(w, V, ld, k, h, n, partials, out, counter);
+        k_axpy_norm_f32<1><<<P, kRedThreads, 0, s>>>(w, V, ld, k, h, n, partials, out, counter, skip);
 }
 
-void launch_normalize_f32(cudaStream_t s, float* v, const float* w, const double* h2, long long n) {
-    if (vec4_ok(n, {v, w})) k_normalize_f32<4><<<grid_for(n / 4, 256), 256, 0, s>>>(v, w, h2, n / 4);
-    else k_normalize_f32<1><<<grid_for(n, 256), 256, 0, s>>>(v, w, h2, n);
+void launch_normalize_f32(cudaStream_t s, float* v, const float* w, const double* h2, long long n,
+                          const unsigned* skip) {
+    if (vec4_ok(n, {v, w})) k_normalize_f32<4><<<grid_for(n / 4, 256), 256, 0, s>>>(v, w, h2, n / 4, skip);
+    else k_normalize_f32<1><<<grid_for(n, 256), 256, 0, s>>>(v, w, h2, n, skip);
+}
+
+void launch_inner_givens(cudaStream_t s, int j, int S, double* h, double tol, unsigned* flags) {
+    k_inner_givens<<<1, 32, 0, s>>>(j, InnerLayout{S}, h, tol, flags);
+}
+
+void launch_inner_backsolve(cudaStream_t s, int S, double* h, unsigned* flags) {
+    k_inner_backsolve<<<1, 32, 0, s>>>(InnerLayout{S}, h, flags);
 }
 
 void launch_to_f32(cudaStream_t s, float* dst, const double* src, long long n) {
     k_to_f32<<<grid_for(n, 256), 256, 0, s>>>(dst, src, n);
 }
 
-void launch_combine_f32(cudaStream_t s, double* z, const float* V, long long ld, int k, const double* y,
+void launch_combine_f32(cudaStream_t s, double* z, const float* V, long long ld, const unsigned* kp, const double* y,
                         double scale, long long n) {
-    k_combine_f32<<<grid_for(n, 256), 256, 0, s>>>(z, V, ld, k, y, scale, n);
+    k_combine_f32<<<grid_for(n, 256), 256, 0, s>>>(z, V, ld, kp, y, scale, n);
 }
 
 void launch_nonfinite(cudaStream_t s, const double* a, long long n, int* flag) {

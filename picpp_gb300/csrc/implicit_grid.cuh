@@ -241,9 +241,12 @@ __device__ __forceinline__ void mu_times(const T* __restrict__ mu, long long N, 
 // it (centre, 6 neighbours, 12 corners: about 190 operations per node).
 // Pass 1: w_a = sum_b mu_ab x_b.  T: FP64, or FP32 for the inner solve of
 // the mixed-precision preconditioner.
+// skip (FP32 inner solve, else nullptr): return at once when it is set.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mu_times(long long N, const T* __restrict__ mu,
-                                                  const T* __restrict__ x, T* __restrict__ w) {
+                                                  const T* __restrict__ x, T* __restrict__ w,
+                                                  const unsigned* __restrict__ skip) {
+    if (skip && *skip) return;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
         T wc[3];
@@ -258,7 +261,9 @@ __global__ void __launch_bounds__(256) k_mu_times(long long N, const T* __restri
 // K/(4 da dd) (w_d(++) - w_d(+-) - w_d(-+) + w_d(--)).  Periodic box.
 template <typename T>
 __global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, const T* __restrict__ x,
-                                                         const T* __restrict__ w, T* __restrict__ y) {
+                                                         const T* __restrict__ w, T* __restrict__ y,
+                                                         const unsigned* __restrict__ skip) {
+    if (skip && *skip) return;
     const long long N = g.N;
     const int n[3] = {g.nx, g.ny, g.nz};
     const long long st[3] = {1, (long long)g.nx, (long long)g.nx * g.ny};
@@ -312,7 +317,9 @@ __global__ void __launch_bounds__(256) k_maxwell_stencil(GridP g, OpCoef oc, con
 constexpr int ZM_TX = 32, ZM_TY = 8, ZM_ZC = 8;
 __global__ void __launch_bounds__(ZM_TX * ZM_TY) k_maxwell_stencil_zm(GridP g, OpCoef oc, const float* __restrict__ x,
                                                                       const float* __restrict__ w,
-                                                                      float* __restrict__ y) {
+                                                                      float* __restrict__ y,
+                                                                      const unsigned* __restrict__ skip) {
+    if (*skip) return;
     constexpr int SX = ZM_TX + 2, SY = ZM_TY + 2, PL = SX * SY;
     __shared__ float sx[3][3][PL], sw[3][3][PL];   // [plane slot][component][y][x]
     const long long N = g.N;

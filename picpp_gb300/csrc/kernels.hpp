@@ -103,7 +103,7 @@ void launch_maxwell_rhs(cudaStream_t s, const GridP& g, const double* E, const d
 void launch_maxwell_apply(cudaStream_t s, const GridP& g, const OpCoef& oc, const double* mu, const double* x,
                           double* y, double* wmu);
 void launch_maxwell_apply_f32(cudaStream_t s, const GridP& g, const OpCoef& oc, const float* mu, const float* x,
-                              float* y, float* wmu);
+                              float* y, float* wmu, const unsigned* skip);
 // conductor wall at x = 0 / open boundary at x = (nx - 2) dx (wall.cuh)
 void launch_wall_moments(cudaStream_t s, const GridP& g, double* J, double* mu, double* rho, double* Pi,
                          int pi_mirror);
@@ -134,19 +134,40 @@ void launch_scale(cudaStream_t s, double* v, const double* w, double sc, long lo
 void launch_div(cudaStream_t s, double* v, const double* w, double d, long long n);
 void launch_combine(cudaStream_t s, double* x, const double* V, long long ld, int k, const double* y, double scale,
                     int accumulate, long long n);
+// Offsets of the inner solve's FP64 scalars (one array): [0] |v|^2, [1]
+// |v|, then the Hessenberg columns (column j at h + j (S + 1), rows 0..j),
+// the squared norms of the new basis vectors, the least-squares solution y,
+// the Givens cosines and sines and the rotated right part g.
+struct InnerLayout {
+    int S;
+    __host__ __device__ long long h() const { return 8; }
+    __host__ __device__ long long hn() const { return 8 + (long long)(S + 1) * S; }
+    __host__ __device__ long long y() const { return hn() + S; }
+    __host__ __device__ long long cs() const { return y() + S + 1; }
+    __host__ __device__ long long sn() const { return cs() + S; }
+    __host__ __device__ long long g() const { return sn() + S; }
+    __host__ __device__ long long size() const { return g() + S + 1; }
+};
+
 // FP32 vectors of the mixed-precision preconditioner (FP64 partials, outputs
 // and coefficients; each reduction one launch, finished by its last block,
-// counter: a zeroed device word)
+// counter: a zeroed device word; skip: the inner solve's done flag, the
+// kernel returns at once when it is set)
 void launch_dot_f32(cudaStream_t s, const float* a, const float* b, long long n, double* partials, int P,
                     double* out, unsigned* counter);
 void launch_multi_dot_f32(cudaStream_t s, const float* V, long long ld, int k, const float* w, long long n,
-                          double* partials, int P, double* out, unsigned* counter);
+                          double* partials, int P, double* out, unsigned* counter, const unsigned* skip);
 void launch_axpy_norm_f32(cudaStream_t s, float* w, const float* V, long long ld, int k, const double* h, long long n,
-                          double* partials, int P, double* out, unsigned* counter);
-void launch_normalize_f32(cudaStream_t s, float* v, const float* w, const double* h2, long long n);
+                          double* partials, int P, double* out, unsigned* counter, const unsigned* skip);
+void launch_normalize_f32(cudaStream_t s, float* v, const float* w, const double* h2, long long n,
+                          const unsigned* skip);
 void launch_to_f32(cudaStream_t s, float* dst, const double* src, long long n);
-void launch_combine_f32(cudaStream_t s, double* z, const float* V, long long ld, int k, const double* y,
+void launch_combine_f32(cudaStream_t s, double* z, const float* V, long long ld, const unsigned* kp, const double* y,
                         double scale, long long n);
+// Givens step j and back-substitution of the inner least-squares problem
+// (scalars laid out as InnerLayout{S} in h; flags: [1] done, [2] columns)
+void launch_inner_givens(cudaStream_t s, int j, int S, double* h, double tol, unsigned* flags);
+void launch_inner_backsolve(cudaStream_t s, int S, double* h, unsigned* flags);
 void launch_residual(cudaStream_t s, double* r, const double* b, const double* Ax, long long n);
 void launch_nonfinite(cudaStream_t s, const double* a, long long n, int* flag);
 void launch_finalize(cudaStream_t s, const double* partials, int P, int nvec, double* out, int ostride, int take_sqrt);

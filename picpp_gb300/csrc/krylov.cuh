@@ -4,6 +4,7 @@
 // in device memory so an Arnoldi step needs no host round trip.
 #pragma once
 #include "common.cuh"
+#include "kernels.hpp"
 
 namespace pic {
 
@@ -194,7 +195,9 @@ __global__ void __launch_bounds__(kRedThreads) k_multi_dot_f32(const float* __re
                                                                int k, const float* __restrict__ w_, long long n,
                                                                double* __restrict__ partials,
                                                                double* __restrict__ out,
-                                                               unsigned* __restrict__ counter) {
+                                                               unsigned* __restrict__ counter,
+                                                               const unsigned* __restrict__ skip) {
+    if (*skip) return;   // the inner solve has converged
     using F = F32Vec<W>;
     const typename F::T* V = reinterpret_cast<const typename F::T*>(V_);
     const typename F::T* w = reinterpret_cast<const typename F::T*>(w_);
@@ -228,7 +231,9 @@ __global__ void __launch_bounds__(kRedThreads) k_axpy_norm_f32(float* __restrict
                                                                long long ld, int k, const double* __restrict__ h,
                                                                long long n, double* __restrict__ partials,
                                                                double* __restrict__ out,
-                                                               unsigned* __restrict__ counter) {
+                                                               unsigned* __restrict__ counter,
+                                                               const unsigned* __restrict__ skip) {
+    if (*skip) return;
     using F = F32Vec<W>;
     typename F::T* w = reinterpret_cast<typename F::T*>(w_);
     const typename F::T* V = reinterpret_cast<const typename F::T*>(V_);
@@ -254,7 +259,8 @@ __global__ void __launch_bounds__(kRedThreads) k_axpy_norm_f32(float* __restrict
 // v = w / sqrt(h2[0]) (zero for h2[0] <= 0); one square root per block.
 template <int W>
 __global__ void k_normalize_f32(float* __restrict__ v_, const float* __restrict__ w_, const double* __restrict__ h2,
-                                long long n) {
+                                long long n, const unsigned* __restrict__ skip) {
+    if (*skip) return;
     using F = F32Vec<W>;
     typename F::T* v = reinterpret_cast<typename F::T*>(v_);
     const typename F::T* w = reinterpret_cast<const typename F::T*>(w_);
@@ -275,9 +281,11 @@ __global__ void k_to_f32(float* __restrict__ dst, const double* __restrict__ src
         dst[i] = float(src[i]);
 }
 
-// z = scale * sum_m V[m] y[m] in FP64 (FP32 basis, FP64 coefficients).
-__global__ void k_combine_f32(double* __restrict__ z, const float* __restrict__ V, long long ld, int k,
-                              const double* __restrict__ y, double scale, long long n) {
+// z = scale * sum_m V[m] y[m], m < *kp, in FP64 (FP32 basis, FP64
+// coefficients).
+__global__ void k_combine_f32(double* __restrict__ z, const float* __restrict__ V, long long ld,
+                              const unsigned* __restrict__ kp, const double* __restrict__ y, double scale, long long n) {
+    const int k = (int)*kp;
     __shared__ float ys[64];
     for (int m = threadIdx.x; m < k; m += blockDim.x) ys[m] = float(y[m]);
     __syncthreads();
@@ -286,6 +294,54 @@ __global__ void k_combine_f32(double* __restrict__ z, const float* __restrict__ 
         for (int m = 0; m < k; ++m) s = fmaf(ys[m], V[(long long)m * ld + i], s);
         z[i] = double(s) * scale;
     }
+}
+
+// One Givens step of the inner least-squares problem, on the device (one
+// thread): rotates column j with the previous rotations, forms rotation j
+// from the column's diagonal and the new vector's norm, updates g and sets
+// flags[1] (done) when |g_{j+1}| <= tol |v| or the Krylov space is
+// invariant; flags[2] = the columns in use.
+__global__ void k_inner_givens(int j, InnerLayout L, double* __restrict__ h, double tol, unsigned* __restrict__ flags) {
+    if (threadIdx.x != 0 || flags[1]) return;
+    double* col = h + L.h() + (long long)j * (L.S + 1);
+    double* cs = h + L.cs();
+    double* sn = h + L.sn();
+    double* gv = h + L.g();
+    if (j == 0) {
+        h[1] = sqrt(fmax(h[0], 0.0));
+        gv[0] = h[1];
+    }
+    for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+        col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+        col[i] = t;
+    }
+    const double a = col[j], b = sqrt(fmax(h[L.hn() + j], 0.0));
+    const double mod = hypot(a, b);
+    const double c_ = mod == 0 ? 1.0 : a / mod, s_ = mod == 0 ? 0.0 : b / mod;
+    cs[j] = c_;
+    sn[j] = s_;
+    col[j] = mod;
+    gv[j + 1] = -s_ * gv[j];
+    gv[j] = c_ * gv[j];
+    flags[2] = (unsigned)(j + 1);
+    if (!(b > 0) || fabs(gv[j + 1]) <= tol * h[1]) flags[1] = 1u;
+}
+
+// y = R^{-1} g over the flags[2] columns in use (one thread); clears the
+// done flag for the next solve.
+__global__ void k_inner_backsolve(InnerLayout L, double* __restrict__ h, unsigned* __restrict__ flags) {
+    if (threadIdx.x != 0) return;
+    const int kk = (int)flags[2];
+    double* y = h + L.y();
+    const double* gv = h + L.g();
+    for (int i = kk - 1; i >= 0; --i) {
+        double acc = gv[i];
+        for (int q = i + 1; q < kk; ++q) acc -= h[L.h() + (long long)q * (L.S + 1) + i] * y[q];
+        const double d = h[L.h() + (long long)i * (L.S + 1) + i];
+        y[i] = d != 0 ? acc / d : 0.0;
+    }
+    flags[1] = 0u;
 }
 
 // flag[0] |= any non-finite value

@@ -91,7 +91,8 @@ __global__ void k_wall_rhs(GridP g, const double* __restrict__ rho_ext, int ex, 
 // wall node E_x(0) - E_x(1), E_y(0), E_z(0); identity rows on nodes nx - 2
 // and nx - 1.
 template <typename T>
-__global__ void k_wall_rows(GridP g, const T* __restrict__ x, T* __restrict__ y) {
+__global__ void k_wall_rows(GridP g, const T* __restrict__ x, T* __restrict__ y, const unsigned* __restrict__ skip) {
+    if (skip && *skip) return;
     const long long N = g.N;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)g.ny * g.nz;
          e += (long long)gridDim.x * blockDim.x) {

@@ -426,15 +426,21 @@ def stiff_solve(a, w):
     _, mu, _, rhs = sim.download_moments()
     plain_opts = P.solve_opts(P.GMRES_RESTARTED, restart=30, max_iter=3000, tol=1e-8)
     learned_opts = P.solve_opts(P.FGMRES_LEARNED, restart=30, max_iter=3000, tol=1e-8)
-    sim.maxwell_solve(mu, rhs, plain_opts)   # warm-up of both paths
+    mixed_opts = P.solve_opts(P.FGMRES_MIXED, restart=30, max_iter=3000, tol=1e-8, inner=a.mixed_inner)
+    sim.maxwell_solve(mu, rhs, plain_opts)   # warm-up of all three paths
     sim.maxwell_solve(mu, rhs, learned_opts)
+    sim.maxwell_solve(mu, rhs, mixed_opts)
     _, ip = sim.maxwell_solve(mu, rhs, plain_opts)
     _, il = sim.maxwell_solve(mu, rhs, learned_opts)
+    _, im = sim.maxwell_solve(mu, rhs, mixed_opts)
     sim.close()
     return {"system": f"first implicit step, {nx}x{ny}x{nz}, dt = 2 (K/dx^2 = 4.2)", "tol": 1e-8,
             "plain": {k: ip[k] for k in ("iterations", "restarts", "rel_residual", "seconds")},
             "learned": {k: il[k] for k in ("iterations", "restarts", "used_fallback", "rel_residual", "seconds")},
             "speedup": ip["seconds"] / il["seconds"] if il["seconds"] > 0 else None,
+            "mixed": {"inner": a.mixed_inner, **{k: im[k] for k in ("iterations", "restarts", "used_fallback",
+                                                                     "rel_residual", "seconds")},
+                      "speedup": ip["seconds"] / im["seconds"] if im["seconds"] > 0 else None},
             "train": {"box": [64, 64, 16], "steps": tr["steps"], "seconds": tr["seconds"],
                       "first_loss": tr["first_loss"], "last_loss": tr["last_loss"]}}
 

@@ -310,7 +310,8 @@ pic_status buneman_steps(pic_ctx* ctx, int nsteps) {
             }
             {
                 Phase ph(ctx, PIC_PHASE_ASSEMBLE, 1);
-                PK<T>::assemble_j(s, g, ctx->tg, ctx->ts, (const double*)ctx->Jpart, ctx->Jfix, ctx->J);
+                PK<T>::assemble_j(s, g, ctx->tg, ctx->ts, (const double*)ctx->Jpart, ctx->Jfix, ctx->J,
+                                  1.0 / (double)PK<T>::fixed_scale(g, S));
             }
         } else {
             {

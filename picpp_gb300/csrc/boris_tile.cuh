@@ -252,7 +252,8 @@ __device__ __forceinline__ void stage_particle(ChunkBuf<TP>* buf, const PartView
 template <typename TP, typename TF, int CT, bool kWall>
 __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_deposit_tile(GridP g, TileGeom t, TileShape s, SpeciesSet<TP> S,
                                                                        const TF* __restrict__ E, const TF* __restrict__ B,
-                                                                       double* __restrict__ Jpart, float fx_scale) {
+                                                                       double* __restrict__ Jpart, float fx_scale,
+                                                                       double inv_dt) {
     constexpr bool kFixed = sizeof(TP) == sizeof(float);   // FP32 particles: fixed-point block
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int fx = CT ? CT + 4 : s.fx, fy = CT ? CT + 4 : s.fy, fz = CT ? CT + 4 : s.fz;
@@ -275,9 +276,10 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
     const int T3 = tx * ty * tz;
     const long long N = g.N;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const TP dt = TP(g.dt), idt = TP(1.0 / g.dt);
+    // reciprocals from the host (no FP64 division per thread)
+    const TP dt = TP(g.dt), idt = TP(inv_dt);
     const TP dx = TP(g.dx), dy = TP(g.dy), dz = TP(g.dz);
-    const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
+    const TP idx = TP(g.idx), idy = TP(g.idy), idz = TP(g.idz);
     const TP vol = dx * dy * dz;
     const int ey = CT ? 1 : (g.y3 ? 1 : 0), ez = CT ? 1 : (g.z3 ? 1 : 0);
     const int fsy = ey ? fx : 0, fsz = ez ? fx * fy : 0;
@@ -482,13 +484,12 @@ __global__ void __launch_bounds__(kTileThreads, PIC_TILE_MIN_BLOCKS) k_push_depo
         __syncthreads();
         double* dst = Jpart + (long long)tile * 3 * JC;
         if (kFixed) {
-            // the exact block sum: |v| < 2^53 and a power-of-two scale, so the
-            // FP64 partial is the fixed-point value itself
-            const double inv = 1.0 / (double)fx_scale;
-            for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) {
-                const long long v = (long long)sHi[e] * 4294967296ll + (long long)sLo[e];
-                dst[e] = (double)v * inv;
-            }
+            // the exact block sums as 64-bit integers (k_assemble_j adds
+            // them exactly and scales once per cell): integer operations
+            // only, nothing on the FP64 pipe
+            long long* dsti = reinterpret_cast<long long*>(dst);
+            for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x)
+                dsti[e] = (long long)sHi[e] * 4294967296ll + (long long)sLo[e];
         } else {
             for (long long e = threadIdx.x; e < 3 * JC; e += blockDim.x) dst[e] = sJ[e];
         }
@@ -508,7 +509,7 @@ template <typename TP, typename TF>
 __global__ void __launch_bounds__(256) k_push_deposit_deferred(GridP g, SpeciesSet<TP> S, const TF* __restrict__ E,
                                                                const TF* __restrict__ B, double* __restrict__ Jfix) {
     const TP dt = TP(g.dt);
-    const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
+    const TP idx = TP(g.idx), idy = TP(g.idy), idz = TP(g.idz);
     const TP vol = TP(g.dx) * TP(g.dy) * TP(g.dz);
     for (int sp = 0; sp < S.ns; ++sp) {
         const PartView<TP> P = S.p[sp];
@@ -562,10 +563,14 @@ __global__ void __launch_bounds__(256) k_push_deposit_deferred(GridP g, SpeciesS
 }
 
 // J[c] = Jfix[c] + sum of every tile partial that covers cell c, tiles and
-// periodic images visited in a fixed order (deterministic, FP64).
+// periodic images visited in a fixed order (deterministic).  FP32 particles:
+// the partials are 64-bit fixed-point integers, summed exactly and scaled by
+// inv_scale (a power of two) once; FP64 particles: FP64 partials.
 template <typename TP>
 __global__ void __launch_bounds__(256) k_assemble_j(GridP g, TileGeom t, TileShape s, const double* __restrict__ Jpart,
-                                                    const double* __restrict__ Jfix, double* __restrict__ J) {
+                                                    const double* __restrict__ Jfix, double* __restrict__ J,
+                                                    double inv_scale) {
+    constexpr bool kFixed = sizeof(TP) == sizeof(float);
     const long long JC = s.jcells;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
          c += (long long)gridDim.x * blockDim.x) {
@@ -599,16 +604,28 @@ __global__ void __launch_bounds__(256) k_assemble_j(GridP g, TileGeom t, TileSha
             }
         }
         double acc[3] = {Jfix[c], Jfix[g.N + c], Jfix[2 * g.N + c]};
+        long long iacc[3] = {0, 0, 0};
         for (int a = 0; a < cnt[0]; ++a)
             for (int b = 0; b < cnt[1]; ++b)
                 for (int d = 0; d < cnt[2]; ++d) {
                     long long tile = ((long long)cand_t[2][d] * t.nty + cand_t[1][b]) * t.ntx + cand_t[0][a];
                     long long e = ((long long)cand_l[2][d] * s.jy + cand_l[1][b]) * s.jx + cand_l[0][a];
                     const double* src = Jpart + tile * 3 * JC;
-                    acc[0] += src[e];
-                    acc[1] += src[JC + e];
-                    acc[2] += src[2 * JC + e];
+                    if constexpr (kFixed) {
+                        const long long* srci = reinterpret_cast<const long long*>(src);
+                        iacc[0] += srci[e];
+                        iacc[1] += srci[JC + e];
+                        iacc[2] += srci[2 * JC + e];
+                    } else {
+                        acc[0] += src[e];
+                        acc[1] += src[JC + e];
+                        acc[2] += src[2 * JC + e];
+                    }
                 }
+        if constexpr (kFixed) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) acc[q] += (double)iacc[q] * inv_scale;
+        }
         J[c] = acc[0]; J[g.N + c] = acc[1]; J[2 * g.N + c] = acc[2];
     }
 }

@@ -42,8 +42,11 @@ struct PK {
     static void push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh,
                                    const SpeciesSet<T>& S, const void* E, const void* B, double* Jpart, double* Jfix,
                                    int grid, size_t smem);
+    // J from the tile partials and Jfix; inv_scale = 1 / fixed_scale for FP32
+    // particles (integer partials), unused for FP64
     static void assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const double* Jpart,
-                           const double* Jfix, double* J);
+                           const double* Jfix, double* J, double inv_scale);
+    static float fixed_scale(const GridP& g, const SpeciesSet<T>& S);
     static size_t tile_smem_bytes(const TileShape& sh);
     static void implicit_deposit(cudaStream_t s, const GridP& g, PartView<T> p, double q, double m, double w,
                                  const double* E, const double* B, double* J, double* mu, double* rho, double* Pi,

@@ -199,34 +199,42 @@ void PK<T>::push_deposit_tiled(cudaStream_t s, const GridP& g, const TileGeom& t
     }
     const bool cube8 = t.tx == 8 && t.ty == 8 && t.tz == 8 && g.y3 && g.z3 && sh.fx == 12 && sh.fy == 12 &&
                        sh.fz == 12 && sh.jx == 12 && sh.jy == 12 && sh.jz == 12;
-    // fixed-point scale of the FP32 current block: the power of two with
-    // max_species |q w / V| * scale <= 2^35 (every zigzag term is bounded by
-    // q w / V because |v| < c = 1; a run total of up to 32 terms stays below
-    // 2^40 and 2^23 such totals per entry below 2^63)
-    double fmax = 0;
-    for (int q = 0; q < S.ns; ++q)
-        fmax = std::max(fmax, std::fabs((double)S.q[q] * (double)S.w[q] / (g.dx * g.dy * g.dz)));
-    const float fx_scale = fmax > 0 ? (float)std::ldexp(1.0, 35 - (int)std::ceil(std::log2(fmax))) : 1.0f;
+    const float fx_scale = fixed_scale(g, S);
+    const double inv_dt = 1.0 / g.dt;
     // a wall box runs its own instantiation (run-time tile shape)
     if (g.wall)
         k_push_deposit_tile<T, T, 0, true><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
-                                                                           fx_scale);
+                                                                           fx_scale, inv_dt);
     else if (cube8)
         k_push_deposit_tile<T, T, 8, false><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
-                                                                            fx_scale);
+                                                                            fx_scale, inv_dt);
     else
         k_push_deposit_tile<T, T, 0, false><<<grid, kTileThreads, smem, s>>>(g, t, sh, S, (const T*)E, (const T*)B, Jpart,
-                                                                            fx_scale);
+                                                                            fx_scale, inv_dt);
     // the particles it left over: one thread per mask word
     long long words = 1;
     for (int q = 0; q < S.ns; ++q) words = std::max(words, (S.p[q].n + 31) / 32 + 1);
     k_push_deposit_deferred<T, T><<<grid_for(words, 256), 256, 0, s>>>(g, S, (const T*)E, (const T*)B, Jfix);
 }
 
+// Fixed-point scale of the FP32 current block: the power of two with
+// max_species |q w / V| * scale <= 2^35 (every zigzag term is bounded by
+// q w / V because |v| < c = 1, so a run total of up to 32 terms stays below
+// 2^40; a tile entry takes at most two terms per particle of the tile, and
+// a cell's sum of at most 27 tile partials stays below 2^63 up to about five
+// million particles per tile).
+template <typename T>
+float PK<T>::fixed_scale(const GridP& g, const SpeciesSet<T>& S) {
+    double fmax = 0;
+    for (int q = 0; q < S.ns; ++q)
+        fmax = std::max(fmax, std::fabs((double)S.q[q] * (double)S.w[q] / (g.dx * g.dy * g.dz)));
+    return fmax > 0 ? (float)std::ldexp(1.0, 35 - (int)std::ceil(std::log2(fmax))) : 1.0f;
+}
+
 template <typename T>
 void PK<T>::assemble_j(cudaStream_t s, const GridP& g, const TileGeom& t, const TileShape& sh, const double* Jpart,
-                       const double* Jfix, double* J) {
-    k_assemble_j<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, t, sh, Jpart, Jfix, J);
+                       const double* Jfix, double* J, double inv_scale) {
+    k_assemble_j<T><<<grid_for(g.N, 256), 256, 0, s>>>(g, t, sh, Jpart, Jfix, J, inv_scale);
 }
 
 template <typename T>

@@ -42,12 +42,16 @@ def _args():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--grid", type=int, nargs=3, default=[128, 128, 128])
     p.add_argument("--ppc", type=int, default=16)
-    p.add_argument("--sort-every", type=int, default=4)
+    # sorting every 5 steps: 3.15 ms per step at 128^3 against 3.36, 3.20, 3.11
+    # and 3.15 every 3, 4, 6 and 8 steps (6 is faster but would put 3 or 4
+    # sorts into 20 timed steps depending on the phase)
+    p.add_argument("--sort-every", type=int, default=5)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--implicit-grid", type=int, nargs=3, default=[256, 256, 64])
     p.add_argument("--implicit-ppc", type=int, default=64)
     p.add_argument("--implicit-steps", type=int, default=200, help="steps of the implicit run (2 untimed)")
+    p.add_argument("--implicit-sort-every", type=int, default=1, help="sort cadence of the implicit run")
     p.add_argument("--drift-steps", type=int, default=500, help="steps of the FP32-vs-FP64 explicit energy run")
     p.add_argument("--no-energy", action="store_true")
     p.add_argument("--shock-grid", type=int, nargs=3, default=[4096, 256, 4])
@@ -88,7 +92,7 @@ def implicit_section(a):
     # sorting every step: the deposit sums the lanes of one cell per warp
     # pass, and the beams move about a cell per step (with a sort every
     # other step the moment phase measured 362 ms instead of 141 ms)
-    sim = P.GpuSimulation(box, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=1)
+    sim = P.GpuSimulation(box, P.IMPLICIT, particle_real=P.F32, pressure_compat=0, sort_every=a.implicit_sort_every)
     N = box.ncells
     sim.add_species(-1.0, 1.0, w, N * ppc)
     sim.add_species(1.0, 25.0, w, N * ppc)

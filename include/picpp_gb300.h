@@ -365,8 +365,8 @@ pic_status pic_profile(pic_ctx* ctx, int enable, double* phase_ms, long* launche
  * the library keeps until exit and that every call shares, so calls that
  * overlap on the GPU race.  The first call on a device looks that array's
  * device address up (cudaGetSymbolAddress) with the device current and
- * caches it; make it before any stream capture, and make no call on a
- * device after a cudaDeviceReset of it.  Limit: at most
+ * caches it; make no call on a device after a cudaDeviceReset of it.
+ * Limit: at most
  * PIC_NOALLOC_MAX_SPECIES species (more returns PIC_ERR_ARG) and fewer than
  * 2^31 cells.
  * E, B: 3*nx*ny*nz FP64 device arrays (either may be NULL); per species s,

@@ -19,8 +19,7 @@
 // Host code cannot use &g_energy_scratch as a device address (the host-side
 // symbol is only a stand-in).  The first call on a device looks the device
 // address up with cudaGetSymbolAddress while that device is current and
-// caches it; make that first call before any stream capture begins, since
-// the lookup may initialise the module.  cudaDeviceReset unloads the module,
+// caches it (the lookup may initialise the module).  cudaDeviceReset unloads the module,
 // so the cached address is not valid after a reset: do not call this entry
 // point on a device that was reset since its first call.
 #include <cmath>

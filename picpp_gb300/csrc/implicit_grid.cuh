@@ -54,7 +54,9 @@ __device__ __forceinline__ void div_pi(const GridP& g, int i, int j, int k, PTf 
             tA = (PT(2, col, i, j, k) + PT(2, col, i, j - 1, k) + PT(2, col, i - 1, j, k) + PT(2, col, i - 1, j - 1, k)) * 0.25;
             boA = (PT(2, col, i, j, k - 1) + PT(2, col, i, j - 1, k - 1) + PT(2, col, i - 1, j, k - 1) + PT(2, col, i - 1, j - 1, k - 1)) * 0.25;
         }
-        out[col] = ((rA - lA) / g.dx) + ((bA - fA) / g.dy) + ((tA - boA) / g.dz);
+        // reciprocals from the host: a division is a dozen operations on
+        // this GPU's 1/64-rate FP64 pipe
+        out[col] = ((rA - lA) * g.idx) + ((bA - fA) * g.idy) + ((tA - boA) * g.idz);
     }
 }
 
@@ -72,7 +74,7 @@ __device__ __forceinline__ double div_j(const GridP& g, int i, int j, int k, JFf
         rZ = (JF(2, i + 1, j, k + 1) + JF(2, i, j, k + 1) + JF(2, i, j + 1, k + 1) + JF(2, i + 1, j + 1, k + 1)) * 0.25;
         lZ = (JF(2, i + 1, j, k) + JF(2, i, j, k) + JF(2, i, j + 1, k) + JF(2, i + 1, j + 1, k)) * 0.25;
     }
-    return ((rX - lX) / g.dx) + ((rY - lY) / g.dy) + ((rZ - lZ) / g.dz);
+    return ((rX - lX) * g.idx) + ((rY - lY) * g.idy) + ((rZ - lZ) * g.idz);
 }
 
 __device__ __forceinline__ int gphys(int r, int n) { return n > 1 ? wrap_any(r - 2, n) : 0; }
@@ -162,12 +164,13 @@ __global__ void k_j_minus_divpi(GridP g, const double* __restrict__ Pi, const do
 // Periodic layout: rho_ext from rho-hat -= theta dt div(J-hat).
 __global__ void k_rho_ext_periodic(GridP g, const double* __restrict__ J, const double* __restrict__ rho,
                                    double* __restrict__ rho_ext, int ex, int ey, int ez) {
-    const long long EN = (long long)ex * ey * ez;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < EN;
-         t += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(t % ex);
-        long long q = t / ex;
-        int j = (int)(q % ey), k = (int)(q / ey);
+    // 32-bit index arithmetic (the extended box has fewer than 2^31 cells;
+    // 64-bit divisions are long integer sequences)
+    const unsigned EN = (unsigned)ex * ey * ez;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < EN; t += gridDim.x * blockDim.x) {
+        const unsigned q = t / (unsigned)ex;
+        const int i = (int)(t - q * (unsigned)ex);
+        const int k = (int)(q / (unsigned)ey), j = (int)(q - (unsigned)k * (unsigned)ey);
         int ii = g.nx > 1 ? i - 1 : 0, jj = g.ny > 1 ? j - 1 : 0, kk = g.nz > 1 ? k - 1 : 0;
         auto JF = [&](int d, int a, int b, int c) -> double { return J[d * g.N + linw(g, a, b, c)]; };
         double div = div_j(g, ii, jj, kk, JF);
@@ -181,6 +184,7 @@ __global__ void __launch_bounds__(256) k_maxwell_rhs(GridP g, const double* __re
                                                      const double* __restrict__ J, const double* __restrict__ rho_ext,
                                                      int ex, int ey, double* __restrict__ rhs) {
     const double cf = g.cfix, cf2 = g.cfix * g.cfix, td = g.theta * g.dt;
+    const double gfac = cf2 * g.theta * g.theta * g.dt * g.dt * 4 * kPi;   // the grad rho term's factor, once
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
          c += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
@@ -202,19 +206,18 @@ __global__ void __launch_bounds__(256) k_maxwell_rhs(GridP g, const double* __re
             if (!g.z3) { BrZ[d] = 0; BlZ[d] = 0; }
         }
         double rot[3];
-        rot[0] = (BrY[2] - BlY[2]) / g.dy - (BrZ[1] - BlZ[1]) / g.dz;
-        rot[1] = (BrZ[0] - BlZ[0]) / g.dz - (BrX[2] - BlX[2]) / g.dx;
-        rot[2] = (BrX[1] - BlX[1]) / g.dx - (BrY[0] - BlY[0]) / g.dy;
+        rot[0] = (BrY[2] - BlY[2]) * g.idy - (BrZ[1] - BlZ[1]) * g.idz;
+        rot[1] = (BrZ[0] - BlZ[0]) * g.idz - (BrX[2] - BlX[2]) * g.idx;
+        rot[2] = (BrX[1] - BlX[1]) * g.idx - (BrY[0] - BlY[0]) * g.idy;
         double dRX = (RH(i, j, k) + RH(i, pj, k) + RH(i, j, pk) + RH(i, pj, pk)) * 0.25;
         double dLX = (RH(pi_, j, k) + RH(pi_, pj, k) + RH(pi_, j, pk) + RH(pi_, pj, pk)) * 0.25;
         double dRY = (RH(i, j, k) + RH(pi_, j, k) + RH(i, j, pk) + RH(pi_, j, pk)) * 0.25;
         double dLY = (RH(i, pj, k) + RH(pi_, pj, k) + RH(i, pj, pk) + RH(pi_, pj, pk)) * 0.25;
         double dRZ = (RH(i, j, k) + RH(i, pj, k) + RH(pi_, j, k) + RH(pi_, pj, k)) * 0.25;
         double dLZ = (RH(i, j, pk) + RH(i, pj, pk) + RH(pi_, j, pk) + RH(pi_, pj, pk)) * 0.25;
-        double grad[3] = {(dRX - dLX) / g.dx, (dRY - dLY) / g.dy, (dRZ - dLZ) / g.dz};
+        double grad[3] = {(dRX - dLX) * g.idx, (dRY - dLY) * g.idy, (dRZ - dLZ) * g.idz};
         for (int d = 0; d < 3; ++d)
-            rhs[d * g.N + c] = E[d * g.N + c] + (rot[d] * cf - (J[d * g.N + c] * 4 * kPi)) * td -
-                               (grad[d] * cf2 * g.theta * g.theta * g.dt * g.dt * 4 * kPi);
+            rhs[d * g.N + c] = E[d * g.N + c] + (rot[d] * cf - (J[d * g.N + c] * 4 * kPi)) * td - (grad[d] * gfac);
     }
 }
 

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(256) k_boris_push(GridP g, PartView<TP> p, TP 
                                                     const TF* __restrict__ E, const TF* __restrict__ B) {
     const TP dt = TP(g.dt);
     const TP beta = q * dt / (TP(2) * m);   // Particle::beta (PIC++/particle.cpp:47)
-    const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
+    const TP idx = TP(g.idx), idy = TP(g.idy), idz = TP(g.idz);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < p.n;
          n += (long long)gridDim.x * blockDim.x) {
         int cell = p.cell[n];
@@ -170,7 +170,7 @@ template <typename TP, typename Sink>
 __device__ __forceinline__ void zigzag_terms(const GridP& g, TP fcd, TP ox, TP oy, TP oz,
                                              const TP v[3], Sink&& sink, bool wall_cell = false) {
     const TP dt = TP(g.dt), dx = TP(g.dx), dy = TP(g.dy), dz = TP(g.dz);
-    const TP idx = TP(1.0 / g.dx), idy = TP(1.0 / g.dy), idz = TP(1.0 / g.dz);
+    const TP idx = TP(g.idx), idy = TP(g.idy), idz = TP(g.idz);
     TP X = ox * dx, Y = oy * dy, Z = oz * dz;
     TP PX, PY, PZ, RX, RY, RZ;
     int si, sj, sk;

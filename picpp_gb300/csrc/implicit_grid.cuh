@@ -460,12 +460,13 @@ __global__ void __launch_bounds__(256) k_maxwell_apply_t(GridP g, OpCoef oc, con
 __global__ void __launch_bounds__(256) k_field_update(GridP g, const double* __restrict__ Et, const double* __restrict__ E,
                                                       const double* __restrict__ B, double* __restrict__ En,
                                                       double* __restrict__ Bn, int doE, int doB) {
+    const double itheta = 1.0 / g.theta;   // once per thread: divisions are slow on the FP64 pipe
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.N;
          c += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         decode(g, (int)c, i, j, k);
         if (doE)
-            for (int d = 0; d < 3; ++d) En[d * g.N + c] = (Et[d * g.N + c] - E[d * g.N + c] * (1 - g.theta)) / g.theta;
+            for (int d = 0; d < 3; ++d) En[d * g.N + c] = (Et[d * g.N + c] - E[d * g.N + c] * (1 - g.theta)) * itheta;
         if (!doB) continue;
         auto EF = [&](int d, int a, int b, int cc) -> double { return Et[d * g.N + linw(g, a, b, cc)]; };
         double rX[3], lX[3], rY[3], lY[3], rZ[3], lZ[3];
@@ -480,9 +481,9 @@ __global__ void __launch_bounds__(256) k_field_update(GridP g, const double* __r
             if (!g.z3) { rZ[d] = 0; lZ[d] = 0; }
         }
         double rot[3];
-        rot[0] = (rY[2] - lY[2]) / g.dy - (rZ[1] - lZ[1]) / g.dz;
-        rot[1] = (rZ[0] - lZ[0]) / g.dz - (rX[2] - lX[2]) / g.dx;
-        rot[2] = (rX[1] - lX[1]) / g.dx - (rY[0] - lY[0]) / g.dy;
+        rot[0] = (rY[2] - lY[2]) * g.idy - (rZ[1] - lZ[1]) * g.idz;
+        rot[1] = (rZ[0] - lZ[0]) * g.idz - (rX[2] - lX[2]) * g.idx;
+        rot[2] = (rX[1] - lX[1]) * g.idx - (rY[0] - lY[0]) * g.idy;
         for (int d = 0; d < 3; ++d) Bn[d * g.N + c] = B[d * g.N + c] - rot[d] * (g.cfix * g.dt);
     }
 }

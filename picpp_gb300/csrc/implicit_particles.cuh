@@ -239,7 +239,7 @@ __device__ __forceinline__ MoverConst<T> mover_const(const GridP& g, double q, d
     c.mm = T(m);
     c.dxT = T(g.dx);
     c.redt = T((1.0 - g.eta) * g.dt);
-    c.id[0] = T(1.0 / g.dx); c.id[1] = T(1.0 / g.dy); c.id[2] = T(1.0 / g.dz);
+    c.id[0] = T(g.idx); c.id[1] = T(g.idy); c.id[2] = T(g.idz);
     c.nn[0] = g.nx; c.nn[1] = g.ny; c.nn[2] = g.nz;
     return c;
 }

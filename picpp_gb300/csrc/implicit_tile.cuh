@@ -657,7 +657,7 @@ __global__ void __launch_bounds__(kMoverThreads, 2) k_implicit_push_tile(GridP g
     const int nsx = ax ? 1 : 0, nsy = ay ? mb.nbx : 0, nsz = az ? mb.nbx * mb.nby : 0;
     const int csx = ax ? 1 : 0, csy = ay ? mb.cbx : 0, csz = az ? mb.cbx * mb.cby : 0;
     const T dt = T(g.dt), eta = T(g.eta), edt = T(g.eta * g.dt);
-    const T id[3] = {T(1.0 / g.dx), T(1.0 / g.dy), T(1.0 / g.dz)};
+    const T id[3] = {T(g.idx), T(g.idy), T(g.idz)};
     const int nn[3] = {g.nx, g.ny, g.nz};
     const T dxT = T(g.dx);
     const T redt = T((1.0 - g.eta) * g.dt);

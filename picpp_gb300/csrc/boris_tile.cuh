@@ -14,17 +14,20 @@
 //      point (in the old cell) and the one from the relay point to the new
 //      position (in the new cell).  Lanes holding the same cell (particles
 //      are sorted by cell) sum each segment's 12 values with a segmented
-//      shuffle reduction, and the first lane of each run adds the totals to a
-//      shared-memory current block (tile plus two cells of halo).  FP32
-//      particles: the block is exact 64-bit fixed point in two 32-bit words
-//      per entry, added with native 32-bit integer shared atomics (FP32 shared
-//      atomics are compare-and-swap loops that collapse under address
-//      conflicts); the block sums are exact and order-independent.  FP64
-//      particles: FP64 shared atomics;
-//   3. writes the block, unreduced, to a per-tile FP64 partial buffer (for
-//      FP32 particles the exact fixed-point sums).
+//      shuffle reduction, and the run totals go into a shared-memory current
+//      block (tile plus two cells of halo).  FP32 particles: the block is
+//      exact 64-bit fixed point in two 32-bit words per entry, added with
+//      native 32-bit integer shared atomics (FP32 shared atomics are
+//      compare-and-swap loops that collapse under address conflicts), the
+//      adds of a warp's run heads spread over its lanes; the block sums are
+//      exact and order-independent.  FP64 particles: FP64 shared atomics.
+//      Each warp copies its next chunk of particles into shared memory with
+//      cp.async while it pushes the current one;
+//   3. writes the block, unreduced, to a per-tile partial buffer (for FP32
+//      particles the exact fixed-point sums as 64-bit integers).
 // k_assemble_j then sums the partials of every cell in a fixed order into
-// the FP64 current grid: no global floating-point atomics on the fast path.
+// the FP64 current grid (FP32 particles: exact integer sums, scaled once):
+// no global floating-point atomics on the fast path.
 // A particle more than one cell outside its tile, or whose zigzag segments
 // leave the tile's current block, is left to k_push_deposit_deferred: the
 // fused kernel sets its bit in a per-species mask and the deferred pass

@@ -157,6 +157,44 @@ def test_wall_steps_with_injection_match_oracle(pg, real, sort_every):
     sim.close()
 
 
+def test_wall_far_drift_takes_the_mover_deferred_pass(pg):
+    """One-cell tiles and a sort every fifth step: after a few steps most
+    particles lie more than the two-cell halo away from their tile, so the
+    tiled mover leaves them to its deferred pass (the wall rules of the
+    untiled mover: reflection at the wall, escape at the open boundary).
+    FP64 fields and particles after 5 steps against the oracle."""
+    st = _flow_state(seed=47)
+    er, br = st.e_right, st.b_right
+    sim = pg.GpuSimulation(st.box, pg.IMPLICIT, particle_real=1, pressure_compat=0, sort_every=5, tile=(1, 1, 1),
+                           boundary_x=pg.BOUNDARY_WALL_OPEN, e_right=er, b_right=br)
+    sim.upload_state(st)
+    g = O.make_grid(st.box, pressure_compat=0, wall_x=1, e_right=er, b_right=br)
+    spo = copy_species(st.species)
+    for sp in spo:
+        sp["id"] = np.arange(len(sp["cell"]), dtype=np.int32)
+    E, B = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()
+    for _ in range(5):
+        sim.implicit_step(pg.solve_opts(pg.GMRES_REFERENCE))
+        O.implicit_step(g, spo, E, B)
+    Eg, Bg, _ = sim.download_fields()
+    b = st.box
+    assert rel_err(phys(Eg, b, 3, False), phys(E, b, 3, False)) < TOL64
+    assert rel_err(phys(Bg, b, 3, True), phys(B, b, 3, True)) < TOL64
+    escaped = 0
+    for s in range(len(spo)):
+        got = by_id(sim.download_particles(s))
+        ref = by_id({k: v for k, v in spo[s].items() if isinstance(v, np.ndarray)})
+        escaped += len(st.species[s]["cell"]) - len(ref["id"])
+        assert np.array_equal(got["id"], ref["id"])
+        xg, _, _ = I.positions(b, got)
+        xr, _, _ = I.positions(b, ref)
+        assert np.abs(xg - xr).max() < 1e-11 * b.dx
+        for k in ("px", "py", "pz"):
+            assert rel_err(got[k], ref[k]) < TOL64
+    assert escaped > 0
+    sim.close()
+
+
 def test_wall_rejects_particles_in_ghost_columns_and_other_setups(pg):
     st = _flow_state()
     er, br = st.e_right, st.b_right

@@ -7,7 +7,7 @@
 // 164-259, 266-409) phase by phase instead of calling simulate(), so that the
 // state can be loaded from a file (no text decks, no srand(time)), the time
 // step is not clamped by updateDeltaT (simulation.cpp:1065-1078) and no
-// output files are written.
+// output files are written.  The wall time of the step loop goes to stdout.
 //
 // Input file (little endian):
 //   int32[10]  solver (0 Buneman, 1 implicit), nx, ny, nz, nspecies, steps,

@@ -124,6 +124,25 @@ def test_oracle_density_moments_match_reference(name):
     assert rel_err(rho, x["rho"]) < 1e-13
 
 
+def test_wall_density_fold_keeps_totals_and_empties_the_ghosts():
+    """The wall box's density pass moves the ghost columns' deposits into the
+    first and last physical cells: the ghost columns end empty, and every
+    particle's weight is still counted once (its cell weights sum to one)."""
+    st = I.shock_plasma(12, 6, 5, ppc=(3, 3, 2), flow_gamma=3.0, theta_e=0.3, seed=71)
+    b = st.box
+    g = O.make_grid(b, wall_x=1, e_right=st.e_right, b_right=st.b_right)
+    conc, en, vel, rho = O.density_moments(g, copy_species(st.species))
+    vol = b.dx * b.dy * b.dz
+    for s, sp in enumerate(st.species):
+        c = conc[s].reshape(b.nz, b.ny, b.nx)
+        assert np.all(c[..., b.nx - 2:] == 0.0)
+        assert np.all(en[s].reshape(b.nz, b.ny, b.nx)[..., b.nx - 2:] == 0.0)
+        assert np.all(vel[s].reshape(3, b.nz, b.ny, b.nx)[..., b.nx - 2:] == 0.0)
+        assert abs(c.sum() * vol / (sp["w"] * len(sp["cell"])) - 1.0) < 1e-12
+    q = sum(sp["q"] * sp["w"] * len(sp["cell"]) for sp in st.species)
+    assert abs(rho.sum() * vol - q) < 1e-12 * sum(abs(sp["q"]) * sp["w"] * len(sp["cell"]) for sp in st.species)
+
+
 @pytest.mark.parametrize("name", golden_names("wall"))
 def test_wall_moments_and_solve_match_reference(name):
     """Conductor wall at x = 0, open boundary at x = (nx - 2) dx: the first

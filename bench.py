@@ -856,15 +856,17 @@ def run_gb300(a):
     e2e_val = replica_value(npart, world, e2e_ms)
 
     sim.close()
+    # the sections after the timed replicas describe one GPU and only rank 0
+    # reports them: the other ranks release their GPUs here
     energy = None
-    if not a.no_energy:
+    if not a.no_energy and rank == 0:
         energy = energy_section(a, st)
     del st
     imp = None
-    if not a.no_implicit:
+    if not a.no_implicit and rank == 0:
         imp = implicit_section(a)
     shock = None
-    if not a.no_shock:
+    if not a.no_shock and rank == 0:
         shock = shock_section(a)
     if rank == 0:
         cpu = None

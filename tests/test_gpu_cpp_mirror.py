@@ -20,7 +20,7 @@ PKG = os.path.join(ROOT, "picpp_gb300")
 
 
 @pytest.fixture(scope="module")
-def driver(tmp_path_factory):
+def caller_exe(tmp_path_factory):
     import torch
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -35,7 +35,7 @@ def driver(tmp_path_factory):
     return exe
 
 
-def run(driver, tmp_path, st, solver, real, steps):
+def run(caller_exe, tmp_path, st, solver, real, steps):
     box = st.box
     N = box.ncells
     fin, fout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
@@ -53,7 +53,7 @@ def run(driver, tmp_path, st, solver, real, steps):
             np.arange(n, dtype="<i4").tofile(f)
         np.asarray(st.E, "<f8").tofile(f)
         np.asarray(st.B, "<f8").tofile(f)
-    r = subprocess.run([driver, fin, fout], capture_output=True, text=True)
+    r = subprocess.run([caller_exe, fin, fout], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     raw = open(fout, "rb").read()
     pos = 0
@@ -87,10 +87,10 @@ def check_particles(box, got, ref, tol_p, tol_x):
         assert rel_err(got[k], ref[k]) <= tol_p
 
 
-def test_cpp_buneman_step_loop_matches_oracle(driver, tmp_path):
+def test_cpp_buneman_step_loop_matches_oracle(caller_exe, tmp_path):
     st = I.buneman_plasma(8, 8, 8, ppc=3, seed=51)
     steps = 3
-    E, B, got = run(driver, tmp_path, st, 0, 1, steps)
+    E, B, got = run(caller_exe, tmp_path, st, 0, 1, steps)
     g = O.make_grid(st.box)
     sp = copy_species(st.species)
     Eo, Bo = st.E.copy(), st.B.copy()
@@ -102,10 +102,10 @@ def test_cpp_buneman_step_loop_matches_oracle(driver, tmp_path):
         check_particles(st.box, got[s], sp[s], 1e-11, 1e-10)
 
 
-def test_cpp_implicit_step_loop_matches_oracle(driver, tmp_path):
+def test_cpp_implicit_step_loop_matches_oracle(caller_exe, tmp_path):
     st = I.beams_plasma(8, 6, 5, ppc=2, beam_gamma=2.0, dt=0.2, seed=52)
     steps = 2
-    E, B, got = run(driver, tmp_path, st, 1, 1, steps)
+    E, B, got = run(caller_exe, tmp_path, st, 1, 1, steps)
     g = O.make_grid(st.box)
     sp = copy_species(st.species)
     Eo, Bo = st.E.reshape(-1).copy(), st.B.reshape(-1).copy()

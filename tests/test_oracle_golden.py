@@ -92,7 +92,7 @@ def test_counting_sort_is_stable_and_tile_major():
 def test_gmres_tiny_system_residual():
     """A small implicit operator solved to the reference's stopping rule; the
     true residual must be at the requested level (in the spirit of the
-    reference's printf GMRES driver, test/test.cpp:70-192, with an assert)."""
+    reference's printf GMRES test program, test/test.cpp:70-192, with an assert)."""
     box = I.Box(5, 5, 5, 0.5, 0.5, 0.5, 0.5)
     g = O.make_grid(box, gmres_max_iter=200)
     rng = np.random.default_rng(3)

@@ -125,7 +125,9 @@ typedef struct {
 } pic_solve_opts;
 
 typedef struct {
-    int iterations;          /* Krylov iterations performed                  */
+    int iterations;          /* Krylov iterations performed (the FP64 outer
+                                iterations for PIC_FGMRES_LEARNED and
+                                PIC_FGMRES_MIXED)                             */
     int restarts;
     int used_fallback;       /* 1 if the learned preconditioner was abandoned */
     double rel_residual;     /* final true |b - A x| / |b| (FP64)             */
